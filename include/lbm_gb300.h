@@ -1,0 +1,171 @@
+/*
+ * lbm_gb300.h -- C ABI of the GB300-native D2Q9 lattice-Boltzmann time step.
+ *
+ * Drop-in for the time loop of the serial solver of
+ * mate-szoke/ParallelLbmCranfield.  One context owns one domain resident on
+ * one GPU; the caller owns every host buffer.  No C++ types and no
+ * exceptions cross this boundary; every entry point returns an lbm_status.
+ *
+ * Reference interfaces replaced (file:line in the reference project):
+ *   lbm_create        CellIni + D2Q9Vars + MRTInitializer + the calloc of the
+ *                     cell array          serial/Iterate.c:176-228,
+ *                                         serial/include/CellFunctions.h:8-15
+ *   lbm_set_state     the initial F / U / V / Rho of the cells
+ *                                         serial/CellFunctions.c:147-150,252-267
+ *   lbm_step          one loop body per step: CollisionStep, UpdateF,
+ *                     StreamingStep, HandleBoundariesStep,
+ *                     UpdateMacroscopicStep, ComputeResiduals
+ *                                         serial/Iterate.c:263-307,
+ *                                         serial/include/Iterate.h:8-19,
+ *                                         serial/include/ComputeResiduals.h:6-7
+ *   lbm_get_fields    reads of Cells[i].Rho/U/V/F/METAF by the writers
+ *                                         serial/FileIO.c:298-427
+ *   lbm_destroy       free(Cells)         serial/Iterate.c:407
+ *   status codes      0 ok / 1 diverged / 2 file error of
+ *                                         cuda/cuda_step3/include/Iterate.h:59-64
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum lbm_status {
+  LBM_OK = 0,
+  LBM_DIVERGED = 1, /* NaN met by a residual/diagnostic (serial/ComputeResiduals.c:47-51) */
+  LBM_IO = 2,       /* file could not be read or written */
+  LBM_CUDA = 3,     /* a CUDA runtime call failed */
+  LBM_TIMEOUT = 4,  /* a bounded device wait gave up */
+  LBM_INVALID = 5,  /* bad argument or unsupported mesh */
+  LBM_NOMEM = 6     /* device or host allocation failed */
+} lbm_status;
+
+typedef enum lbm_precision {
+  LBM_FP64 = 0,    /* FP64 storage and arithmetic in the reference's order (parity mode) */
+  LBM_FP32 = 1,    /* FP32 storage and arithmetic */
+  LBM_FP16DEV = 2, /* FP16 storage of scaled (f_k - w_k rho0), FP32 arithmetic */
+  LBM_BF16DEV = 3  /* BF16 storage of scaled (f_k - w_k rho0), FP32 arithmetic */
+} lbm_precision;
+
+typedef enum lbm_pattern {
+  LBM_AB = 0, /* two population buffers, pull streaming */
+  LBM_AA = 1  /* one population buffer, in-place AA streaming */
+} lbm_pattern;
+
+/* Mesh in the reference's file format, already parsed:
+ *   nodes: num_nodes x 5 floats  (i, j, x, y, fluid)            Mesh/D2node.dat
+ *   conns: num_conns x 7 floats  (i, j, dir, type, x, y, id)    Mesh/BCconnectors.dat
+ * (serial/FileIO.c:39-44 and :116-133). */
+typedef struct lbm_mesh {
+  const float *nodes;
+  int32_t num_nodes;
+  const float *conns;
+  int32_t num_conns;
+} lbm_mesh;
+
+/* The SetUpData.ini switches of the time step (serial/FileIO.c:263-289) plus
+ * the GB300 storage choices. */
+typedef struct lbm_params {
+  float uavg, vavg, rho_ini, viscosity; /* ini lines 1-4 (parsed as float) */
+  int32_t inlet_profile;     /* 1 parabolic, 2 uniform Uavg */
+  int32_t collision_model;   /* 1 BGKW, 2 TRT, 3 MRT */
+  int32_t curved_boundaries; /* 1 curved (Bouzidi), 2 bounce-back of the streamed-in value */
+  int32_t outlet_profile;    /* 1 Zou-He velocity, 2 2nd-order extrapolation,
+                                3 none (as the serial code), 4 constant pressure rho_out */
+  int32_t drag_lift_id;      /* CalculateDragLift: boundary ID of the force surface, 0 = none */
+  int32_t precision;         /* lbm_precision */
+  int32_t pattern;           /* lbm_pattern */
+  int32_t device;            /* CUDA device ordinal */
+  double rho_out;            /* outlet density for outlet_profile 4 */
+  void *stream;              /* cudaStream_t to run on; NULL = a stream owned by the context */
+} lbm_params;
+
+typedef struct lbm_ctx lbm_ctx;
+
+/* Full-field diagnostics (FP64 reductions on the GPU), none of which the
+ * serial code computes correctly (its residual only visits cells 0..m-1). */
+typedef struct lbm_diagnostics {
+  int64_t iteration;   /* completed iterations */
+  double l2_full;      /* ||F - METAF||_2 over fluid cells (the CUDA/UPC variants' residual) */
+  double du_rel;       /* ||(u,v) - (u,v)_prev|| / ||(u,v)|| since the previous lbm_check */
+  double mass;         /* sum rho over fluid cells */
+  double momentum[2];  /* sum rho u, sum rho v */
+  double force[2];     /* momentum-exchange force on wall links of drag_lift_id cells */
+  double max_speed;    /* max |u| over fluid cells */
+} lbm_diagnostics;
+
+/* Library / status helpers. */
+const char *lbm_status_string(lbm_status s);
+/* Text of the last error seen by this thread, or "" */
+const char *lbm_last_error(void);
+
+lbm_status lbm_create(const lbm_mesh *mesh, const lbm_params *params, lbm_ctx **out);
+void lbm_destroy(lbm_ctx *ctx);
+/* Grid size n (x) and m (y) as CompDataNode derives them (serial/FileIO.c:193-194). */
+lbm_status lbm_get_dims(const lbm_ctx *ctx, int32_t *n, int32_t *m);
+
+/* State at the current iteration.  Arrays are cell-major, cells row-major
+ * (j * n + i), length n*m (f: 9*n*m).  f == NULL sets f = f_eq(rho, u, v);
+ * rho/u/v == NULL keep the values CellIni gave (rho_ini, Uo, 0).  The next
+ * collision uses rho/u/v as given, like the reference's first step. */
+lbm_status lbm_set_state(lbm_ctx *ctx, const double *f, const double *rho, const double *u,
+                         const double *v);
+
+/* Advance nsteps iterations.  For every step s (1-based within this call)
+ * with check_every > 0 and s % check_every == 0, 4 doubles are appended to
+ * residuals (may be NULL): the reference's L2_norm, L2_norm_weighted, Drag,
+ * Lift (serial/ComputeResiduals.c:6-51, including its index quirk).  The
+ * buffer must hold 4 * (nsteps / check_every) doubles.  Returns LBM_DIVERGED
+ * if any reported residual is NaN. */
+lbm_status lbm_step(lbm_ctx *ctx, int32_t nsteps, int32_t check_every, double *residuals);
+
+/* Fields after the last completed iteration; any pointer may be NULL.
+ * f and metaf are cell-major 9 per cell (F and METAF of the reference cells). */
+lbm_status lbm_get_fields(lbm_ctx *ctx, double *rho, double *u, double *v, double *f,
+                          double *metaf);
+
+/* Full-field FP64 diagnostics of the current state; also advances the
+ * du_rel reference fields.  LBM_DIVERGED if any sum is NaN. */
+lbm_status lbm_check(lbm_ctx *ctx, lbm_diagnostics *out);
+
+/* Completed iterations, device bytes held, bytes moved per node per step. */
+lbm_status lbm_get_info(const lbm_ctx *ctx, int64_t *iteration, int64_t *device_bytes,
+                        int32_t *bytes_per_node_step);
+
+/* Host-only view of the preprocessing lbm_create performs (no GPU needed).
+ * Per cell (row-major j*n+i, arrays of n*m, any pointer may be NULL):
+ *   cls:   0 solid, 1 fluid without boundary work, 3 fluid with boundary work
+ *   flags: for class-3 cells, bit k (0..8) = StreamLattice[k], bit 9+k =
+ *          (BC_ID[k] == 1), bit 18 lid inlet, bit 19 west inlet, bit 20
+ *          BC_ID[1] == 3, bit 21 BoundaryID == drag_lift_id; 0 otherwise
+ *   q:     Q[k] of class-3 cells (9 per cell), 0.5 elsewhere
+ * These are the decisions of CellIni (serial/CellFunctions.c:99-270). */
+lbm_status lbm_inspect_mesh(const lbm_mesh *mesh, const lbm_params *params, int32_t *n,
+                            int32_t *m, uint8_t *cls, uint32_t *flags, double *q);
+
+/* ---------------------------------------------------------------------------
+ * Mesh helpers (the reference's readers, serial/FileIO.c:14-289, and a
+ * generator for meshes in the same format).  Buffers returned in lbm_mesh are
+ * owned by the library and released with lbm_mesh_free.
+ * ------------------------------------------------------------------------ */
+lbm_status lbm_mesh_read(const char *node_file, const char *conn_file, lbm_mesh *out);
+/* Lid-driven square cavity with the layout of the shipped cases: fluid cells
+ * i,j in [1, side], solid ring, an extra solid row on top, unit square,
+ * lid (type 2, ID 2) on top, walls left=1, right=3, bottom=4 (type 1). */
+lbm_status lbm_mesh_cavity(int32_t side, lbm_mesh *out);
+/* Channel nx by ny fluid cells: west inlet (type 2, ID 1), east outlet
+ * (type 3, ID 3), walls top=2 / bottom=4, and ncyl circles (type 1, ID 5)
+ * with centres (cx, cy) and radius r in lattice units of the fluid-cell grid. */
+lbm_status lbm_mesh_channel(int32_t nx, int32_t ny, int32_t ncyl, const double *cx,
+                            const double *cy, const double *r, lbm_mesh *out);
+lbm_status lbm_mesh_write(const lbm_mesh *mesh, const char *node_file, const char *conn_file);
+void lbm_mesh_free(lbm_mesh *mesh);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LBM_GB300_H */

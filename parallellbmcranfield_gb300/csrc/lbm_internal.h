@@ -1,0 +1,50 @@
+// Internal host-side declarations shared by the library's translation units.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/lbm_gb300.h"
+#include "lbm_types.h"
+
+namespace lbm {
+
+// Records `msg` as this thread's last error and returns `s`.
+lbm_status fail(lbm_status s, const std::string &msg);
+
+// Host result of the per-cell preprocessing (CellIni restated in O(N)).
+struct Prep {
+  int n = 0, m = 0, pitch = 0;
+  long long plane = 0;
+  double delta = 0, min_y = 0, max_y = 0;
+  double omega = 0, omegaA = 0;
+  double stmiv[81] = {};
+  std::vector<uint8_t> cls;   // m * pitch
+  std::vector<uint32_t> aux;  // m * pitch
+  std::vector<BRec> rec;
+  uint32_t nsb = 0;           // side-buffer slots (AA)
+  long long nfluid = 0;
+  std::vector<double> uo_cell; // Uo of every cell (n*m) with a parabolic inlet, CellIni's initial U
+};
+
+// Builds the per-node class/record tables of a mesh; for the AA pattern it
+// also assigns the side-buffer slots.  Returns LBM_INVALID (with a message) for meshes
+// the fused kernel cannot treat exactly.
+lbm_status preprocess(const lbm_mesh *mesh, const lbm_params *p, Prep *out);
+
+// Launch tables, one per storage precision (lbm_kernels_<prec>.cu).
+typedef void (*StepFn)(StepArgs);
+struct KernelSet {
+  const void *step[4][3];    // [model 1..3][Phase]
+  const void *init[4][2];    // [model 1..3][0: AB, 1: AA]
+  const void *finish[3];     // [layout]
+  const void *resid[3];      // [layout]
+  const void *reduce;        // k_reduce_partials
+  int elem_size;
+};
+const KernelSet &kernels_f64();
+const KernelSet &kernels_f32();
+const KernelSet &kernels_f16();
+const KernelSet &kernels_b16();
+
+}  // namespace lbm

@@ -1,0 +1,77 @@
+// Host/device shared types of the D2Q9 step library.
+#pragma once
+#include <cstdint>
+
+namespace lbm {
+
+// Per-node class byte (the only per-node metadata every launch reads).
+enum NodeClass : uint8_t {
+  CLS_SOLID = 0,    // solid or padding: never updated, reads as F = METAF = 0
+  CLS_BULK = 1,     // fluid, no boundary link, all 8 neighbours fluid
+  CLS_BULK_REC = 2, // bulk node whose METAF is also kept in the side buffer (AA only)
+  CLS_SPECIAL = 3   // fluid node with boundary work: described by a BRec
+};
+
+// Flag bits of BRec::flags.
+enum : uint32_t {
+  FL_STREAM_SHIFT = 0,  // bits 0..8: StreamLattice[k] == 1
+  FL_WALL_SHIFT = 9,    // bits 9..17: BC_ID[k] == 1
+  FL_LID = 1u << 18,    // InletBC top branch active (serial/BoundaryConditions.c:25)
+  FL_WEST = 1u << 19,   // InletBC left branch active (serial/BoundaryConditions.c:39)
+  FL_EAST = 1u << 20,   // BC_ID[1] == 3: east outlet cell
+  FL_DRAG = 1u << 21,   // BoundaryID == CalculateDragLift != 0
+};
+
+// One record per special node (cold data, read only by that node's thread
+// and by the outlet extrapolation of its east neighbours).
+struct BRec {
+  uint32_t node;  // linear node index y * pitch + x
+  uint32_t flags;
+  uint32_t sb;    // side-buffer slot (AA pattern)
+  uint32_t pad;
+  double uo;      // Uo of CellIni (inlet / velocity-outlet speed)
+  double q[9];    // Q[k] of CellIni
+  double x, y;    // CoordX, CoordY (drag/lift placeholder)
+};
+static_assert(sizeof(BRec) == 112, "BRec layout");
+
+// Layout / phase of the population array for one launch.
+enum Phase : int {
+  PH_AB = 0,    // pull from src (A-B pattern)
+  PH_AA_A = 1,  // AA: state in A layout (slot opp(k) at x), output B layout
+  PH_AA_B = 2   // AA: state in B layout (slot k at x + e_k), output A layout
+};
+
+constexpr int NSUM = 10;  // finish-kernel reduction lanes
+enum SumLane : int {
+  S_L2 = 0, S_MASS, S_MX, S_MY, S_FX, S_FY, S_DU, S_UU, S_VMAX, S_NAN
+};
+
+// Everything a launch needs, passed by value (kernel parameter space).
+struct StepArgs {
+  int n, m, pitch;
+  int model, curved, outlet;
+  long long plane;          // elements per population plane
+  const uint8_t *cls;
+  const uint32_t *aux;      // record index (CLS_SPECIAL) / side-buffer slot (CLS_BULK_REC)
+  const BRec *rec;
+  void *src;                // population state read
+  void *dst;                // population state written (== src for AA)
+  double *sb_src, *sb_dst;  // AA side buffers (9 doubles per recorded node)
+  double omega, omegaA, rho_out;
+  double rho0;              // deviation reference density (16-bit storage)
+  float scale[9], inv_scale[9];
+  double stmiv[81];         // Minv * diag(s) of MRTInitializer, row-major
+};
+
+// Outputs of the read-only finish kernel (any pointer may be null).
+struct FinishOut {
+  double *rho, *u, *v;      // n*m, cell-major
+  double *f, *metaf;        // 9*n*m, cell-major
+  const double *rho_solid;  // values reported for solid cells (set_state)
+  const double *u_solid, *v_solid;
+  float *uprev, *vprev;     // du_rel reference fields (read, then replaced), n*m
+  double *partial;          // NSUM per block
+};
+
+}  // namespace lbm

@@ -1,0 +1,382 @@
+"""Benchmark of the fused D2Q9 step on one GB300 (MLUPS and HBM roofline).
+
+Workload (the large single cavity): a lid-driven cavity of 16382^2 fluid
+cells in a 16384 x 16385 node array (268.4 M nodes), lid u = 0.05,
+Re = 10000 (nu = u L / Re), MRT collision, FP32 populations, A-B pattern,
+started from f = f_eq at rest.  A step is one time step over the whole array.
+
+  value   MLUPS = nodes x steps / device time of the timed steps (CUDA events
+          on the solver's stream; state resident in HBM; 19.3 GB of
+          populations per step, far above the 129 MB L2, so no flush is needed)
+  e2e     the same job through the C ABI with host buffers: lbm_set_state
+          from pinned host rho/u/v, K x lbm_step(1) with the reference's
+          per-step residual line copied back, lbm_get_fields to host
+  roofline  algorithmic bytes 72 B/node/step (9 FP32 loads + 9 stores) per
+          launch / average launch time, against the measured HBM copy peak
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+  torchrun --nproc-per-node N bench.py --gpus N ...   (N replicas, one per GPU)
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+W9 = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4)
+PREC_NAME = {0: "fp64", 1: "fp32", 2: "fp16dev", 3: "bf16dev"}
+DTYPE = {0: "f64", 1: "f32", 2: "f16 storage, f32 compute", 3: "bf16 storage, f32 compute"}
+BYTES = {0: 144, 1: 72, 2: 36, 3: 36}
+CPU_SAMPLE_SIDE = 1022  # 1024 x 1025 node cavity for the CPU legs
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=100)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--side", type=int, default=16382, help="fluid cells per cavity side")
+    p.add_argument("--precision", default="fp32", choices=list(PREC_NAME.values()))
+    p.add_argument("--pattern", default="ab", choices=["ab", "aa"])
+    p.add_argument("--model", type=int, default=3)
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--variants", action="store_true",
+                   help="also time AA and 16-bit storage (fewer steps)")
+    return p.parse_args()
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if os.environ.get("LBM_BENCH_GLOO") is None else "gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(ws, x, device):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-i", str(self.idx), "-lms", "100"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        try:
+            with open(self.f.name) as fh:
+                for line in fh:
+                    parts = [x.strip() for x in line.split(",")]
+                    if len(parts) >= 9:
+                        rows.append(parts)
+        finally:
+            os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def feq_rest(rho0, N):
+    return np.tile(rho0 * W9, (N, 1))
+
+
+def cpu_port_mlups(side, model, seconds, steps=None):
+    """The oracle (C restatement of the serial reference, 1 thread) on a cavity sample."""
+    import parallellbmcranfield_gb300 as G
+    from oracle import oracle as O
+
+    O.build(ref=False)
+    mesh = G.Mesh.cavity(side)
+    nu = 0.05 * side / 10000.0
+    port = O.Port(mesh.nodes, mesh.conns, uavg=0.05, vavg=0.0, rho_ini=1.0, viscosity=nu,
+                  inlet_profile=2, model=model, curved=1, outlet=2)
+    n, m = mesh.shape
+    N = n * m
+    port.set_state(feq_rest(1.0, N), np.ones(N), np.zeros(N), np.zeros(N))
+    port.run(1, want_resid=False)
+    done, t0 = 0, time.perf_counter()
+    while True:
+        port.run(1, want_resid=True)
+        done += 1
+        el = time.perf_counter() - t0
+        if (steps is not None and done >= steps) or (steps is None and el >= seconds):
+            break
+    port.close()
+    return N * done / el / 1e6, N, done, el
+
+
+def reference_arm(args):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    import parallellbmcranfield_gb300 as G  # noqa: F401  (mesh generator)
+    from oracle import oracle as O
+
+    O.build(ref=False)
+    side = CPU_SAMPLE_SIDE
+    mesh = G.Mesh.cavity(side)
+    nu = 0.05 * side / 10000.0
+    port = O.Port(mesh.nodes, mesh.conns, uavg=0.05, vavg=0.0, rho_ini=1.0, viscosity=nu,
+                  inlet_profile=2, model=args.model, curved=1, outlet=2)
+    n, m = mesh.shape
+    N = n * m
+    port.set_state(feq_rest(1.0, N), np.ones(N), np.zeros(N), np.zeros(N))
+    port.run(args.warmup, want_resid=True)
+    t0 = time.perf_counter()
+    port.run(args.steps, want_resid=True)
+    el = time.perf_counter() - t0
+    mlups = N * args.steps / el / 1e6
+    sample = (f"cavity {n}x{m} nodes (fluid {side}^2), MRT, FP64, lid 0.05, Re 10000, "
+              f"{args.steps} steps after {args.warmup} warm-up; per-step residual as the serial loop")
+    line = {
+        "impl": "reference", "metric": "MLUPS", "value": round(mlups, 3), "unit": "MLUPS",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(el / args.steps * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args, args.side),
+        "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": 1, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(mlups, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args, side):
+    n, m = side + 2, side + 3
+    return {"workload": f"lid-driven cavity {n}x{m} nodes ({side}^2 fluid), lid u=0.05, Re=10000, "
+                        f"D2Q9 MRT, {args.precision} {args.pattern.upper()}",
+            "nodes": n * m, "fluid_nodes": side * side, "precision": args.precision,
+            "pattern": args.pattern, "collision_model": args.model,
+            "l2_flush": "inputs larger than L2 (populations 19.3 GB at fp32 A-B)"}
+
+
+def load_traffic(precision, pattern, model):
+    """Per-launch DRAM bytes from the committed ncu summary of this kernel, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as fh:
+            t = json.load(fh)
+        return t.get(f"{precision}_{pattern}_m{model}")
+    except (OSError, ValueError):
+        return None
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback"
+
+
+def run_gpu(args):
+    import torch
+
+    import parallellbmcranfield_gb300 as G
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    prec = G.PRECISIONS[args.precision]
+    pat = G.PATTERNS[args.pattern]
+    side = args.side
+    nu = 0.05 * side / 10000.0
+    t_setup = time.perf_counter()
+    mesh = G.Mesh.cavity(side)
+    n, m = mesh.shape
+    N = n * m
+    stream = torch.cuda.Stream(device=dev)
+    solver = G.Solver(mesh, uavg=0.05, vavg=0.0, rho_ini=1.0, viscosity=nu, inlet_profile=2,
+                      collision_model=args.model, curved_boundaries=1, outlet_profile=2,
+                      precision=prec, pattern=pat, device=local, stream=stream.cuda_stream)
+    del mesh
+    # pinned host state: f = f_eq at rest is formed on the device from rho/u/v
+    rho_h = torch.ones(N, dtype=torch.float64, pin_memory=True)
+    u_h = torch.zeros(N, dtype=torch.float64, pin_memory=True)
+    v_h = torch.zeros(N, dtype=torch.float64, pin_memory=True)
+    solver.set_state(None, rho_h.numpy(), u_h.numpy(), v_h.numpy())
+    setup_s = time.perf_counter() - t_setup
+
+    # ---- device-resident throughput
+    solver.step(args.warmup, 0)
+    torch.cuda.synchronize(dev)
+    barrier(ws)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize(dev)
+        ev0.record(stream)
+        solver.step(args.steps, 0)
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+    ms = ev0.elapsed_time(ev1)
+    barrier(ws)
+    ms_max = max_over_ranks(ws, ms, dev)
+    clocks = clk.summary()
+    launches = args.steps  # one fused step kernel per step, nothing else in the timed region
+    mlups = ws * N * args.steps / (ms_max / 1e3) / 1e6
+    per_launch_s = ms / 1e3 / args.steps
+    bpn = BYTES[prec]
+    achieved = bpn * N / per_launch_s / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = load_traffic(args.precision, args.pattern, args.model)
+    diag = solver.check()
+
+    # ---- end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        res_h = np.zeros((args.steps, 4))
+        rho_o = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+        u_o = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+        v_o = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+        barrier(ws)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        solver.set_state(None, rho_h.numpy(), u_h.numpy(), v_h.numpy())
+        for i in range(args.steps):
+            res_h[i] = solver.step(1, 1)[0]
+        out = solver.L.lbm_get_fields(solver.h, rho_o.ctypes.data, u_o.ctypes.data,
+                                      v_o.ctypes.data, None, None)
+        torch.cuda.synchronize(dev)
+        el = time.perf_counter() - t0
+        assert out == 0
+        el = max_over_ranks(ws, el, dev)
+        e2e = {"value": round(ws * N * args.steps / el / 1e6, 1), "unit": "MLUPS",
+               "h2d_bytes_per_step": int(3 * 8 * N / args.steps),
+               "d2h_bytes_per_step": int(32 + 3 * 8 * N / args.steps),
+               "what": "lbm_set_state(host rho,u,v) + steps x lbm_step(1, residual line) + "
+                       "lbm_get_fields(host rho,u,v), wall clock"}
+
+    variants = {}
+    if args.variants:
+        solver.close()
+        for vp, vpat in (("fp32", "aa"), ("fp16dev", "ab"), ("fp16dev", "aa"), ("bf16dev", "aa")):
+            variants[f"{vp}_{vpat}"] = time_variant(args, G, torch, dev, stream, local, vp, vpat)
+    else:
+        solver.close()
+
+    if rank != 0:
+        return
+    cpu_mlups, cpu_N, cpu_steps, cpu_s = cpu_port_mlups(CPU_SAMPLE_SIDE, args.model,
+                                                        args.cpu_seconds)
+    line = {
+        "metric": "MLUPS", "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": DTYPE[prec], "data": "synthetic",
+        "config": workload_config(args, side),
+        "fluid_mlups": round(ws * args.side ** 2 * args.steps / (ms_max / 1e3) / 1e6, 1),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "peak_kind": peak_kind, "bytes_per_node_step": bpn,
+                     "kernel": "lbm::k_step (fused pull-stream + BC + moments + collision)"},
+        "cpu_baseline": {"value": round(cpu_mlups, 3), "unit": "MLUPS", "cores": 1, "kind": "port",
+                         "sample": f"oracle port (serial reference restated, bit-identical), cavity "
+                                   f"{CPU_SAMPLE_SIDE + 2}x{CPU_SAMPLE_SIDE + 3} MRT FP64, "
+                                   f"{cpu_steps} steps in {cpu_s:.1f} s, 1 thread"},
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "diagnostics": {"mass": diag["mass"], "max_speed": diag["max_speed"]},
+        "setup_s": round(setup_s, 1),
+    }
+    if variants:
+        line["variants"] = variants
+    print(json.dumps(line), flush=True)
+
+
+def time_variant(args, G, torch, dev, stream, local, prec_name, pat_name, steps=None):
+    side = args.side
+    steps = steps or max(10, args.steps // 2)
+    mesh = G.Mesh.cavity(side)
+    n, m = mesh.shape
+    N = n * m
+    s = G.Solver(mesh, uavg=0.05, vavg=0.0, rho_ini=1.0, viscosity=0.05 * side / 10000.0,
+                 collision_model=args.model, curved_boundaries=1, outlet_profile=2,
+                 precision=G.PRECISIONS[prec_name], pattern=G.PATTERNS[pat_name], device=local,
+                 stream=stream.cuda_stream)
+    del mesh
+    s.set_state(None, np.ones(N), np.zeros(N), np.zeros(N))
+    s.step(4, 0)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s.step(steps, 0)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1)
+    s.close()
+    prec = G.PRECISIONS[prec_name]
+    per = ms / 1e3 / steps
+    peak, _ = measured_peak()
+    return {"mlups": round(N / per / 1e6, 1),
+            "ms_per_step": round(ms / steps, 4), "steps": steps,
+            "hbm_frac": round(BYTES[prec] * N / per / 1e9 / peak, 4)}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -99,17 +99,19 @@ def test_split_calls_equal_one_call():
 
 
 @pytest.mark.parametrize("pattern", [G.AB, G.AA])
-@pytest.mark.parametrize("precision,tol_rho,tol_u", [(G.FP32, 2e-6, 2e-4), (G.FP16DEV, 2e-4, 3e-2),
-                                                     (G.BF16DEV, 2e-3, 2e-1)])
+@pytest.mark.parametrize("precision,tol_rho,tol_u", [(G.FP32, 1e-5, 1e-3), (G.FP16DEV, 1e-3, 5e-2),
+                                                     (G.BF16DEV, 1e-2, 3e-1)])
 @pytest.mark.parametrize("name", ["cavity_mrt_curved", "chan_mrt_pressure", "cavity_trt_curved"])
 def test_reduced_precision_against_fp64(name, precision, tol_rho, tol_u, pattern):
     """Per-field tolerances after the case's step count, relative to max |field|."""
     _, ref, _ = run_gpu(name, G.FP64, G.AB, check_every=0)
     _, low, _ = run_gpu(name, precision, pattern, check_every=0)
     a, b = low.fields(), ref.fields()
-    assert rel_err(a["rho"], b["rho"]) <= tol_rho
     speed = np.sqrt(b["u"] ** 2 + b["v"] ** 2).max()
     err_u = np.sqrt((a["u"] - b["u"]) ** 2 + (a["v"] - b["v"]) ** 2).max() / speed
+    err_rho = rel_err(a["rho"], b["rho"])
+    print(f"{name} prec={precision} pat={pattern}: rho {err_rho:.3e} u {err_u:.3e}")
+    assert err_rho <= tol_rho
     assert err_u <= tol_u
 
 

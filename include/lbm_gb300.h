@@ -132,6 +132,20 @@ lbm_status lbm_get_fields(lbm_ctx *ctx, double *rho, double *u, double *v, doubl
  * du_rel reference fields.  LBM_DIVERGED if any sum is NaN. */
 lbm_status lbm_check(lbm_ctx *ctx, lbm_diagnostics *out);
 
+/* lbm_check without any device allocation, for callers that cannot call
+ * cudaMalloc when they want the diagnostics (a host that gives all device
+ * memory to its own pool, a loop that must not allocate between steps).
+ * No counterpart in the reference, whose residual needs no device memory.
+ * Same sums as lbm_check except du_rel (returned as NaN: it needs per-cell
+ * reference fields).  Uses one fixed 5 MiB device array inside the library,
+ * held on every GPU that loads it until exit, so domains whose diagnostics
+ * grid needs more than 65536 blocks of 128 positions (about 8.4 M grid
+ * positions) get LBM_INVALID.  Calls share that array: calls whose kernels
+ * overlap on the GPU (other streams or host threads) race; serialise them.
+ * The first call on a device looks up the array's address; make it before
+ * any stream capture. */
+lbm_status lbm_check_noalloc(lbm_ctx *ctx, lbm_diagnostics *out);
+
 /* Completed iterations, device bytes held, bytes moved per node per step. */
 lbm_status lbm_get_info(const lbm_ctx *ctx, int64_t *iteration, int64_t *device_bytes,
                         int32_t *bytes_per_node_step);

@@ -56,7 +56,8 @@ class lbm_diagnostics(C.Structure):
 
 # every symbol include/lbm_gb300.h declares
 EXPORTS = ["lbm_status_string", "lbm_last_error", "lbm_create", "lbm_destroy", "lbm_get_dims",
-           "lbm_set_state", "lbm_step", "lbm_get_fields", "lbm_check", "lbm_get_info",
+           "lbm_set_state", "lbm_step", "lbm_get_fields", "lbm_check", "lbm_check_noalloc",
+           "lbm_get_info",
            "lbm_inspect_mesh", "lbm_mesh_read", "lbm_mesh_cavity", "lbm_mesh_channel", "lbm_mesh_write",
            "lbm_mesh_free"]
 
@@ -84,6 +85,7 @@ def load():
     L.lbm_step.argtypes = [vp, i32, i32, dp]
     L.lbm_get_fields.argtypes = [vp, dp, dp, dp, dp, dp]
     L.lbm_check.argtypes = [vp, C.POINTER(lbm_diagnostics)]
+    L.lbm_check_noalloc.argtypes = [vp, C.POINTER(lbm_diagnostics)]
     L.lbm_get_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(i32)]
     L.lbm_inspect_mesh.argtypes = [C.POINTER(lbm_mesh), C.POINTER(lbm_params), C.POINTER(i32),
                                    C.POINTER(i32), dp, dp, dp]

@@ -449,3 +449,28 @@ lbm_status lbm_check(lbm_ctx *ctx, lbm_diagnostics *out) {
 }
 
 }  // extern "C"
+
+// Allocation-free variant of lbm_check (see lbm_noalloc.cu for the fixed
+// scratch array it uses and its limits).
+extern "C" lbm_status lbm_check_noalloc(lbm_ctx *ctx, lbm_diagnostics *out) {
+  if (!ctx || !out) return fail(LBM_INVALID, "null argument");
+  if (!ctx->have_state || ctx->iter == 0)
+    return fail(LBM_INVALID, "no completed iteration to check");
+  LBM_CK(cudaSetDevice(ctx->p.device));
+  double h[lbm::NSUM];
+  lbm_status s = lbm::check_noalloc(ctx->ks, args_now(ctx), layout_of(ctx), node_grid(ctx),
+                                    ctx->stream, h);
+  if (s != LBM_OK) return s;
+  out->iteration = ctx->iter;
+  out->l2_full = std::sqrt(h[lbm::S_L2]);
+  out->mass = h[lbm::S_MASS];
+  out->momentum[0] = h[lbm::S_MX];
+  out->momentum[1] = h[lbm::S_MY];
+  out->force[0] = h[lbm::S_FX];
+  out->force[1] = h[lbm::S_FY];
+  out->max_speed = h[lbm::S_VMAX];
+  out->du_rel = NAN;  // needs per-cell reference fields, which this variant cannot allocate
+  if (h[lbm::S_NAN] > 0 || h[lbm::S_MASS] != h[lbm::S_MASS])
+    return fail(LBM_DIVERGED, "NaN in the macroscopic fields");
+  return LBM_OK;
+}

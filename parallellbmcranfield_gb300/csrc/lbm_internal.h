@@ -1,5 +1,7 @@
 // Internal host-side declarations shared by the library's translation units.
 #pragma once
+#include <cuda_runtime.h>
+
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -47,4 +49,11 @@ const KernelSet &kernels_f32();
 const KernelSet &kernels_f16();
 const KernelSet &kernels_b16();
 
+}  // namespace lbm
+
+namespace lbm {
+// Diagnostics reduction with the library's fixed device scratch array
+// (lbm_noalloc.cu); performs no device allocation.
+lbm_status check_noalloc(const KernelSet *ks, const StepArgs &a, int layout, dim3 grid,
+                         cudaStream_t stream, double sums[NSUM]);
 }  // namespace lbm

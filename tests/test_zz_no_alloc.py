@@ -1,0 +1,75 @@
+"""GPU: lbm_check_noalloc, the diagnostics entry point that allocates nothing.
+
+Some callers cannot call cudaMalloc when they want the diagnostics: a host
+that has handed all device memory to its own pool, or a stepping loop that
+must not allocate between time steps.  lbm_check_noalloc serves them with a
+fixed device array inside the library instead of allocated scratch.  This
+file checks it through the C ABI against lbm_check, the existing entry point,
+on consecutive calls (the shared array keeps the previous call's contents),
+and checks that a domain larger than the array's limit is refused.  It is
+named so that pytest collects it last.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import cases
+import parallellbmcranfield_gb300 as G
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10  # the FP64 tolerance of the parity tests
+
+
+def diag(solver, fn):
+    d = G.lbm_diagnostics()
+    status = fn(solver.h, ctypes.byref(d))
+    assert status == G.LBM_OK, G.load().lbm_last_error()
+    return d
+
+
+def assert_same(a, b):
+    for name in ("l2_full", "mass", "max_speed"):
+        x, y = getattr(a, name), getattr(b, name)
+        assert abs(x - y) <= RTOL * max(abs(x), 1e-300), name
+    for name in ("momentum", "force"):
+        x, y = np.array(getattr(a, name)), np.array(getattr(b, name))
+        scale = max(np.abs(x).max(), abs(a.mass) * 1e-12, 1e-300)
+        assert np.abs(x - y).max() <= RTOL * scale, name
+    assert a.iteration == b.iteration
+    assert np.isnan(b.du_rel)
+
+
+@pytest.mark.parametrize("name,precision,pattern", [("chan_mrt_extrap", G.FP64, G.AB),
+                                                    ("cavity_trt_curved", G.FP32, G.AA)])
+def test_noalloc_matches_check_on_consecutive_calls(name, precision, pattern):
+    spec, params, start, _ = cases.ALL[name]
+    mesh = cases.build_mesh(spec)
+    s = G.Solver(mesh, precision=precision, pattern=pattern, **params)
+    s.set_state(*cases.start_state(mesh, params, start))
+    L = G.load()
+    s.step(40)
+    ref = diag(s, L.lbm_check)
+    first = diag(s, L.lbm_check_noalloc)
+    second = diag(s, L.lbm_check_noalloc)
+    assert_same(ref, first)
+    assert_same(ref, second)
+    s.step(33)  # odd count: the AA layout flips between the two checks
+    ref2 = diag(s, L.lbm_check)
+    third = diag(s, L.lbm_check_noalloc)
+    assert_same(ref2, third)
+    assert ref2.mass != ref.mass or ref2.l2_full != ref.l2_full
+    s.close()
+
+
+def test_noalloc_rejects_domains_beyond_its_scratch():
+    mesh = G.Mesh.cavity(3000)  # 3002 x 3003 positions: 72k blocks of 128 > 65536
+    s = G.Solver(mesh, precision=G.FP32, uavg=0.05, rho_ini=1.0, viscosity=0.05)
+    s.step(1)
+    d = G.lbm_diagnostics()
+    status = G.load().lbm_check_noalloc(s.h, ctypes.byref(d))
+    assert status == G.LBM_INVALID
+    assert b"scratch" in G.load().lbm_last_error()
+    s.check()  # the allocating entry point still serves this domain
+    s.close()

@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--model", type=int, default=3)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--tile", type=int, default=0,
+                   help="fused-step tile variant 1..4; 0 = autotune")
     p.add_argument("--variants", action="store_true",
                    help="also time AA and 16-bit storage (fewer steps)")
     return p.parse_args()
@@ -245,8 +247,10 @@ def run_gpu(args):
     stream = torch.cuda.Stream(device=dev)
     solver = G.Solver(mesh, uavg=0.05, vavg=0.0, rho_ini=1.0, viscosity=nu, inlet_profile=2,
                       collision_model=args.model, curved_boundaries=1, outlet_profile=2,
-                      precision=prec, pattern=pat, device=local, stream=stream.cuda_stream)
+                      precision=prec, pattern=pat, device=local, stream=stream.cuda_stream,
+                      tile_variant=args.tile)
     del mesh
+    tune = solver.autotune(5) if args.tile == 0 else {"variant": args.tile - 1, "fixed": True}
     # pinned host state: f = f_eq at rest is formed on the device from rho/u/v
     rho_h = torch.ones(N, dtype=torch.float64, pin_memory=True)
     u_h = torch.zeros(N, dtype=torch.float64, pin_memory=True)
@@ -335,6 +339,7 @@ def run_gpu(args):
         "clocks": clocks,
         "diagnostics": {"mass": diag["mass"], "max_speed": diag["max_speed"]},
         "setup_s": round(setup_s, 1),
+        "tile": tune,
     }
     if variants:
         line["variants"] = variants
@@ -342,6 +347,7 @@ def run_gpu(args):
 
 
 def time_variant(args, G, torch, dev, stream, local, prec_name, pat_name, steps=None):
+    """MLUPS of another storage/pattern on the same cavity (autotuned tile)."""
     side = args.side
     steps = steps or max(10, args.steps // 2)
     mesh = G.Mesh.cavity(side)
@@ -352,6 +358,7 @@ def time_variant(args, G, torch, dev, stream, local, prec_name, pat_name, steps=
                  precision=G.PRECISIONS[prec_name], pattern=G.PATTERNS[pat_name], device=local,
                  stream=stream.cuda_stream)
     del mesh
+    tune = s.autotune(5)
     s.set_state(None, np.ones(N), np.zeros(N), np.zeros(N))
     s.step(4, 0)
     torch.cuda.synchronize(dev)
@@ -367,7 +374,7 @@ def time_variant(args, G, torch, dev, stream, local, prec_name, pat_name, steps=
     peak, _ = measured_peak()
     return {"mlups": round(N / per / 1e6, 1),
             "ms_per_step": round(ms / steps, 4), "steps": steps,
-            "hbm_frac": round(BYTES[prec] * N / per / 1e9 / peak, 4)}
+            "hbm_frac": round(BYTES[prec] * N / per / 1e9 / peak, 4), "tile": tune}
 
 
 def main():

@@ -82,6 +82,7 @@ typedef struct lbm_params {
   int32_t device;            /* CUDA device ordinal */
   double rho_out;            /* outlet density for outlet_profile 4 */
   void *stream;              /* cudaStream_t to run on; NULL = a stream owned by the context */
+  int32_t tile_variant;      /* fused-step tile: 0 = default or lbm_autotune's choice, 1..4 fixed */
 } lbm_params;
 
 typedef struct lbm_ctx lbm_ctx;
@@ -145,6 +146,16 @@ lbm_status lbm_check(lbm_ctx *ctx, lbm_diagnostics *out);
  * The first call on a device looks up the array's address; make it before
  * any stream capture. */
 lbm_status lbm_check_noalloc(lbm_ctx *ctx, lbm_diagnostics *out);
+
+/* Autotuner (no counterpart in the reference): times every tile variant of
+ * the fused step (threads along x, rows per thread) on this context's domain
+ * and keeps the fastest.  Must run before lbm_set_state: it steps a scratch
+ * state at rest and discards it.  cache_path (NULL = none) is a file of JSON
+ * lines keyed by GPU, storage, pattern, model and grid size: a hit skips the
+ * timing, a miss appends the result.  report (NULL = none) receives the
+ * JSON line. */
+lbm_status lbm_autotune(lbm_ctx *ctx, int32_t steps_per_trial, const char *cache_path,
+                        char *report, size_t report_cap);
 
 /* Completed iterations, device bytes held, bytes moved per node per step. */
 lbm_status lbm_get_info(const lbm_ctx *ctx, int64_t *iteration, int64_t *device_bytes,

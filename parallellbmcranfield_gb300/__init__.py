@@ -45,7 +45,7 @@ class lbm_params(C.Structure):
                 ("collision_model", C.c_int32), ("curved_boundaries", C.c_int32),
                 ("outlet_profile", C.c_int32), ("drag_lift_id", C.c_int32),
                 ("precision", C.c_int32), ("pattern", C.c_int32), ("device", C.c_int32),
-                ("rho_out", C.c_double), ("stream", C.c_void_p)]
+                ("rho_out", C.c_double), ("stream", C.c_void_p), ("tile_variant", C.c_int32)]
 
 
 class lbm_diagnostics(C.Structure):
@@ -57,7 +57,7 @@ class lbm_diagnostics(C.Structure):
 # every symbol include/lbm_gb300.h declares
 EXPORTS = ["lbm_status_string", "lbm_last_error", "lbm_create", "lbm_destroy", "lbm_get_dims",
            "lbm_set_state", "lbm_step", "lbm_get_fields", "lbm_check", "lbm_check_noalloc",
-           "lbm_get_info",
+           "lbm_get_info", "lbm_autotune",
            "lbm_inspect_mesh", "lbm_mesh_read", "lbm_mesh_cavity", "lbm_mesh_channel", "lbm_mesh_write",
            "lbm_mesh_free"]
 
@@ -86,6 +86,7 @@ def load():
     L.lbm_get_fields.argtypes = [vp, dp, dp, dp, dp, dp]
     L.lbm_check.argtypes = [vp, C.POINTER(lbm_diagnostics)]
     L.lbm_check_noalloc.argtypes = [vp, C.POINTER(lbm_diagnostics)]
+    L.lbm_autotune.argtypes = [vp, i32, C.c_char_p, C.c_char_p, C.c_size_t]
     L.lbm_get_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(i32)]
     L.lbm_inspect_mesh.argtypes = [C.POINTER(lbm_mesh), C.POINTER(lbm_params), C.POINTER(i32),
                                    C.POINTER(i32), dp, dp, dp]
@@ -169,14 +170,14 @@ class Mesh:
 
 def make_params(uavg=0.05, vavg=0.0, rho_ini=1.0, viscosity=0.01, inlet_profile=2,
                 collision_model=BGKW, curved_boundaries=2, outlet_profile=2, drag_lift_id=0,
-                precision=FP64, pattern=AB, rho_out=1.0, device=0, stream=None):
+                precision=FP64, pattern=AB, rho_out=1.0, device=0, stream=None, tile_variant=0):
     if isinstance(precision, str):
         precision = PRECISIONS[precision]
     if isinstance(pattern, str):
         pattern = PATTERNS[pattern]
     return lbm_params(uavg, vavg, rho_ini, viscosity, inlet_profile, collision_model,
                       curved_boundaries, outlet_profile, drag_lift_id, precision, pattern,
-                      device, rho_out, stream)
+                      device, rho_out, stream, tile_variant)
 
 
 def inspect_mesh(mesh, **params):
@@ -204,11 +205,12 @@ class Solver:
 
     def __init__(self, mesh, uavg=0.05, vavg=0.0, rho_ini=1.0, viscosity=0.01,
                  inlet_profile=2, collision_model=BGKW, curved_boundaries=2, outlet_profile=2,
-                 drag_lift_id=0, precision=FP64, pattern=AB, rho_out=1.0, device=0, stream=None):
+                 drag_lift_id=0, precision=FP64, pattern=AB, rho_out=1.0, device=0, stream=None,
+                 tile_variant=0):
         L = self.L = load()
         p = make_params(uavg, vavg, rho_ini, viscosity, inlet_profile, collision_model,
                         curved_boundaries, outlet_profile, drag_lift_id, precision, pattern,
-                        rho_out, device, stream)
+                        rho_out, device, stream, tile_variant)
         precision, pattern = p.precision, p.pattern
         self.mesh = mesh
         self.h = C.c_void_p()
@@ -247,6 +249,15 @@ class Solver:
         return {"iteration": d.iteration, "l2_full": d.l2_full, "du_rel": d.du_rel,
                 "mass": d.mass, "momentum": tuple(d.momentum), "force": tuple(d.force),
                 "max_speed": d.max_speed}
+
+    def autotune(self, steps_per_trial=10, cache_path=None):
+        """Pick the fastest fused-step tile for this domain (before set_state)."""
+        buf = C.create_string_buffer(1024)
+        _check(self.L.lbm_autotune(self.h, int(steps_per_trial),
+                                   None if cache_path is None else str(cache_path).encode(),
+                                   buf, len(buf)), "lbm_autotune")
+        import json
+        return json.loads(buf.value.decode())
 
     def info(self):
         it, db, bpn = C.c_int64(), C.c_int64(), C.c_int32()

@@ -10,6 +10,7 @@ import os
 import shutil
 import subprocess
 import sys
+import time
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
@@ -25,22 +26,34 @@ def _nvcc():
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build liblbm_gb300.so")
 
 
+INST = "lbm_kernels_inst.cu"  # compiled once per (precision, part)
+PRECS = ["f64", "f32", "f16", "b16"]
+
+
 def sources():
-    cu = sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
-    cpp = sorted(f for f in os.listdir(CSRC) if f.endswith(".cpp"))
-    return cu, cpp
+    """(object name, source, extra flags) for every translation unit."""
+    units = []
+    for f in sorted(os.listdir(CSRC)):
+        if f == INST:
+            for p, name in enumerate(PRECS):
+                for part in range(4):
+                    flags = [f"-DLBM_PREC={p}", f"-DLBM_PART={part}"]
+                    if name == "f64":
+                        flags.append("--fmad=false")
+                    units.append((f"lbm_kernels_{name}_{part}", f, flags))
+        elif f.endswith((".cu", ".cpp")):
+            units.append((os.path.splitext(f)[0], f, []))
+    return units
 
 
-def _cmd(src):
+def _cmd(obj, src, flags):
     nvcc = _nvcc()
-    out = os.path.join(OBJ, os.path.splitext(src)[0] + ".o")
+    out = os.path.join(OBJ, obj + ".o")
     path = os.path.join(CSRC, src)
     if src.endswith(".cu"):
         cmd = [nvcc, *ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
-               "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",
+               "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr", *flags,
                "-c", path, "-o", out]
-        if src.endswith("_f64.cu"):
-            cmd.insert(1, "--fmad=false")
         if os.environ.get("LBM_PTXAS_VERBOSE"):
             cmd.insert(1, "-Xptxas=-v")
     else:
@@ -58,26 +71,32 @@ def _stale(out, deps):
 
 def build(verbose=False, jobs=None):
     os.makedirs(OBJ, exist_ok=True)
-    cu, cpp = sources()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(os.path.dirname(HERE), "include", "lbm_gb300.h"))
     jobs_ = []
     objs = []
-    for src in cu + cpp:
-        cmd, out, path = _cmd(src)
+    for obj, src, flags in sources():
+        cmd, out, path = _cmd(obj, src, flags)
         objs.append(out)
         if _stale(out, [path, *headers, __file__]):
-            jobs_.append((src, cmd))
+            jobs_.append((obj, cmd))
+    # objects of sources that no longer exist must not be linked
+    for f in os.listdir(OBJ):
+        if f.endswith(".o") and os.path.join(OBJ, f) not in objs:
+            os.remove(os.path.join(OBJ, f))
     errors = []
 
     def run(item):
         src, cmd = item
         if verbose:
             print(" ".join(cmd), flush=True)
+        t0 = time.time()
         p = subprocess.run(cmd, capture_output=True, text=True)
+        if verbose:
+            print(f"  {src}: {time.time() - t0:.1f} s", flush=True)
         return src, p
 
-    with cf.ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=jobs or min(24, os.cpu_count() or 4)) as ex:
         for src, p in ex.map(run, jobs_):
             if p.returncode != 0:
                 errors.append(f"--- {src}\n{p.stdout}\n{p.stderr}")

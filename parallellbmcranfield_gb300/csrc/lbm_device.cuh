@@ -22,6 +22,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <cstring>
 #include <type_traits>
 
 #include "lbm_types.h"
@@ -43,6 +44,8 @@ __device__ __forceinline__ R wgt(int k) {
 struct StF64 {
   using T = double;
   using R = double;
+  static __device__ __forceinline__ R cvt(T v, int, const StepArgs &) { return v; }
+  static __device__ __forceinline__ T pack(R v, int, const StepArgs &) { return v; }
   static __device__ __forceinline__ R ld(const T *p, int, const StepArgs &) { return __ldg(p); }
   static __device__ __forceinline__ void st(T *p, int, R v, const StepArgs &) { *p = v; }
 };
@@ -50,6 +53,8 @@ struct StF64 {
 struct StF32 {
   using T = float;
   using R = float;
+  static __device__ __forceinline__ R cvt(T v, int, const StepArgs &) { return v; }
+  static __device__ __forceinline__ T pack(R v, int, const StepArgs &) { return v; }
   static __device__ __forceinline__ R ld(const T *p, int, const StepArgs &) { return __ldg(p); }
   static __device__ __forceinline__ void st(T *p, int, R v, const StepArgs &) { __stcs(p, v); }
 };
@@ -58,22 +63,77 @@ struct StF32 {
 struct StF16 {
   using T = __half;
   using R = float;
+  static __device__ __forceinline__ R cvt(T v, int k, const StepArgs &a) {
+    return fmaf(__half2float(v), a.inv_scale[k], wgt<float>(k) * (float)a.rho0);
+  }
+  static __device__ __forceinline__ T pack(R v, int k, const StepArgs &a) {
+    return __float2half_rn((v - wgt<float>(k) * (float)a.rho0) * a.scale[k]);
+  }
   static __device__ __forceinline__ R ld(const T *p, int k, const StepArgs &a) {
-    return fmaf(__half2float(__ldg(p)), a.inv_scale[k], wgt<float>(k) * (float)a.rho0);
+    return cvt(__ldg(p), k, a);
   }
-  static __device__ __forceinline__ void st(T *p, int k, R v, const StepArgs &a) {
-    *p = __float2half_rn((v - wgt<float>(k) * (float)a.rho0) * a.scale[k]);
-  }
+  static __device__ __forceinline__ void st(T *p, int k, R v, const StepArgs &a) { *p = pack(v, k, a); }
 };
 
 struct StB16 {
   using T = __nv_bfloat16;
   using R = float;
-  static __device__ __forceinline__ R ld(const T *p, int k, const StepArgs &a) {
-    return fmaf(__bfloat162float(__ldg(p)), a.inv_scale[k], wgt<float>(k) * (float)a.rho0);
+  static __device__ __forceinline__ R cvt(T v, int k, const StepArgs &a) {
+    return fmaf(__bfloat162float(v), a.inv_scale[k], wgt<float>(k) * (float)a.rho0);
   }
-  static __device__ __forceinline__ void st(T *p, int k, R v, const StepArgs &a) {
-    *p = __float2bfloat16_rn((v - wgt<float>(k) * (float)a.rho0) * a.scale[k]);
+  static __device__ __forceinline__ T pack(R v, int k, const StepArgs &a) {
+    return __float2bfloat16_rn((v - wgt<float>(k) * (float)a.rho0) * a.scale[k]);
+  }
+  static __device__ __forceinline__ R ld(const T *p, int k, const StepArgs &a) {
+    return cvt(__ldg(p), k, a);
+  }
+  static __device__ __forceinline__ void st(T *p, int k, R v, const StepArgs &a) { *p = pack(v, k, a); }
+};
+
+// Aligned loads / streaming stores of V consecutive elements as 4..16-byte words.
+template <class T, int V>
+struct VecIO {
+  static constexpr int B = (int)sizeof(T) * V;
+  static_assert(B == 2 || B == 4 || B == 8 || B % 16 == 0, "vector width");
+  static __device__ __forceinline__ void load(const T *p, T out[V]) {
+    if constexpr (B == 2) {
+      unsigned short r = __ldg((const unsigned short *)p);
+      memcpy(out, &r, 2);
+    } else if constexpr (B == 4) {
+      unsigned r = __ldg((const unsigned *)p);
+      memcpy(out, &r, 4);
+    } else if constexpr (B == 8) {
+      uint2 r = __ldg((const uint2 *)p);
+      memcpy(out, &r, 8);
+    } else {
+#pragma unroll
+      for (int i = 0; i < B / 16; i++) {
+        uint4 r = __ldg((const uint4 *)p + i);
+        memcpy((char *)out + 16 * i, &r, 16);
+      }
+    }
+  }
+  static __device__ __forceinline__ void store(T *p, const T in[V]) {
+    if constexpr (B == 2) {
+      unsigned short r;
+      memcpy(&r, in, 2);
+      __stcs((unsigned short *)p, r);
+    } else if constexpr (B == 4) {
+      unsigned r;
+      memcpy(&r, in, 4);
+      __stcs((unsigned *)p, r);
+    } else if constexpr (B == 8) {
+      uint2 r;
+      memcpy(&r, in, 8);
+      __stcs((uint2 *)p, r);
+    } else {
+#pragma unroll
+      for (int i = 0; i < B / 16; i++) {
+        uint4 r;
+        memcpy(&r, (const char *)in + 16 * i, 16);
+        __stcs((uint4 *)p + i, r);
+      }
+    }
   }
 };
 
@@ -291,6 +351,56 @@ __device__ __forceinline__ void collide(const R F[9], R rho, R u, R v, const Ste
   else collide_mrt<R>(F, rho, u, v, a, M);
 }
 
+// Moments plus collision of a node without boundary work.  In FP32 the MRT
+// operator takes rho, j from its own moment transform (rho = m0, j = m3, m5)
+// so the conserved moments relax by exactly zero and need no work; rho^2 q is
+// formed as |j|^2.  FP64 keeps the reference's two-pass arithmetic.
+template <int MODEL, class R>
+__device__ __forceinline__ void collide_bulk(const R F[9], const StepArgs &a, R M[9]) {
+  if constexpr (MODEL == 3 && !std::is_same<R, double>::value) {
+    const R om = (R)a.omega;
+    R a13 = F[1] + F[3], a24 = F[2] + F[4];
+    R a14 = a13 + a24;
+    R p57 = F[5] + F[7], p68 = F[6] + F[8];
+    R a58 = p57 + p68;
+    R rho = (F[0] + a14) + a58;
+    R m1 = R(2) * a58 - a14 - R(4) * F[0];
+    R m2 = (R(4) * F[0] + a58) - R(2) * a14;
+    R d13 = F[1] - F[3], d24 = F[2] - F[4];
+    R e57 = F[5] - F[7], e86 = F[8] - F[6];
+    R x58 = e57 + e86, y58 = e57 - e86;
+    R jx = d13 + x58, jy = d24 + y58;
+    R m4 = x58 - R(2) * d13, m6 = y58 - R(2) * d24;
+    R m7 = a13 - a24, m8 = p57 - p68;
+    R inv = R(1) / rho;
+    R jj = jx * jx + jy * jy;
+    R d1 = R(1.4) * (m1 + R(2) * rho - R(3) * jj);
+    R d2 = R(1.4) * (m2 - rho + R(3) * jj);
+    R d4 = R(1.2) * (m4 + jx);
+    R d6 = R(1.2) * (m6 + jy);
+    R d7 = om * (m7 - (jx * jx - jy * jy) * inv);
+    R d8 = om * (m8 - jx * jy * inv);
+    const R c = R(1.0 / 36.0);
+    R ax = -d1 - R(2) * d2;
+    R dg = R(2) * d1 + d2;
+    R X = R(-6) * d4, Y = R(-6) * d6, P = R(9) * d7;
+    R Xd = R(3) * d4, Yd = R(3) * d6, Q = R(9) * d8;
+    M[0] = F[0] - c * (R(4) * (d2 - d1));
+    M[1] = F[1] - c * (ax + X + P);
+    M[2] = F[2] - c * (ax + Y - P);
+    M[3] = F[3] - c * (ax - X + P);
+    M[4] = F[4] - c * (ax - Y - P);
+    M[5] = F[5] - c * (dg + Xd + Yd + Q);
+    M[6] = F[6] - c * (dg - Xd + Yd - Q);
+    M[7] = F[7] - c * (dg - Xd - Yd + Q);
+    M[8] = F[8] - c * (dg + Xd - Yd - Q);
+  } else {
+    R rho, u, v;
+    moments<R>(F, rho, u, v);
+    collide<MODEL, R>(F, rho, u, v, a, M);
+  }
+}
+
 // ------------------------------------------------------ boundary conditions
 
 // F of a special node after streaming and the inlet / wall treatments of
@@ -414,39 +524,13 @@ __device__ __forceinline__ bool node_xy(const StepArgs &a, int &x, int &y) {
   return x < a.n;
 }
 
-// Fused step: METAF_t (layout PH) -> METAF_{t+1}.
-template <class ST, int MODEL, int PH>
-__global__ void __launch_bounds__(128) k_step(const __grid_constant__ StepArgs a) {
-  using R = typename ST::R;
+// Store of one fluid node's post-collision populations in the output layout
+// (plus its side-buffer copy in the AA pattern when it is recorded).
+template <class ST, int PH>
+__device__ __forceinline__ void store_node(const StepArgs &a, long long node, uint8_t c,
+                                           const typename ST::R M[9]) {
   using T = typename ST::T;
-  int x, y;
-  if (!node_xy(a, x, y)) return;
-  const long long node = (long long)y * a.pitch + x;
-  const uint8_t c = a.cls[node];
-  if (c == CLS_SOLID) return;
-  const T *s = (const T *)a.src;
   T *d = (T *)a.dst;
-  R F[9], rho, u, v;
-  if (c != CLS_SPECIAL) {
-#pragma unroll
-    for (int k = 0; k < 9; k++) {
-      long long i;
-      if (PH == PH_AB) i = (long long)k * a.plane + node - nb(k, a.pitch);
-      else if (PH == PH_AA_A) i = (long long)OPP[k] * a.plane + node - nb(k, a.pitch);
-      else i = (long long)k * a.plane + node;
-      F[k] = ST::ld(s + i, k, a);
-    }
-    moments<R>(F, rho, u, v);
-  } else {
-    R mac[3];
-    if (PH == PH_AB) special_node<R>(a, AccMain<ST, PH_AB>(a, a.src), node, F, mac);
-    else special_node<R>(a, AccSide<ST>(a, nullptr), node, F, mac);
-    rho = mac[0];
-    u = mac[1];
-    v = mac[2];
-  }
-  R M[9];
-  collide<MODEL, R>(F, rho, u, v, a, M);
 #pragma unroll
   for (int k = 0; k < 9; k++) {
     long long i;
@@ -460,6 +544,531 @@ __global__ void __launch_bounds__(128) k_step(const __grid_constant__ StepArgs a
     if (c == CLS_SPECIAL) sbi = a.rec[sbi].sb;
 #pragma unroll
     for (int k = 0; k < 9; k++) a.sb_dst[(size_t)sbi * 9 + k] = (double)M[k];
+  }
+}
+
+// Collision and store of one fluid node whose F and moments are known.
+template <class ST, int MODEL, int PH>
+__device__ __forceinline__ void collide_store(const StepArgs &a, long long node, uint8_t c,
+                                              const typename ST::R F[9], typename ST::R rho,
+                                              typename ST::R u, typename ST::R v) {
+  using R = typename ST::R;
+  R M[9];
+  collide<MODEL, R>(F, rho, u, v, a, M);
+  store_node<ST, PH>(a, node, c, M);
+}
+
+// Collision and store of a node without boundary work.
+template <class ST, int MODEL, int PH>
+__device__ __forceinline__ void bulk_store(const StepArgs &a, long long node, uint8_t c,
+                                           const typename ST::R F[9]) {
+  using R = typename ST::R;
+  R M[9];
+  collide_bulk<MODEL, R>(F, a, M);
+  store_node<ST, PH>(a, node, c, M);
+}
+
+// Index of the pulled F[k](node) in the state of layout PH.
+template <int PH>
+__device__ __forceinline__ long long pull_index(int k, long long node, const StepArgs &a) {
+  if (PH == PH_AB) return (long long)k * a.plane + node - nb(k, a.pitch);
+  if (PH == PH_AA_A) return (long long)OPP[k] * a.plane + node - nb(k, a.pitch);
+  return (long long)k * a.plane + node;
+}
+
+// The whole fused update of one node of any class.
+template <class ST, int MODEL, int PH>
+__device__ __forceinline__ void step_one(const StepArgs &a, long long node, uint8_t c) {
+  using R = typename ST::R;
+  using T = typename ST::T;
+  if (c == CLS_SOLID) return;
+  const T *s = (const T *)a.src;
+  R F[9], rho, u, v;
+  if (c != CLS_SPECIAL) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) F[k] = ST::ld(s + pull_index<PH>(k, node, a), k, a);
+    bulk_store<ST, MODEL, PH>(a, node, c, F);
+    return;
+  } else {
+    R mac[3];
+    if constexpr (PH == PH_AB) special_node<R>(a, AccMain<ST, PH_AB>(a, a.src), node, F, mac);
+    else special_node<R>(a, AccSide<ST>(a, nullptr), node, F, mac);
+    rho = mac[0];
+    u = mac[1];
+    v = mac[2];
+  }
+  collide_store<ST, MODEL, PH>(a, node, c, F, rho, u, v);
+}
+
+// Fused step: METAF_t (layout PH) -> METAF_{t+1}.  A block is BX threads
+// along x; each thread updates NPT consecutive rows of its column.  When all
+// NPT nodes are free of boundary work their 9*NPT loads are issued before any
+// arithmetic (more bytes in flight per thread).
+template <class ST, int MODEL, int PH, int BX, int NPT>
+__global__ void __launch_bounds__(BX) k_step(const __grid_constant__ StepArgs a) {
+  using R = typename ST::R;
+  using T = typename ST::T;
+  const int x = blockIdx.x * BX + threadIdx.x;
+  const int y0 = blockIdx.y * NPT;
+  if (x >= a.n) return;
+  uint8_t c[NPT];
+  bool bulk = true;
+#pragma unroll
+  for (int j = 0; j < NPT; j++) {
+    const int y = y0 + j;
+    c[j] = (y < a.m) ? a.cls[(long long)y * a.pitch + x] : (uint8_t)CLS_SOLID;
+    bulk = bulk && c[j] != CLS_SPECIAL;
+  }
+  if (NPT == 1 || !bulk) {
+#pragma unroll
+    for (int j = 0; j < NPT; j++)
+      step_one<ST, MODEL, PH>(a, (long long)(y0 + j) * a.pitch + x, c[j]);
+    return;
+  }
+  const T *s = (const T *)a.src;
+  R F[NPT][9];
+#pragma unroll
+  for (int j = 0; j < NPT; j++) {
+    const long long node = (long long)(y0 + j) * a.pitch + x;
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+      F[j][k] = (c[j] != CLS_SOLID) ? ST::ld(s + pull_index<PH>(k, node, a), k, a) : R(0);
+  }
+#pragma unroll
+  for (int j = 0; j < NPT; j++) {
+    if (c[j] == CLS_SOLID) continue;
+    bulk_store<ST, MODEL, PH>(a, (long long)(y0 + j) * a.pitch + x, c[j], F[j]);
+  }
+}
+
+// Fused step over x-chunks: each thread owns V consecutive nodes of NPT rows
+// and moves every population plane with one aligned 4..16-byte word per
+// chunk.  The +-1 x-shift of the pull is served by a warp shuffle from the
+// neighbouring lane (lanes 0 and 31 read the chunk edge themselves).  Warps
+// that touch any node with boundary work fall back to the per-node path, so
+// the shuffles always run with the whole warp.
+template <class ST, int MODEL, int PH, int BX, int V, int NPT>
+__global__ void __launch_bounds__(BX) k_step_vec(const __grid_constant__ StepArgs a) {
+  using R = typename ST::R;
+  using T = typename ST::T;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int x0 = (blockIdx.x * BX + threadIdx.x) * V;
+  const int y0 = blockIdx.y * NPT;
+  if (x0 - lane * V >= a.pitch) return;  // the whole warp lies past the row
+  uint8_t cl[NPT][V];
+  bool special = false, fluid = false;
+#pragma unroll
+  for (int j = 0; j < NPT; j++)
+#pragma unroll
+    for (int i = 0; i < V; i++) {
+      const int y = y0 + j, x = x0 + i;
+      cl[j][i] = (y < a.m && x < a.n) ? a.cls[(long long)y * a.pitch + x] : (uint8_t)CLS_SOLID;
+      special = special || cl[j][i] == CLS_SPECIAL;
+      fluid = fluid || cl[j][i] != CLS_SOLID;
+    }
+  if (__any_sync(FULL, special)) {
+#pragma unroll
+    for (int j = 0; j < NPT; j++)
+#pragma unroll
+      for (int i = 0; i < V; i++)
+        if (x0 + i < a.n && y0 + j < a.m)
+          step_one<ST, MODEL, PH>(a, (long long)(y0 + j) * a.pitch + x0 + i, cl[j][i]);
+    return;
+  }
+  if (!__any_sync(FULL, fluid)) return;
+  const T *s = (const T *)a.src;
+  T *d = (T *)a.dst;
+  R F[NPT][V][9];
+#pragma unroll
+  for (int j = 0; j < NPT; j++) {
+    const int y = y0 + j;
+    const bool inner = y >= 1 && y < a.m - 1;  // warp-uniform: border rows are solid
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      if (!inner) {
+#pragma unroll
+        for (int i = 0; i < V; i++) F[j][i][k] = R(0);
+        continue;
+      }
+      const int plane = (PH == PH_AA_A) ? OPP[k] : k;
+      const int sx = (PH == PH_AA_B) ? 0 : CX[k];
+      const int row = (PH == PH_AA_B) ? y : y - CY[k];
+      const long long base = (long long)plane * a.plane + (long long)row * a.pitch + x0;
+      T raw[V];
+      VecIO<T, V>::load(s + base, raw);
+      R val[V];
+#pragma unroll
+      for (int i = 0; i < V; i++) val[i] = ST::cvt(raw[i], k, a);
+      if (sx == 0) {
+#pragma unroll
+        for (int i = 0; i < V; i++) F[j][i][k] = val[i];
+      } else if (sx == 1) {
+        R edge = __shfl_up_sync(FULL, val[V - 1], 1);
+        if (lane == 0) edge = x0 > 0 ? ST::ld(s + base - 1, k, a) : R(0);
+        F[j][0][k] = edge;
+#pragma unroll
+        for (int i = 1; i < V; i++) F[j][i][k] = val[i - 1];
+      } else {
+        R edge = __shfl_down_sync(FULL, val[0], 1);
+        if (lane == 31) edge = ST::ld(s + base + V, k, a);
+        F[j][V - 1][k] = edge;
+#pragma unroll
+        for (int i = 0; i < V - 1; i++) F[j][i][k] = val[i + 1];
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < NPT; j++) {
+    const int y = y0 + j;
+    if (!(y >= 1 && y < a.m - 1)) continue;
+    bool rowfluid = false;
+#pragma unroll
+    for (int i = 0; i < V; i++) {
+      rowfluid = rowfluid || cl[j][i] != CLS_SOLID;
+      R M[9];
+      if (cl[j][i] != CLS_SOLID) {
+        collide_bulk<MODEL, R>(F[j][i], a, M);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 9; k++) M[k] = R(0);
+      }
+#pragma unroll
+      for (int k = 0; k < 9; k++) F[j][i][k] = M[k];
+      if (PH != PH_AB && cl[j][i] == CLS_BULK_REC) {
+        const uint32_t sbi = a.aux[(long long)y * a.pitch + x0 + i];
+#pragma unroll
+        for (int k = 0; k < 9; k++) a.sb_dst[(size_t)sbi * 9 + k] = (double)M[k];
+      }
+    }
+    if (!rowfluid) continue;
+    const long long node0 = (long long)y * a.pitch + x0;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      if (PH == PH_AA_A) {
+        // neighbour write x + e_k: element-wise (only fluid nodes own a slot there)
+#pragma unroll
+        for (int i = 0; i < V; i++)
+          if (cl[j][i] != CLS_SOLID)
+            ST::st(d + (long long)k * a.plane + node0 + i + nb(k, a.pitch), k, F[j][i][k], a);
+      } else {
+        T raw[V];
+#pragma unroll
+        for (int i = 0; i < V; i++) raw[i] = ST::pack(F[j][i][k], k, a);
+        const int plane = (PH == PH_AB) ? k : OPP[k];
+        VecIO<T, V>::store(d + (long long)plane * a.plane + node0, raw);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------ 16-bit storage, paired nodes
+
+// Two adjacent nodes per thread, moved as one 32-bit word (two 16-bit
+// values) per population plane.  All 9 x NPT words of a thread are loaded
+// before any arithmetic; the +-1 x-shift of the pull is a warp shuffle of the
+// neighbouring lane's word and a byte permute (lanes 0 and 31 load the
+// half-word beyond the warp themselves, also up front).  Warps that touch a
+// node with boundary work run the per-node path instead, so the shuffles
+// always involve the whole warp.  Only for 2-byte storage.
+template <class ST>
+__device__ __forceinline__ void unpack2(uint32_t w, int k, const StepArgs &a, float &lo, float &hi) {
+  using T = typename ST::T;
+  T t[2];
+  memcpy(t, &w, 4);
+  lo = ST::cvt(t[0], k, a);
+  hi = ST::cvt(t[1], k, a);
+}
+template <class ST>
+__device__ __forceinline__ uint32_t pack2(float lo, float hi, int k, const StepArgs &a) {
+  using T = typename ST::T;
+  T t[2] = {ST::pack(lo, k, a), ST::pack(hi, k, a)};
+  uint32_t w;
+  memcpy(&w, t, 4);
+  return w;
+}
+
+// Edge half-word slot of a shifted plane: cx = +1 planes 1, 5, 8 (lane 0) and
+// cx = -1 planes 3, 6, 7 (lane 31) each use slots 0..2.
+__device__ __forceinline__ constexpr int edge_slot(int k) {
+  return (k == 1 || k == 3) ? 0 : ((k == 5 || k == 6) ? 1 : 2);
+}
+
+template <class ST, int MODEL, int PH, int NPT>
+__global__ void __launch_bounds__(128) k_step_h2(const __grid_constant__ StepArgs a) {
+  using T = typename ST::T;
+  static_assert(sizeof(T) == 2, "paired-node kernel is for 16-bit storage");
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int x0 = (blockIdx.x * 128 + threadIdx.x) * 2;
+  const int y0 = blockIdx.y * NPT;
+  if (x0 - lane * 2 >= a.pitch) return;  // the whole warp lies past the row
+  uint8_t cl[NPT][2];
+  bool special = false, fluid = false;
+#pragma unroll
+  for (int j = 0; j < NPT; j++)
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+      const int y = y0 + j, x = x0 + i;
+      cl[j][i] = (y < a.m && x < a.n) ? a.cls[(long long)y * a.pitch + x] : (uint8_t)CLS_SOLID;
+      special = special || cl[j][i] == CLS_SPECIAL;
+      fluid = fluid || cl[j][i] != CLS_SOLID;
+    }
+  if (__any_sync(FULL, special)) {
+#pragma unroll
+    for (int j = 0; j < NPT; j++)
+#pragma unroll
+      for (int i = 0; i < 2; i++)
+        if (x0 + i < a.n && y0 + j < a.m)
+          step_one<ST, MODEL, PH>(a, (long long)(y0 + j) * a.pitch + x0 + i, cl[j][i]);
+    return;
+  }
+  if (!__any_sync(FULL, fluid)) return;
+  const T *s = (const T *)a.src;
+  T *d = (T *)a.dst;
+  constexpr bool SHIFT = PH != PH_AA_B;
+  // ---- loads: every word first, the two warp-edge half-words alongside
+  uint32_t w[NPT][9];
+  T edge[NPT][3];  // lane 0: x0-1 for the cx=+1 planes; lane 31: x0+2 for cx=-1
+#pragma unroll
+  for (int j = 0; j < NPT; j++) {
+    const int y = y0 + j;
+    const bool inner = y >= 1 && y < a.m - 1;  // warp-uniform: border rows are solid
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      const int plane = (PH == PH_AA_A) ? OPP[k] : k;
+      const int row = SHIFT ? y - CY[k] : y;
+      const long long base = (long long)plane * a.plane + (long long)row * a.pitch + x0;
+      w[j][k] = inner ? __ldg((const unsigned *)(s + base)) : 0u;
+      if (SHIFT && CX[k] == 1 && lane == 0 && inner) edge[j][edge_slot(k)] = __ldg(s + base - 1);
+      if (SHIFT && CX[k] == -1 && lane == 31 && inner) edge[j][edge_slot(k)] = __ldg(s + base + 2);
+    }
+  }
+  // ---- per row: assemble the pulled pairs, collide, store
+#pragma unroll
+  for (int j = 0; j < NPT; j++) {
+    const int y = y0 + j;
+    if (!(y >= 1 && y < a.m - 1)) continue;
+    float F0[9], F1[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      uint32_t word = w[j][k];
+      if (SHIFT && CX[k] == 1) {
+        uint32_t prev = __shfl_up_sync(FULL, word, 1);
+        if (lane == 0) {
+          uint16_t h;
+          memcpy(&h, &edge[j][edge_slot(k)], 2);
+          prev = (uint32_t)h << 16;
+        }
+        word = __byte_perm(prev, word, 0x5432);  // (x0-1, x0)
+      } else if (SHIFT && CX[k] == -1) {
+        uint32_t next = __shfl_down_sync(FULL, word, 1);
+        if (lane == 31) {
+          uint16_t h;
+          memcpy(&h, &edge[j][edge_slot(k)], 2);
+          next = (uint32_t)h;
+        }
+        word = __byte_perm(word, next, 0x5432);  // (x0+1, x0+2)
+      }
+      unpack2<ST>(word, k, a, F0[k], F1[k]);
+    }
+    float M0[9], M1[9];
+    if (cl[j][0] != CLS_SOLID) collide_bulk<MODEL, float>(F0, a, M0);
+    else
+      for (int k = 0; k < 9; k++) M0[k] = 0.f;
+    if (cl[j][1] != CLS_SOLID) collide_bulk<MODEL, float>(F1, a, M1);
+    else
+      for (int k = 0; k < 9; k++) M1[k] = 0.f;
+    const long long node0 = (long long)y * a.pitch + x0;
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+      if (PH != PH_AB && cl[j][i] == CLS_BULK_REC) {
+        const uint32_t sbi = a.aux[node0 + i];
+        const float *M = i ? M1 : M0;
+#pragma unroll
+        for (int k = 0; k < 9; k++) a.sb_dst[(size_t)sbi * 9 + k] = (double)M[k];
+      }
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      if (PH == PH_AA_A) {
+        // neighbour write x + e_k, element-wise for fluid nodes
+        if (cl[j][0] != CLS_SOLID) ST::st(d + (long long)k * a.plane + node0 + nb(k, a.pitch), k, M0[k], a);
+        if (cl[j][1] != CLS_SOLID)
+          ST::st(d + (long long)k * a.plane + node0 + 1 + nb(k, a.pitch), k, M1[k], a);
+      } else {
+        const int plane = (PH == PH_AB) ? k : OPP[k];
+        __stcs((unsigned *)(d + (long long)plane * a.plane + node0), pack2<ST>(M0[k], M1[k], k, a));
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------- TMA pipeline
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+  uint64_t state;
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
+               : "=l"(state)
+               : "r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+  asm volatile("" ::"l"(state));
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: gives up after `polls` polls (each poll may suspend briefly).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int polls) {
+  for (int i = 0; i < polls; i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+// One contiguous global -> shared copy by the bulk-copy (TMA) engine; both
+// addresses 16-byte aligned, size a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                         uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// Fused step with TMA-staged sources.  The grid is persistent; a block walks
+// tiles of TX x TY nodes (rows 1..m-2, which hold every fluid node).  For each
+// tile warp 0 issues 10*TY bulk copies -- for every population plane the TY
+// source rows, TX + 2H elements wide (H = one 16-byte granule of halo on each
+// side, so every copy starts and ends on a 16-byte boundary), and the TY rows
+// of class bytes -- into one stage of a ring of shared-memory stages;
+// completion arrives on the stage's mbarrier.  Copies run a.tma_stages - 1
+// tiles ahead of the computation, so the bytes in flight are bounded by
+// shared memory, not registers, and the node loop reads its 9 inputs from
+// shared memory at fixed offsets.  Nodes with boundary work take the per-node
+// path with global loads (in the AA pattern their inputs live in the side
+// buffer anyway).  Shared-memory stage layout: populations [k][j][W], then
+// class bytes [j][TX].
+template <class T, int TX, int TY>
+struct TmaStage {
+  static constexpr int H = 16 / (int)sizeof(T);
+  static constexpr int W = TX + 2 * H;
+  static constexpr int POP_BYTES = 9 * TY * W * (int)sizeof(T);
+  static constexpr int BYTES = (POP_BYTES + TY * TX + 127) / 128 * 128;
+};
+
+template <class ST, int MODEL, int PH, int TX, int TY, int RPT>
+__global__ void __launch_bounds__(TX * TY / RPT, 3) k_step_tma(const __grid_constant__ StepArgs a) {
+  using R = typename ST::R;
+  using T = typename ST::T;
+  using G = TmaStage<T, TX, TY>;
+  constexpr int H = G::H, W = G::W;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  uint64_t *bars = (uint64_t *)smem_raw;
+  unsigned char *stages = smem_raw + 128;
+  const int S = a.tma_stages;
+  const int ntx = a.tma_tiles_x;
+  const int ntiles = ntx * a.tma_tiles_y;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const bool producer = tid < 32;
+  const T *src = (const T *)a.src;
+  if (tid == 0) {
+    for (int st = 0; st < S; st++) mbar_init(&bars[st], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  // executed by the 32 lanes of warp 0
+  auto issue = [&](int tile, int st) {
+    const int tx0 = (tile % ntx) * TX;
+    const int ty0 = 1 + (tile / ntx) * TY;
+    const int rows = min(TY, (a.m - 1) - ty0);
+    if (lane == 0) mbar_arrive_expect_tx(&bars[st], (uint32_t)(rows * (9 * W * sizeof(T) + TX)));
+    __syncwarp();
+    unsigned char *base = stages + (size_t)st * G::BYTES;
+    for (int q = lane; q < 10 * rows; q += 32) {
+      if (q < 9 * rows) {
+        const int k = q / rows, j = q - k * rows;
+        const int plane = (PH == PH_AA_A) ? OPP[k] : k;
+        const int dy = (PH == PH_AA_B) ? 0 : -CY[k];
+        const T *g = src + (long long)plane * a.plane + (long long)(ty0 + j + dy) * a.pitch + tx0 - H;
+        bulk_g2s(base + (size_t)(k * TY + j) * W * sizeof(T), g, (uint32_t)(W * sizeof(T)), &bars[st]);
+      } else {
+        const int j = q - 9 * rows;
+        bulk_g2s(base + G::POP_BYTES + j * TX, a.cls + (long long)(ty0 + j) * a.pitch + tx0,
+                 (uint32_t)TX, &bars[st]);
+      }
+    }
+  };
+
+  int issued = 0, consumed = 0;
+  if (producer)
+    for (int q = 0; q < S - 1; q++) {
+      const int t = blockIdx.x + q * gridDim.x;
+      if (t < ntiles) issue(t, q), issued++;
+    }
+  const int col = tid % TX, rgrp = tid / TX;
+  for (int tile = blockIdx.x, it = 0; tile < ntiles; tile += gridDim.x, it++) {
+    const int st = it % S;
+    if (producer) {
+      const int ahead = tile + (S - 1) * gridDim.x;
+      if (ahead < ntiles) {
+        // the stage being refilled was read through the generic proxy in the
+        // previous iteration (ordered by its trailing __syncthreads)
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        issue(ahead, (it + S - 1) % S);
+        issued++;
+      }
+    }
+    const bool ok = mbar_wait_bounded(&bars[st], (uint32_t)((it / S) & 1), 1 << 18);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        atomicExch(a.err, 1);
+        // let the copies still in flight land before the block's shared memory goes away
+        for (int q = consumed; q < issued; q++)
+          mbar_wait_bounded(&bars[q % S], (uint32_t)((q / S) & 1), 1 << 16);
+      }
+      return;
+    }
+    consumed++;
+    const int tx0 = (tile % ntx) * TX;
+    const int ty0 = 1 + (tile / ntx) * TY;
+    const unsigned char *base = stages + (size_t)st * G::BYTES;
+    const T *sb = (const T *)base;
+    const uint8_t *scls = base + G::POP_BYTES;
+    const int x = tx0 + col;
+#pragma unroll
+    for (int r = 0; r < RPT; r++) {
+      const int j = rgrp * RPT + r;
+      const int y = ty0 + j;
+      if (x >= a.n || y > a.m - 2) continue;
+      const uint8_t c = scls[j * TX + col];
+      if (c == CLS_SOLID) continue;
+      const long long node = (long long)y * a.pitch + x;
+      if (c == CLS_SPECIAL) {
+        step_one<ST, MODEL, PH>(a, node, c);
+        continue;
+      }
+      R F[9];
+#pragma unroll
+      for (int k = 0; k < 9; k++) {
+        const int dx = (PH == PH_AA_B) ? 0 : -CX[k];
+        F[k] = ST::cvt(sb[(k * TY + j) * W + H + col + dx], k, a);
+      }
+      bulk_store<ST, MODEL, PH>(a, node, c, F);
+    }
+    __syncthreads();
   }
 }
 
@@ -540,19 +1149,27 @@ __device__ __forceinline__ void block_reduce_store(double acc[NSUM], double *par
 }
 
 // Read-only: F_{t+1}, macroscopic fields and FP64 diagnostics from METAF_t.
+// Blocks stride over rows (grid.y may be smaller than m).  Per-cell terms are
+// formed in the storage's arithmetic type; with FP32/16-bit storage they are
+// summed in FP32 over at most 8 rows per thread and then in FP64, so that the
+// reductions are FP64 without an FP64 operation per term (GB300's FP64 rate
+// is a small fraction of its FP32 rate).
 template <class ST, int L>
 __global__ void __launch_bounds__(128) k_finish(const __grid_constant__ StepArgs a, const FinishOut o) {
   using R = typename ST::R;
-  int x = blockIdx.x * blockDim.x + threadIdx.x;
-  int y = blockIdx.y;
+  using T = typename ST::T;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
   double acc[NSUM];
+  R part[NSUM];
 #pragma unroll
-  for (int i = 0; i < NSUM; i++) acc[i] = 0.0;
-  if (x < a.n) {
+  for (int i = 0; i < NSUM; i++) acc[i] = 0.0, part[i] = R(0);
+  const T *src = (const T *)a.src;
+  AccMain<ST, L> acc_m(a, a.src);
+  int chunk = 0;
+  for (int y = blockIdx.y; y < a.m && x < a.n; y += gridDim.y) {
     const long long node = (long long)y * a.pitch + x;
     const long long cell = (long long)y * a.n + x;
     const uint8_t c = a.cls[node];
-    AccMain<ST, L> acc_m(a, a.src);
     if (c == CLS_SOLID) {
       if (o.f)
         for (int k = 0; k < 9; k++) o.f[cell * 9 + k] = 0.0;
@@ -561,58 +1178,80 @@ __global__ void __launch_bounds__(128) k_finish(const __grid_constant__ StepArgs
       if (o.rho) o.rho[cell] = o.rho_solid[cell];
       if (o.u) o.u[cell] = o.u_solid[cell];
       if (o.v) o.v[cell] = o.v_solid[cell];
-    } else {
-      R F[9], rho, u, v;
-      if (c != CLS_SPECIAL) {
-        boundary_F<false, R>(a, acc_m, node, F);
-        moments<R>(F, rho, u, v);
-      } else {
-        R mac[3];
-        special_node<R>(a, acc_m, node, F, mac);
-        rho = mac[0];
-        u = mac[1];
-        v = mac[2];
-      }
-      double l2 = 0.0;
+      continue;
+    }
+    R F[9], M[9], rho, u, v;
+    if (c != CLS_SPECIAL) {
+      // bulk: all neighbours fluid, plain loads in the state's layout
 #pragma unroll
       for (int k = 0; k < 9; k++) {
-        double mk = (double)acc_m.meta(node, k);
-        double dk = (double)F[k] - mk;
-        l2 += dk * dk;
-        if (o.f) o.f[cell * 9 + k] = (double)F[k];
-        if (o.metaf) o.metaf[cell * 9 + k] = mk;
+        F[k] = ST::ld(src + slot_of<L>(k, node - nb(k, a.pitch), a), k, a);
+        M[k] = ST::ld(src + slot_of<L>(k, node, a), k, a);
       }
-      if (o.rho) o.rho[cell] = (double)rho;
-      if (o.u) o.u[cell] = (double)u;
-      if (o.v) o.v[cell] = (double)v;
-      const double dr = rho, du = u, dv = v;
-      acc[S_L2] = l2;
-      acc[S_MASS] = dr;
-      acc[S_MX] = dr * du;
-      acc[S_MY] = dr * dv;
-      acc[S_UU] = du * du + dv * dv;
-      acc[S_VMAX] = sqrt(du * du + dv * dv);
-      acc[S_NAN] = (dr != dr || du != du || dv != dv) ? 1.0 : 0.0;
-      if (o.uprev) {
-        double pu = o.uprev[cell], pv = o.vprev[cell];
-        acc[S_DU] = (du - pu) * (du - pu) + (dv - pv) * (dv - pv);
-        o.uprev[cell] = (float)du;
-        o.vprev[cell] = (float)dv;
-      }
-      if (c == CLS_SPECIAL) {
-        const BRec &r = a.rec[a.aux[node]];
-        if (r.flags & FL_DRAG) {
-          // momentum exchange over the wall links of this cell
-          const uint32_t wall = (r.flags >> FL_WALL_SHIFT) & 0x1FFu;
-          for (int k = 1; k < 9; k++)
-            if ((wall >> k) & 1u) {
-              double g = (double)acc_m.meta(node, k) + (double)F[OPP[k]];
-              acc[S_FX] += g * CX[k];
-              acc[S_FY] += g * CY[k];
-            }
-        }
+      moments<R>(F, rho, u, v);
+    } else {
+      R mac[3];
+      special_node<R>(a, acc_m, node, F, mac);
+      rho = mac[0];
+      u = mac[1];
+      v = mac[2];
+#pragma unroll
+      for (int k = 0; k < 9; k++) M[k] = acc_m.meta(node, k);
+    }
+    R l2 = R(0);
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      R dk = F[k] - M[k];
+      l2 += dk * dk;
+    }
+    if (o.f)
+      for (int k = 0; k < 9; k++) o.f[cell * 9 + k] = (double)F[k];
+    if (o.metaf)
+      for (int k = 0; k < 9; k++) o.metaf[cell * 9 + k] = (double)M[k];
+    if (o.rho) o.rho[cell] = (double)rho;
+    if (o.u) o.u[cell] = (double)u;
+    if (o.v) o.v[cell] = (double)v;
+    const R uu = u * u + v * v;
+    part[S_L2] += l2;
+    part[S_MASS] += rho;
+    part[S_MX] += rho * u;
+    part[S_MY] += rho * v;
+    part[S_UU] += uu;
+    part[S_VMAX] = fmax(part[S_VMAX], sqrt(uu));
+    if (rho != rho || u != u || v != v) part[S_NAN] += R(1);
+    if (o.uprev) {
+      const R pu = (R)o.uprev[cell], pv = (R)o.vprev[cell];
+      part[S_DU] += (u - pu) * (u - pu) + (v - pv) * (v - pv);
+      o.uprev[cell] = (float)u;
+      o.vprev[cell] = (float)v;
+    }
+    if (c == CLS_SPECIAL) {
+      const BRec &r = a.rec[a.aux[node]];
+      if (r.flags & FL_DRAG) {
+        // momentum exchange over the wall links of this cell, in FP64
+        const uint32_t wall = (r.flags >> FL_WALL_SHIFT) & 0x1FFu;
+        for (int k = 1; k < 9; k++)
+          if ((wall >> k) & 1u) {
+            double g = (double)M[k] + (double)F[OPP[k]];
+            acc[S_FX] += g * CX[k];
+            acc[S_FY] += g * CY[k];
+          }
       }
     }
+    if (std::is_same<R, double>::value || ++chunk == 8) {
+      chunk = 0;
+#pragma unroll
+      for (int i = 0; i < NSUM; i++) {
+        if (i == S_VMAX) acc[i] = fmax(acc[i], (double)part[i]);
+        else if (i != S_FX && i != S_FY) acc[i] += (double)part[i];
+        part[i] = R(0);
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < NSUM; i++) {
+    if (i == S_VMAX) acc[i] = fmax(acc[i], (double)part[i]);
+    else if (i != S_FX && i != S_FY) acc[i] += (double)part[i];
   }
   block_reduce_store(acc, o.partial);
 }

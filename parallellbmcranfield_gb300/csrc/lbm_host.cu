@@ -52,12 +52,16 @@ struct lbm_ctx {
   int64_t g = 0;             // index of the METAF generation held on the device
   bool have_state = false;
   int64_t dev_bytes = 0;
+  int variant = 0;           // tile variant of the fused step
+  void *pop_raw[2] = {nullptr, nullptr};  // allocations behind pop[] (guard elements in front)
+  int *d_err = nullptr;      // device error word of bounded waits
   lbm::StepArgs base{};
 };
 
 namespace {
 
 constexpr int kBlock = 128;
+constexpr unsigned kFinishBlocks = 8192;  // partial rows of the diagnostics reduction
 
 template <class T>
 lbm_status dalloc(lbm_ctx *c, T **p, size_t count) {
@@ -72,7 +76,7 @@ lbm_status dalloc(lbm_ctx *c, T **p, size_t count) {
 }
 
 void release(lbm_ctx *c) {
-  void *ptrs[] = {c->pop[0], c->pop[1], c->sb[0],    c->sb[1],      c->d_cls,
+  void *ptrs[] = {c->pop_raw[0], c->pop_raw[1], c->sb[0], c->sb[1], c->d_cls, c->d_err,
                   c->d_aux,  c->d_rec,  c->d_rho0,   c->d_u0,       c->d_v0,
                   c->d_uprev, c->d_vprev, c->d_partial, c->d_sums, c->d_hist};
   for (void *q : ptrs)
@@ -109,14 +113,84 @@ lbm_status launch(const void *fn, dim3 grid, dim3 block, void **args, cudaStream
   return LBM_OK;
 }
 
+// Launch shape of tile variant `var` (grid, block, dynamic shared memory).
+// Returns false when the variant cannot run for this storage (TMA ring too
+// large for the shared-memory budget).
+bool step_config(lbm_ctx *c, int var, dim3 *grid, dim3 *block, size_t *smem) {
+  const lbm::TileVariant &V = lbm::VARS[var];
+  *smem = 0;
+  if (V.kind == 3 && c->ks->elem_size != 2) {  // runs as the scalar tile (bx 128)
+    *grid = dim3((unsigned)((c->P.n + 127) / 128), (unsigned)((c->P.m + V.npt - 1) / V.npt));
+    *block = dim3(128);
+    return true;
+  }
+  if (V.kind == 0 || V.kind == 1 || V.kind == 3) {
+    const int span = V.kind == 0 ? c->P.n : c->P.pitch;  // vector tiles cover whole padded rows
+    *grid = dim3((unsigned)((span + V.bx * V.v - 1) / (V.bx * V.v)),
+                 (unsigned)((c->P.m + V.npt - 1) / V.npt));
+    *block = dim3(V.bx);
+    return true;
+  }
+  // stage layout of k_step_tma: 9 population planes of ty rows of
+  // tx + 2 granules, then ty rows of tx class bytes, rounded to 128 bytes
+  const int es = c->ks->elem_size;
+  const int W = V.tx + 2 * (16 / es);
+  const size_t stage = ((size_t)9 * V.ty * W * es + (size_t)V.ty * V.tx + 127) / 128 * 128;
+  // ring depth: up to 4 stages within ~75 KB so that 3 blocks share an SM;
+  // a larger stage gets 2 stages within the 200 KB budget
+  int S = (int)((75 * 1024 - 128) / stage);
+  if (S > lbm::TMA_MAX_STAGES) S = lbm::TMA_MAX_STAGES;
+  if (S < 2) S = (128 + 2 * stage <= (size_t)lbm::TMA_MAX_SMEM) ? 2 : 0;
+  if (S < 2) return false;
+  *smem = 128 + (size_t)S * stage;
+  const int threads = V.tx * V.ty / V.rpt;
+  const void *fn = c->ks->step[c->p.collision_model][layout_of(c)][var];
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem) !=
+      cudaSuccess)
+    return false;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, *smem) != cudaSuccess ||
+      per_sm < 1)
+    return false;
+  int dev = c->p.device, sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int tiles_x = (c->P.pitch + V.tx - 1) / V.tx;
+  const int tiles_y = (c->P.m - 2 + V.ty - 1) / V.ty;
+  long long tiles = (long long)tiles_x * tiles_y;
+  long long blocks = (long long)sms * per_sm;
+  if (blocks > tiles) blocks = tiles;
+  *grid = dim3((unsigned)(blocks > 0 ? blocks : 1));
+  *block = dim3(threads);
+  c->base.tma_stages = S;
+  c->base.tma_tiles_x = tiles_x;
+  c->base.tma_tiles_y = tiles_y;
+  return true;
+}
+
 lbm_status launch_step(lbm_ctx *c) {
+  const int var = c->variant;
+  dim3 grid, block;
+  size_t smem;
+  if (!step_config(c, var, &grid, &block, &smem))
+    return fail(LBM_INVALID, "tile variant " + std::to_string(var + 1) + " cannot run here");
   lbm::StepArgs a = args_now(c);
   void *args[] = {&a};
-  int ph = layout_of(c);
-  lbm_status s = launch(c->ks->step[c->p.collision_model][ph], node_grid(c), dim3(kBlock), args,
-                        c->stream);
-  if (s != LBM_OK) return s;
+  const void *fn = c->ks->step[c->p.collision_model][layout_of(c)][var];
+  cudaError_t e = cudaLaunchKernel(fn, grid, block, args, smem, c->stream);
+  if (e != cudaSuccess) return fail(LBM_CUDA, std::string("step launch: ") + cudaGetErrorString(e));
   c->g++;
+  return LBM_OK;
+}
+
+// A bounded device wait that gave up sets the error word; report and clear it.
+lbm_status check_device_error(lbm_ctx *c) {
+  int h = 0;
+  LBM_CK(cudaMemcpyAsync(&h, c->d_err, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+  LBM_CK(cudaStreamSynchronize(c->stream));
+  if (h != 0) {
+    cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
+    return fail(LBM_TIMEOUT, "a bounded device wait (TMA stage barrier) gave up");
+  }
   return LBM_OK;
 }
 
@@ -126,13 +200,25 @@ lbm_status launch_resid(lbm_ctx *c, double *out) {
   return launch(c->ks->resid[layout_of(c)], dim3(1), dim3(256), args, c->stream);
 }
 
+// Grid of the finish kernel: one block column per 128 x positions, block rows
+// striding over the grid so that at most kFinishBlocks partial rows result.
+dim3 finish_grid(const lbm_ctx *c) {
+  dim3 g = node_grid(c);
+  unsigned rows = kFinishBlocks / g.x;
+  if (rows < 1) rows = 1;
+  if (rows < g.y) g.y = rows;
+  return g;
+}
+
 lbm_status launch_finish(lbm_ctx *c, lbm::FinishOut &o) {
   lbm::StepArgs a = args_now(c);
   o.partial = c->d_partial;
   void *args[] = {&a, &o};
-  lbm_status s = launch(c->ks->finish[layout_of(c)], node_grid(c), dim3(kBlock), args, c->stream);
+  const dim3 g = finish_grid(c);
+  int nb = (int)(g.x * g.y);
+  lbm_status s = launch(c->ks->finish[layout_of(c)], g, dim3(kBlock), args, c->stream);
   if (s != LBM_OK) return s;
-  void *rargs[] = {&c->d_partial, &c->nblk, &c->d_sums};
+  void *rargs[] = {&c->d_partial, &nb, &c->d_sums};
   return launch(c->ks->reduce, dim3(1), dim3(32 * lbm::NSUM), rargs,
                 c->stream);
 }
@@ -221,6 +307,11 @@ lbm_status lbm_create(const lbm_mesh *mesh, const lbm_params *params, lbm_ctx **
     delete c;
     return s;
   }
+  if (params->tile_variant < 0 || params->tile_variant > lbm::NVAR) {
+    delete c;
+    return fail(LBM_INVALID, "tile_variant must be 0 (default/tuned) or 1.." + std::to_string(lbm::NVAR));
+  }
+  c->variant = params->tile_variant > 0 ? params->tile_variant - 1 : 0;
   if (c->P.m > 65535) {
     delete c;
     return fail(LBM_INVALID, "grid taller than 65535 rows");
@@ -247,13 +338,22 @@ lbm_status lbm_create(const lbm_mesh *mesh, const lbm_params *params, lbm_ctx **
   }
   const lbm::Prep &P = c->P;
   const size_t N = (size_t)P.n * P.m;
-  const size_t pop_elems = (size_t)P.plane * 9;
+  // guard elements before the first and after the last plane: the 16-byte
+  // halo granules of the TMA row copies and the edge reads of the vector
+  // tiles reach up to 16 bytes (plus one row for the last tile) outside
+  const size_t guard = 1024;
+  const size_t pop_elems = (size_t)P.plane * 9 + 2 * guard + (size_t)P.pitch;
   const int npop = params->pattern == LBM_AB ? 2 : 1;
   for (int i = 0; i < npop; i++) {
-    if ((s = dalloc(c, (char **)&c->pop[i], pop_elems * c->ks->elem_size)) != LBM_OK) return bail(s);
-    if (cudaMemset(c->pop[i], 0, pop_elems * c->ks->elem_size) != cudaSuccess)
+    if ((s = dalloc(c, (char **)&c->pop_raw[i], pop_elems * c->ks->elem_size)) != LBM_OK)
+      return bail(s);
+    if (cudaMemset(c->pop_raw[i], 0, pop_elems * c->ks->elem_size) != cudaSuccess)
       return bail(fail(LBM_CUDA, "cudaMemset failed"));
+    c->pop[i] = (char *)c->pop_raw[i] + guard * c->ks->elem_size;
   }
+  if ((s = dalloc(c, &c->d_err, 1)) != LBM_OK) return bail(s);
+  if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess)
+    return bail(fail(LBM_CUDA, "cudaMemset failed"));
   if (params->pattern == LBM_AA)
     for (int i = 0; i < 2; i++)
       if ((s = dalloc(c, &c->sb[i], (size_t)P.nsb * 9)) != LBM_OK) return bail(s);
@@ -263,7 +363,7 @@ lbm_status lbm_create(const lbm_mesh *mesh, const lbm_params *params, lbm_ctx **
   if ((s = dalloc(c, &c->d_rho0, N)) != LBM_OK) return bail(s);
   if ((s = dalloc(c, &c->d_u0, N)) != LBM_OK) return bail(s);
   if ((s = dalloc(c, &c->d_v0, N)) != LBM_OK) return bail(s);
-  c->nblk = (int)(node_grid(c).x * node_grid(c).y);
+  c->nblk = (int)(finish_grid(c).x * finish_grid(c).y);
   if ((s = dalloc(c, &c->d_partial, (size_t)c->nblk * lbm::NSUM)) != LBM_OK) return bail(s);
   if ((s = dalloc(c, &c->d_sums, lbm::NSUM)) != LBM_OK) return bail(s);
   if (cudaMemcpy(c->d_cls, P.cls.data(), P.cls.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -297,6 +397,7 @@ lbm_status lbm_create(const lbm_mesh *mesh, const lbm_params *params, lbm_ctx **
     a.inv_scale[k] = (float)(1.0 / sc);
   }
   std::memcpy(a.stmiv, P.stmiv, sizeof a.stmiv);
+  a.err = c->d_err;
   *out = c;
   return LBM_OK;
 }
@@ -363,6 +464,7 @@ lbm_status lbm_step(lbm_ctx *ctx, int32_t nsteps, int32_t check_every, double *r
                            cudaMemcpyDeviceToHost, ctx->stream));
   LBM_CK(cudaStreamSynchronize(ctx->stream));
   LBM_CK(cudaGetLastError());
+  if ((s = check_device_error(ctx)) != LBM_OK) return s;
   if (residuals)
     for (int r = 0; r < rows; r++)
       if (residuals[4 * r] != residuals[4 * r])
@@ -472,5 +574,114 @@ extern "C" lbm_status lbm_check_noalloc(lbm_ctx *ctx, lbm_diagnostics *out) {
   out->du_rel = NAN;  // needs per-cell reference fields, which this variant cannot allocate
   if (h[lbm::S_NAN] > 0 || h[lbm::S_MASS] != h[lbm::S_MASS])
     return fail(LBM_DIVERGED, "NaN in the macroscopic fields");
+  return LBM_OK;
+}
+
+// ------------------------------------------------------------------ autotuner
+
+namespace {
+
+std::string tune_key(const lbm_ctx *c) {
+  cudaDeviceProp prop;
+  std::string gpu = "gpu";
+  if (cudaGetDeviceProperties(&prop, c->p.device) == cudaSuccess) gpu = prop.name;
+  const char *prec[] = {"fp64", "fp32", "fp16dev", "bf16dev"};
+  return gpu + "|" + prec[c->p.precision] + "|" + (c->p.pattern == LBM_AB ? "ab" : "aa") + "|m" +
+         std::to_string(c->p.collision_model) + "|" + std::to_string(c->P.n) + "x" +
+         std::to_string(c->P.m);
+}
+
+// Cache lines: {"key": "<key>", "variant": <v>, "ms": [..]} -- last line for a key wins.
+int cache_lookup(const char *path, const std::string &key) {
+  if (!path) return -1;
+  FILE *f = std::fopen(path, "r");
+  if (!f) return -1;
+  char line[1024];
+  int found = -1;
+  const std::string pat = "\"key\": \"" + key + "\"";
+  while (std::fgets(line, sizeof line, f)) {
+    const char *k = std::strstr(line, pat.c_str());
+    const char *v = std::strstr(line, "\"variant\": ");
+    if (k && v) {
+      int var = std::atoi(v + 11);
+      if (var >= 0 && var < lbm::NVAR) found = var;
+    }
+  }
+  std::fclose(f);
+  return found;
+}
+
+}  // namespace
+
+extern "C" lbm_status lbm_autotune(lbm_ctx *ctx, int32_t steps_per_trial, const char *cache_path,
+                                   char *report, size_t report_cap) {
+  if (!ctx) return fail(LBM_INVALID, "null argument");
+  if (ctx->have_state) return fail(LBM_INVALID, "lbm_autotune must run before lbm_set_state");
+  LBM_CK(cudaSetDevice(ctx->p.device));
+  const std::string key = tune_key(ctx);
+  std::string rep = "{\"key\": \"" + key + "\"";
+  int best = cache_lookup(cache_path, key);
+  if (best >= 0) {
+    ctx->variant = best;
+    rep += ", \"variant\": " + std::to_string(best) + ", \"cached\": true}";
+  } else {
+    if (steps_per_trial < 1) steps_per_trial = 1;
+    const size_t N = (size_t)ctx->P.n * ctx->P.m;
+    std::vector<double> rho(N, (double)ctx->p.rho_ini), zero(N, 0.0);
+    lbm_status s = set_state_impl(ctx, nullptr, rho.data(), zero.data(), zero.data(), false);
+    if (s != LBM_OK) return s;
+    cudaEvent_t e0, e1;
+    LBM_CK(cudaEventCreate(&e0));
+    LBM_CK(cudaEventCreate(&e1));
+    double ms[lbm::NVAR];
+    best = 0;
+    for (int v = 0; v < lbm::NVAR && s == LBM_OK; v++) {
+      dim3 g_, b_;
+      size_t sm_;
+      if (!step_config(ctx, v, &g_, &b_, &sm_)) {
+        ms[v] = INFINITY;
+        continue;
+      }
+      ctx->variant = v;
+      for (int i = 0; i < 2 && s == LBM_OK; i++) s = launch_step(ctx);
+      cudaEventRecord(e0, ctx->stream);
+      for (int i = 0; i < steps_per_trial && s == LBM_OK; i++) s = launch_step(ctx);
+      cudaEventRecord(e1, ctx->stream);
+      cudaEventSynchronize(e1);
+      float t = 0.f;
+      cudaEventElapsedTime(&t, e0, e1);
+      ms[v] = (double)t / steps_per_trial;
+      if (ms[v] < ms[best]) best = v;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s == LBM_OK) s = check_device_error(ctx);
+    ctx->have_state = false;  // the trial state is discarded
+    ctx->iter = 0;
+    ctx->g = 0;
+    if (s != LBM_OK) return s;
+    LBM_CK(cudaGetLastError());
+    ctx->variant = best;
+    std::string arr = "[";
+    char buf[64];
+    for (int v = 0; v < lbm::NVAR; v++) {
+      if (std::isinf(ms[v])) std::snprintf(buf, sizeof buf, "%snull", v ? ", " : "");
+      else std::snprintf(buf, sizeof buf, "%s%.5f", v ? ", " : "", ms[v]);
+      arr += buf;
+    }
+    arr += "]";
+    rep += ", \"variant\": " + std::to_string(best) + ", \"ms\": " + arr + "}";
+    if (cache_path) {
+      FILE *f = std::fopen(cache_path, "a");
+      if (f) {
+        std::fprintf(f, "%s\n", rep.c_str());
+        std::fclose(f);
+      }
+    }
+  }
+  if (report && report_cap > 0) {
+    std::strncpy(report, rep.c_str(), report_cap - 1);
+    report[report_cap - 1] = '\0';
+  }
   return LBM_OK;
 }

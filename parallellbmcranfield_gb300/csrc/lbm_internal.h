@@ -34,10 +34,19 @@ struct Prep {
 // the fused kernel cannot treat exactly.
 lbm_status preprocess(const lbm_mesh *mesh, const lbm_params *p, Prep *out);
 
-// Launch tables, one per storage precision (lbm_kernels_<prec>.cu).
+// Launch tables, one per storage precision, assembled (lbm_kernels_table.cpp)
+// from parts compiled separately (lbm_kernels_inst.cu).
+struct KernelPart {
+  const void *step[3][NVAR];  // [Phase][tile variant] of one collision model
+  const void *init[2];        // [0: AB, 1: AA]
+  const void *finish[3];
+  const void *resid[3];
+  const void *reduce;
+  int elem_size;
+};
 typedef void (*StepFn)(StepArgs);
 struct KernelSet {
-  const void *step[4][3];    // [model 1..3][Phase]
+  const void *step[4][3][NVAR];  // [model 1..3][Phase][tile variant]
   const void *init[4][2];    // [model 1..3][0: AB, 1: AA]
   const void *finish[3];     // [layout]
   const void *resid[3];      // [layout]

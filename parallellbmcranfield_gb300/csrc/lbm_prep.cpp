@@ -92,7 +92,7 @@ lbm_status preprocess(const lbm_mesh *mesh, const lbm_params *p, Prep *P) {
       for (int j = 0; j < 9; j++) P->stmiv[i * 9 + j] = ((double)MINV36[i][j] * a1) * sm[j];
   }
 
-  const int pitch = (n + 63) / 64 * 64;
+  const int pitch = (n + 255) / 256 * 256;  // whole warps of the widest vector tile
   P->pitch = pitch;
   P->plane = (long long)m * pitch;
   const size_t N = (size_t)n * m;

@@ -42,6 +42,24 @@ enum Phase : int {
   PH_AA_B = 2   // AA: state in B layout (slot k at x + e_k), output A layout
 };
 
+// Tile variants of the fused step.  kind 0: one thread per node column
+// with NPT rows (bx threads per block); kind 1: V nodes per thread moved as
+// one vector word per plane; kind 3: two nodes per thread as one 32-bit word
+// per plane, NPT rows (16-bit storage; other storage runs kind 0 with bx 128);
+// kind 2: TMA pipeline -- tiles of tx x ty nodes
+// whose 9 source planes are staged in shared memory by cp.async.bulk row
+// copies (a ring of stages, mbarrier completion), rpt rows per thread.  The
+// autotuner picks one per domain and storage.
+struct TileVariant {
+  int kind, bx, v, npt, tx, ty, rpt;
+};
+constexpr int NVAR = 6;
+constexpr TileVariant VARS[NVAR] = {
+    {0, 128, 1, 1, 0, 0, 0},   {0, 64, 1, 4, 0, 0, 0},   {1, 128, 4, 1, 0, 0, 0},
+    {2, 0, 0, 0, 128, 4, 2},   {3, 128, 2, 2, 0, 0, 0},  {3, 128, 2, 4, 0, 0, 0}};
+constexpr int TMA_MAX_SMEM = 200 * 1024;  // dynamic shared memory budget of one TMA block
+constexpr int TMA_MAX_STAGES = 4;
+
 constexpr int NSUM = 10;  // finish-kernel reduction lanes
 enum SumLane : int {
   S_L2 = 0, S_MASS, S_MX, S_MY, S_FX, S_FY, S_DU, S_UU, S_VMAX, S_NAN
@@ -62,6 +80,9 @@ struct StepArgs {
   double rho0;              // deviation reference density (16-bit storage)
   float scale[9], inv_scale[9];
   double stmiv[81];         // Minv * diag(s) of MRTInitializer, row-major
+  int *err;                 // device error word: set when a bounded wait gives up
+  int tma_stages;           // ring depth of the TMA step (from the shared-memory budget)
+  int tma_tiles_x, tma_tiles_y;
 };
 
 // Outputs of the read-only finish kernel (any pointer may be null).

@@ -84,6 +84,89 @@ def test_aa_equals_ab_bitwise(name):
         assert np.array_equal(fa[k], fb[k]), k
 
 
+@pytest.mark.parametrize("pattern", [G.AB, G.AA])
+@pytest.mark.parametrize("name", ["chan_mrt_extrap", "cavity_trt_curved"])
+@pytest.mark.parametrize("tile", [2, 3, 4, 5, 6])
+def test_tile_variants_bitwise(tile, pattern, name):
+    """Every tile variant of the fused step computes the same FP64 state."""
+    spec, params, start, steps = cases.ALL[name]
+    mesh = cases.build_mesh(spec)
+    out = []
+    for t in (1, tile):
+        s = G.Solver(mesh, precision=G.FP64, pattern=pattern, tile_variant=t, **params)
+        s.set_state(*cases.start_state(mesh, params, start))
+        s.step(steps)
+        out.append(s.fields(f=True, metaf=True))
+        s.close()
+    for k in out[0]:
+        assert np.array_equal(out[0][k], out[1][k]), k
+
+
+MID_CASES = {
+    # cases wide enough that whole warps of every tile shape see only bulk
+    # nodes, so the vector / paired / TMA paths run (not only the per-node path)
+    "mid_cavity": (("cavity", 300), dict(uavg=0.05, vavg=0.0, rho_ini=1.0, viscosity=0.02,
+                                         inlet_profile=2, collision_model=3, curved_boundaries=1,
+                                         outlet_profile=2), 120),
+    "mid_channel": (("channel", 700, 90, [(150.0, 45.5, 12.0)]),
+                    dict(uavg=0.04, vavg=0.0, rho_ini=1.0, viscosity=0.03, inlet_profile=1,
+                         collision_model=2, curved_boundaries=1, outlet_profile=2), 120),
+}
+
+
+def run_mid(name, precision, pattern, tile):
+    spec, params, steps = MID_CASES[name]
+    mesh = cases.build_mesh(spec)
+    s = G.Solver(mesh, precision=precision, pattern=pattern, tile_variant=tile, **params)
+    s.set_state(*cases.start_state(mesh, params, "feq"))
+    s.step(steps)
+    out = s.fields(f=True)
+    s.close()
+    return out
+
+
+@pytest.mark.parametrize("pattern", [G.AB, G.AA])
+@pytest.mark.parametrize("tile", [2, 3, 4, 5, 6])
+@pytest.mark.parametrize("name", sorted(MID_CASES))
+def test_tile_variants_bitwise_mid(name, tile, pattern):
+    """FP64 on the wider cases: every tile shape gives the bitwise-same state."""
+    a = run_mid(name, G.FP64, pattern, 1)
+    b = run_mid(name, G.FP64, pattern, tile)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("precision,tol", [(G.FP32, 1e-5), (G.FP16DEV, 2e-3), (G.BF16DEV, 2e-2)])
+@pytest.mark.parametrize("pattern", [G.AB, G.AA])
+@pytest.mark.parametrize("tile", [2, 3, 4, 5, 6])
+@pytest.mark.parametrize("name", sorted(MID_CASES))
+def test_tile_variants_reduced_precision(name, tile, pattern, precision, tol):
+    """Every tile reproduces the default tile's state in FP32 and 16-bit
+    storage.  The node arithmetic is the same, but the compiler may contract a
+    different set of multiply-adds in each kernel, so the check is at rounding
+    level (relative to max |field|)."""
+    a = run_mid(name, precision, pattern, 1)
+    b = run_mid(name, precision, pattern, tile)
+    for k in a:
+        assert rel_err(b[k], a[k]) <= tol, k
+
+
+def test_autotune_picks_a_variant(tmp_path):
+    spec, params, start, _ = cases.ALL["cavity_mrt_curved"]
+    mesh = cases.build_mesh(spec)
+    cache = tmp_path / "tune.jsonl"
+    s = G.Solver(mesh, precision=G.FP32, **params)
+    rep = s.autotune(3, cache)
+    assert 0 <= rep["variant"] < 6 and len(rep["ms"]) == 6
+    s.set_state(*cases.start_state(mesh, params, start))
+    s.step(10)
+    s2 = G.Solver(mesh, precision=G.FP32, **params)
+    rep2 = s2.autotune(3, cache)
+    assert rep2.get("cached") and rep2["variant"] == rep["variant"]
+    with pytest.raises(G.LbmError):
+        s.autotune(3)  # only before set_state
+
+
 def test_split_calls_equal_one_call():
     """lbm_step(a) + lbm_step(b) == lbm_step(a + b), with odd splits for AA parity."""
     _, one, _ = run_gpu("chan_mrt_extrap", G.FP64, G.AA, check_every=0, steps=101)

@@ -173,6 +173,40 @@ lbm_status lbm_inspect_mesh(const lbm_mesh *mesh, const lbm_params *params, int3
                             int32_t *m, uint8_t *cls, uint32_t *flags, double *q);
 
 /* ---------------------------------------------------------------------------
+ * Batches.  No counterpart in the reference, which runs one case per process:
+ * many independent domains (cavities, channels of different sizes and
+ * parameters) advanced together by one persistent launch per step over a
+ * device-side list of (case, tile).  Per-case convergence flags live on the
+ * device; each run segment (check_every steps and one check) is one CUDA graph
+ * replay.  All cases share precision (FP64, FP32 or FP16-dev), the A-B pattern,
+ * the collision model and the device; everything else is per case.
+ * ------------------------------------------------------------------------ */
+typedef struct lbm_batch lbm_batch;
+lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, int32_t ncases,
+                            lbm_batch **out);
+void lbm_batch_destroy(lbm_batch *b);
+/* Every case at rest: f = f_eq(rho_ini, 0, 0), then its first collision. */
+lbm_status lbm_batch_set_rest(lbm_batch *b);
+/* Fixes the batched step's tile shape (0..3: 128x1, 64x4, 128x2, 128x4 threads x rows). */
+lbm_status lbm_batch_set_tile(lbm_batch *b, int32_t tile_variant);
+/* Times the batched step's tile shapes and keeps the fastest (before stepping). */
+lbm_status lbm_batch_autotune(lbm_batch *b, int32_t steps_per_trial, char *report,
+                              size_t report_cap);
+/* Steps every unconverged case until all have converged or max_steps have run.
+ * Every check_every steps each active case gets du_rel = ||(u,v) - (u,v)_prev||
+ * / ||(u,v)|| against the previous check (FP64 sums); a case with du_rel <= tol
+ * stops stepping.  Per case (any pointer may be NULL): fused steps run (the
+ * completed iterations are one more), the last du_rel, converged (1 yes, 0 no,
+ * -1 NaN seen); seconds = wall time of the loop.  LBM_DIVERGED if a case saw NaN. */
+lbm_status lbm_batch_run(lbm_batch *b, int64_t max_steps, int32_t check_every, double tol,
+                         int64_t *steps, double *du_rel, int32_t *converged, double *seconds);
+lbm_status lbm_batch_get_fields(lbm_batch *b, int32_t case_index, double *rho, double *u,
+                                double *v);
+lbm_status lbm_batch_dims(const lbm_batch *b, int32_t case_index, int32_t *n, int32_t *m);
+lbm_status lbm_batch_info(const lbm_batch *b, int64_t *nodes, int64_t *fluid_nodes,
+                          int32_t *tile_variant, int64_t *device_bytes);
+
+/* ---------------------------------------------------------------------------
  * Mesh helpers (the reference's readers, serial/FileIO.c:14-289, and a
  * generator for meshes in the same format).  Buffers returned in lbm_mesh are
  * owned by the library and released with lbm_mesh_free.

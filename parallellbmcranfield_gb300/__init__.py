@@ -58,7 +58,9 @@ class lbm_diagnostics(C.Structure):
 EXPORTS = ["lbm_status_string", "lbm_last_error", "lbm_create", "lbm_destroy", "lbm_get_dims",
            "lbm_set_state", "lbm_step", "lbm_get_fields", "lbm_check", "lbm_check_noalloc",
            "lbm_get_info", "lbm_autotune",
-           "lbm_inspect_mesh", "lbm_mesh_read", "lbm_mesh_cavity", "lbm_mesh_channel", "lbm_mesh_write",
+           "lbm_inspect_mesh", "lbm_batch_create", "lbm_batch_destroy", "lbm_batch_set_rest", "lbm_batch_set_tile",
+           "lbm_batch_autotune", "lbm_batch_run", "lbm_batch_get_fields", "lbm_batch_dims",
+           "lbm_batch_info", "lbm_mesh_read", "lbm_mesh_cavity", "lbm_mesh_channel", "lbm_mesh_write",
            "lbm_mesh_free"]
 
 _lib = None
@@ -90,6 +92,17 @@ def load():
     L.lbm_get_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(i32)]
     L.lbm_inspect_mesh.argtypes = [C.POINTER(lbm_mesh), C.POINTER(lbm_params), C.POINTER(i32),
                                    C.POINTER(i32), dp, dp, dp]
+    L.lbm_batch_create.argtypes = [C.POINTER(lbm_mesh), C.POINTER(lbm_params), i32, C.POINTER(vp)]
+    L.lbm_batch_destroy.argtypes = [vp]
+    L.lbm_batch_destroy.restype = None
+    L.lbm_batch_set_rest.argtypes = [vp]
+    L.lbm_batch_set_tile.argtypes = [vp, i32]
+    L.lbm_batch_autotune.argtypes = [vp, i32, C.c_char_p, C.c_size_t]
+    L.lbm_batch_run.argtypes = [vp, C.c_int64, i32, C.c_double, dp, dp, dp, C.POINTER(C.c_double)]
+    L.lbm_batch_get_fields.argtypes = [vp, i32, dp, dp, dp]
+    L.lbm_batch_dims.argtypes = [vp, i32, C.POINTER(i32), C.POINTER(i32)]
+    L.lbm_batch_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(i32),
+                                 C.POINTER(C.c_int64)]
     L.lbm_mesh_read.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(lbm_mesh)]
     L.lbm_mesh_cavity.argtypes = [i32, C.POINTER(lbm_mesh)]
     L.lbm_mesh_channel.argtypes = [i32, i32, i32, dp, dp, dp, C.POINTER(lbm_mesh)]
@@ -97,7 +110,8 @@ def load():
     L.lbm_mesh_free.argtypes = [C.POINTER(lbm_mesh)]
     L.lbm_mesh_free.restype = None
     for name in EXPORTS:
-        if name not in ("lbm_destroy", "lbm_mesh_free", "lbm_status_string", "lbm_last_error"):
+        if name not in ("lbm_destroy", "lbm_mesh_free", "lbm_status_string", "lbm_last_error",
+                        "lbm_batch_destroy"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -276,3 +290,73 @@ class Solver:
 
     def __exit__(self, *a):
         self.close()
+
+
+class Batch:
+    """Many independent domains stepped together (wraps lbm_batch).
+
+    ``cases`` is a list of (Mesh, params dict); all cases share precision
+    (fp64, fp32 or fp16dev), the A-B pattern and the collision model.
+    """
+
+    def __init__(self, cases, precision=FP32, device=0):
+        L = self.L = load()
+        if isinstance(precision, str):
+            precision = PRECISIONS[precision]
+        self.meshes = [m for m, _ in cases]
+        self._mesh_structs = (lbm_mesh * len(cases))(*[m.c_struct() for m in self.meshes])
+        self._params = (lbm_params * len(cases))(
+            *[make_params(precision=precision, pattern=AB, device=device, **p) for _, p in cases])
+        self.h = C.c_void_p()
+        _check(L.lbm_batch_create(self._mesh_structs, self._params, len(cases), C.byref(self.h)),
+               "lbm_batch_create")
+        self.n_cases = len(cases)
+
+    def autotune(self, steps_per_trial=5):
+        import json
+        buf = C.create_string_buffer(512)
+        _check(self.L.lbm_batch_autotune(self.h, int(steps_per_trial), buf, len(buf)),
+               "lbm_batch_autotune")
+        return json.loads(buf.value.decode())
+
+    def set_rest(self):
+        _check(self.L.lbm_batch_set_rest(self.h), "lbm_batch_set_rest")
+
+    def set_tile(self, variant):
+        _check(self.L.lbm_batch_set_tile(self.h, int(variant)), "lbm_batch_set_tile")
+
+    def run(self, max_steps, check_every=100, tol=1e-6, raise_on_nan=True):
+        nc = self.n_cases
+        steps = np.zeros(nc, np.int64)
+        du = np.zeros(nc)
+        conv = np.zeros(nc, np.int32)
+        sec = C.c_double()
+        st = self.L.lbm_batch_run(self.h, int(max_steps), int(check_every), float(tol), _ptr(steps),
+                                  _ptr(du), _ptr(conv), C.byref(sec))
+        if st != LBM_DIVERGED or raise_on_nan:
+            _check(st, "lbm_batch_run")
+        return {"steps": steps, "du_rel": du, "converged": conv, "seconds": sec.value}
+
+    def fields(self, case):
+        n, m = C.c_int32(), C.c_int32()
+        _check(self.L.lbm_batch_dims(self.h, int(case), C.byref(n), C.byref(m)), "lbm_batch_dims")
+        N = n.value * m.value
+        out = {k: np.zeros(N) for k in ("rho", "u", "v")}
+        _check(self.L.lbm_batch_get_fields(self.h, int(case), _ptr(out["rho"]), _ptr(out["u"]),
+                                           _ptr(out["v"])), "lbm_batch_get_fields")
+        return out
+
+    def info(self):
+        nodes, fluid, dev = C.c_int64(), C.c_int64(), C.c_int64()
+        var = C.c_int32()
+        _check(self.L.lbm_batch_info(self.h, C.byref(nodes), C.byref(fluid), C.byref(var),
+                                     C.byref(dev)), "lbm_batch_info")
+        return {"nodes": nodes.value, "fluid_nodes": fluid.value, "tile_variant": var.value,
+                "device_bytes": dev.value}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.lbm_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close

@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblbm_gb300.so")
+SOLVER = os.path.join(HERE, "bin", "lbm_solver")  # drop-in for the serial program
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -27,6 +28,7 @@ def _nvcc():
 
 
 INST = "lbm_kernels_inst.cu"  # compiled once per (precision, part)
+BATCH_INST = "lbm_batch_inst.cu"  # compiled once per batch precision (FP64, FP32, FP16-dev)
 PRECS = ["f64", "f32", "f16", "b16"]
 
 
@@ -41,7 +43,11 @@ def sources():
                     if name == "f64":
                         flags.append("--fmad=false")
                     units.append((f"lbm_kernels_{name}_{part}", f, flags))
-        elif f.endswith((".cu", ".cpp")):
+        elif f == BATCH_INST:
+            for p in range(3):
+                flags = [f"-DLBM_PREC={p}"] + (["--fmad=false"] if p == 0 else [])
+                units.append((f"lbm_batch_{PRECS[p]}", f, flags))
+        elif f.endswith((".cu", ".cpp")) and not f.endswith("_main.cpp"):
             units.append((os.path.splitext(f)[0], f, []))
     return units
 
@@ -107,6 +113,14 @@ def build(verbose=False, jobs=None):
     if jobs_ or not os.path.exists(LIB):
         cmd = [_nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart_static", "-lrt",
                "-ldl", "-lpthread"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        subprocess.check_call(cmd)
+    main = os.path.join(CSRC, "lbm_solver_main.cpp")
+    if _stale(SOLVER, [main, LIB, os.path.join(os.path.dirname(HERE), "include", "lbm_gb300.h")]):
+        os.makedirs(os.path.dirname(SOLVER), exist_ok=True)
+        cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", main, "-o", SOLVER,
+               "-L", HERE, "-llbm_gb300", "-Wl,-rpath,$ORIGIN/.."]
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.check_call(cmd)

@@ -1,0 +1,136 @@
+// Batched stepping of many independent domains (cavities, channels) with one
+// launch per step: a device-side work list of (case, tile) is walked by a
+// persistent grid; per-case parity, step counters and convergence flags live
+// on the device so that a whole run segment (steps + check) can be captured
+// in one CUDA graph.
+#pragma once
+#include "lbm_device.cuh"
+
+namespace lbm {
+
+// Per-case launch arguments for both A-B parities (args[p] reads buffer p).
+struct BatchCase {
+  StepArgs args[2];
+  float *uprev, *vprev;  // du_rel reference fields, n*m
+};
+
+// Tile shapes of the batched step (threads along x, rows per thread).
+constexpr int BVAR = 4;
+constexpr int BVAR_BX[BVAR] = {128, 64, 128, 128};
+constexpr int BVAR_NPT[BVAR] = {1, 4, 2, 4};
+
+struct BatchState {
+  int *active;        // 1 while the case still steps
+  int *gpar;          // METAF generation parity of each case
+  long long *steps;   // iterations completed by each case
+  double *acc;        // per case: sum |du|^2, sum |u|^2
+  int *bad;           // per case: NaN seen
+  double *du_last;    // per case: du_rel of the last check
+  int *have_prev;     // per case: reference fields valid
+  long long *conv_at; // per case: iteration at which du_rel <= tol was first seen (-1)
+};
+
+template <class ST, int MODEL, int BX, int NPT>
+__global__ void __launch_bounds__(BX) k_batch_step(const BatchCase *cases, const int4 *tiles,
+                                                   int ntiles, const int *active,
+                                                   const int *gpar) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int4 tl = tiles[t];
+    if (!active[tl.x]) continue;
+    const StepArgs &a = cases[tl.x].args[gpar[tl.x] & 1];
+    step_column<ST, MODEL, PH_AB, NPT>(a, tl.y * BX + threadIdx.x, tl.z * NPT);
+  }
+}
+
+// After a step: active cases advance their parity and counters.
+static __global__ void k_batch_advance(int ncases, BatchState s) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < ncases && s.active[c]) {
+    s.gpar[c]++;
+    s.steps[c]++;
+  }
+}
+
+// du_rel sums of every active case: tiles are 128 positions of one row.
+template <class ST>
+__global__ void __launch_bounds__(128) k_batch_du(const BatchCase *cases, const int4 *rows,
+                                                  int nrows, BatchState s) {
+  using R = typename ST::R;
+  __shared__ double sh[2][4];
+  for (int t = blockIdx.x; t < nrows; t += gridDim.x) {
+    const int4 tl = rows[t];
+    const int c = tl.x;
+    if (!s.active[c]) continue;  // uniform per block
+    const BatchCase &bc = cases[c];
+    const StepArgs &a = bc.args[s.gpar[c] & 1];
+    const int x = tl.y * 128 + threadIdx.x, y = tl.z;
+    double du = 0.0, uu = 0.0;
+    int bad = 0;
+    if (x < a.n) {
+      const long long node = (long long)y * a.pitch + x;
+      const uint8_t cl = a.cls[node];
+      if (cl != CLS_SOLID) {
+        AccMain<ST, PH_AB, ST::SHIFT> acc(a, a.src);  // deviations for shifted storage
+        R F[9], rho, u, v;
+        if (cl != CLS_SPECIAL) {
+          boundary_F<false, R>(a, acc, node, F);
+          moments_form<ST>(F, a, rho, u, v);
+        } else {
+          R mac[3];
+          special_node<R>(a, acc, node, F, mac);
+          rho = mac[0];
+          u = mac[1];
+          v = mac[2];
+        }
+        const long long cell = (long long)y * a.n + x;
+        const double pu = bc.uprev[cell], pv = bc.vprev[cell];
+        du = ((double)u - pu) * ((double)u - pu) + ((double)v - pv) * ((double)v - pv);
+        uu = (double)u * u + (double)v * v;
+        bc.uprev[cell] = (float)u;
+        bc.vprev[cell] = (float)v;
+        bad = (rho != rho || u != u || v != v);
+      }
+    }
+    du = warp_sum(du);
+    uu = warp_sum(uu);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+      sh[0][wid] = du;
+      sh[1][wid] = uu;
+    }
+    const int anybad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) {
+      atomicAdd(&s.acc[2 * c], sh[0][0] + sh[0][1] + sh[0][2] + sh[0][3]);
+      atomicAdd(&s.acc[2 * c + 1], sh[1][0] + sh[1][1] + sh[1][2] + sh[1][3]);
+      if (anybad) s.bad[c] = 1;
+    }
+    __syncthreads();
+  }
+}
+
+// Per-case convergence decision after k_batch_du.
+static __global__ void k_batch_converge(int ncases, BatchState s, double tol) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncases || !s.active[c]) return;
+  const double uu = s.acc[2 * c + 1];
+  const double du = uu > 0 ? sqrt(s.acc[2 * c] / uu) : INFINITY;
+  s.du_last[c] = s.have_prev[c] ? du : INFINITY;
+  if (s.bad[c]) {
+    s.active[c] = 0;  // diverged: frozen, reported by the host
+  } else if (s.have_prev[c] && du <= tol) {
+    s.active[c] = 0;
+    s.conv_at[c] = s.steps[c];
+  }
+  s.have_prev[c] = 1;
+  s.acc[2 * c] = 0.0;
+  s.acc[2 * c + 1] = 0.0;
+}
+
+struct BatchKernels {
+  const void *step[4][BVAR];  // [model 1..3][tile shape]
+  const void *du;
+  const void *advance;
+  const void *converge;
+};
+
+}  // namespace lbm

@@ -41,28 +41,50 @@ __device__ __forceinline__ R wgt(int k) {
 
 // ------------------------------------------------------------ storage policies
 
+// Each policy gives absolute populations (cvt / pack / ld / st, used by the
+// boundary paths and the read-back) and, for the bulk path, populations in
+// the form its arithmetic uses (cvt_dev / pack_dev / ld_dev / st_dev): with
+// SHIFT the deviations f_k - w_k rho0 ("DDF shifting"), which keeps the
+// rounding of FP32 arithmetic and of 16-bit storage relative to the small
+// deviations instead of to f ~ w_k rho0.  FP64 (the parity mode) stays absolute.
 struct StF64 {
   using T = double;
   using R = double;
+  static constexpr bool SHIFT = false;
   static __device__ __forceinline__ R cvt(T v, int, const StepArgs &) { return v; }
   static __device__ __forceinline__ T pack(R v, int, const StepArgs &) { return v; }
   static __device__ __forceinline__ R ld(const T *p, int, const StepArgs &) { return __ldg(p); }
   static __device__ __forceinline__ void st(T *p, int, R v, const StepArgs &) { *p = v; }
+  static __device__ __forceinline__ R cvt_dev(T v, int k, const StepArgs &a) { return cvt(v, k, a); }
+  static __device__ __forceinline__ T pack_dev(R v, int k, const StepArgs &a) { return pack(v, k, a); }
 };
 
+// FP32 storage of d_k = f_k - w_k rho0.
 struct StF32 {
   using T = float;
   using R = float;
-  static __device__ __forceinline__ R cvt(T v, int, const StepArgs &) { return v; }
-  static __device__ __forceinline__ T pack(R v, int, const StepArgs &) { return v; }
-  static __device__ __forceinline__ R ld(const T *p, int, const StepArgs &) { return __ldg(p); }
-  static __device__ __forceinline__ void st(T *p, int, R v, const StepArgs &) { __stcs(p, v); }
+  static constexpr bool SHIFT = true;
+  static __device__ __forceinline__ R cvt(T v, int k, const StepArgs &a) {
+    return v + wgt<float>(k) * (float)a.rho0;
+  }
+  static __device__ __forceinline__ T pack(R v, int k, const StepArgs &a) {
+    return v - wgt<float>(k) * (float)a.rho0;
+  }
+  static __device__ __forceinline__ R ld(const T *p, int k, const StepArgs &a) {
+    return cvt(__ldg(p), k, a);
+  }
+  static __device__ __forceinline__ void st(T *p, int k, R v, const StepArgs &a) {
+    __stcs(p, pack(v, k, a));
+  }
+  static __device__ __forceinline__ R cvt_dev(T v, int, const StepArgs &) { return v; }
+  static __device__ __forceinline__ T pack_dev(R v, int, const StepArgs &) { return v; }
 };
 
 // 16-bit storage of s_k = (f_k - w_k rho0) * scale_k; arithmetic in FP32.
 struct StF16 {
   using T = __half;
   using R = float;
+  static constexpr bool SHIFT = true;
   static __device__ __forceinline__ R cvt(T v, int k, const StepArgs &a) {
     return fmaf(__half2float(v), a.inv_scale[k], wgt<float>(k) * (float)a.rho0);
   }
@@ -73,11 +95,18 @@ struct StF16 {
     return cvt(__ldg(p), k, a);
   }
   static __device__ __forceinline__ void st(T *p, int k, R v, const StepArgs &a) { *p = pack(v, k, a); }
+  static __device__ __forceinline__ R cvt_dev(T v, int k, const StepArgs &a) {
+    return __half2float(v) * a.inv_scale[k];
+  }
+  static __device__ __forceinline__ T pack_dev(R v, int k, const StepArgs &a) {
+    return __float2half_rn(v * a.scale[k]);
+  }
 };
 
 struct StB16 {
   using T = __nv_bfloat16;
   using R = float;
+  static constexpr bool SHIFT = true;
   static __device__ __forceinline__ R cvt(T v, int k, const StepArgs &a) {
     return fmaf(__bfloat162float(v), a.inv_scale[k], wgt<float>(k) * (float)a.rho0);
   }
@@ -88,6 +117,12 @@ struct StB16 {
     return cvt(__ldg(p), k, a);
   }
   static __device__ __forceinline__ void st(T *p, int k, R v, const StepArgs &a) { *p = pack(v, k, a); }
+  static __device__ __forceinline__ R cvt_dev(T v, int k, const StepArgs &a) {
+    return __bfloat162float(v) * a.inv_scale[k];
+  }
+  static __device__ __forceinline__ T pack_dev(R v, int k, const StepArgs &a) {
+    return __float2bfloat16_rn(v * a.scale[k]);
+  }
 };
 
 // Aligned loads / streaming stores of V consecutive elements as 4..16-byte words.
@@ -137,6 +172,22 @@ struct VecIO {
   }
 };
 
+// Bulk-form load / streaming store of one population.
+template <class ST>
+__device__ __forceinline__ typename ST::R ld_dev(const typename ST::T *p, int k,
+                                                 const StepArgs &a) {
+  return ST::cvt_dev(__ldg(p), k, a);
+}
+template <class ST>
+__device__ __forceinline__ void st_dev(typename ST::T *p, int k, typename ST::R v,
+                                       const StepArgs &a) {
+  if constexpr (sizeof(typename ST::T) == 2) {
+    *p = ST::pack_dev(v, k, a);
+  } else {
+    __stcs(p, ST::pack_dev(v, k, a));
+  }
+}
+
 // Offset of the neighbour x + e_k in linear node index.
 __device__ __forceinline__ long long nb(int k, int pitch) {
   return (long long)CX[k] + (long long)CY[k] * pitch;
@@ -154,33 +205,38 @@ __device__ __forceinline__ long long slot_of(int k, long long z, const StepArgs 
 }
 
 // Read METAF[k](z) of the state (solid and padding cells read as 0, as the
-// reference's never-collided solid cells do).
-template <class ST, int L>
+// reference's never-collided solid cells do).  With DEV the value comes back
+// as the deviation METAF - w_k rho0 (a solid cell's 0 becomes -w_k rho0).
+template <class ST, int L, bool DEV = false>
 struct AccMain {
   using R = typename ST::R;
+  static constexpr bool dev = DEV;
   const StepArgs &a;
   const typename ST::T *s;
   __device__ AccMain(const StepArgs &a_, const void *src)
       : a(a_), s((const typename ST::T *)src) {}
   __device__ __forceinline__ R meta(long long z, int k) const {
-    if (a.cls[z] == CLS_SOLID) return R(0);
-    return ST::ld(s + slot_of<L>(k, z, a), k, a);
+    if (a.cls[z] == CLS_SOLID) return DEV ? -wgt<R>(k) * (R)a.rho0 : R(0);
+    const typename ST::T *p = s + slot_of<L>(k, z, a);
+    return DEV ? ST::cvt_dev(__ldg(p), k, a) : ST::ld(p, k, a);
   }
 };
 
 // AA pattern: METAF of recorded nodes comes from the side buffer of the
 // current parity, never from the in-place array another thread rewrites.
-template <class ST>
+template <class ST, bool DEV = false>
 struct AccSide {
   using R = typename ST::R;
+  static constexpr bool dev = DEV;
   const StepArgs &a;
   __device__ AccSide(const StepArgs &a_, const void *) : a(a_) {}
   __device__ __forceinline__ R meta(long long z, int k) const {
     uint8_t c = a.cls[z];
-    if (c == CLS_SOLID) return R(0);
+    if (c == CLS_SOLID) return DEV ? -wgt<R>(k) * (R)a.rho0 : R(0);
     uint32_t s = a.aux[z];
     if (c == CLS_SPECIAL) s = a.rec[s].sb;
-    return (R)a.sb_src[(size_t)s * 9 + k];
+    const double v = a.sb_src[(size_t)s * 9 + k];
+    return DEV ? (R)(v - wgt<double>(k) * a.rho0) : (R)v;
   }
 };
 
@@ -209,6 +265,26 @@ __device__ __forceinline__ void moments(const R F[9], R &rho, R &u, R &v) {
     R inv = R(1) / rho;
     u = jx * inv;
     v = jy * inv;
+  }
+}
+
+// Moments of populations in the storage's bulk form (deviations for the
+// shifted storages: rho = rho0 + sum d, j = sum c d; absolute otherwise).
+template <class ST>
+__device__ __forceinline__ void moments_form(const typename ST::R F[9], const StepArgs &a,
+                                             typename ST::R &rho, typename ST::R &u,
+                                             typename ST::R &v) {
+  using R = typename ST::R;
+  if constexpr (ST::SHIFT) {
+    R rt = ((F[0] + F[1]) + (F[2] + F[3])) + ((F[4] + F[5]) + (F[6] + F[7])) + F[8];
+    R jx = (F[1] - F[3]) + (F[5] - F[6]) + (F[8] - F[7]);
+    R jy = (F[2] - F[4]) + (F[5] - F[7]) + (F[6] - F[8]);
+    rho = (R)a.rho0 + rt;
+    R inv = R(1) / rho;
+    u = jx * inv;
+    v = jy * inv;
+  } else {
+    moments<R>(F, rho, u, v);
   }
 }
 
@@ -401,6 +477,88 @@ __device__ __forceinline__ void collide_bulk(const R F[9], const StepArgs &a, R 
   }
 }
 
+// Bulk collision in the storage's bulk form: FP64 absolute (collide_bulk
+// above, the reference's arithmetic); the shifted storages take and return
+// deviations d_k = f_k - w_k rho0.  With rho~ = sum d (= rho - rho0) and
+// j = sum c d, the operators are the same as on f: the MRT rows 1, 2 see
+// M w = (1, -2, 1, 0, ...) so m1 + 2 rho becomes m1(d) + 2 rho~ and
+// m2 - rho becomes m2(d) - rho~; BGK/TRT use f_eq - w rho0 =
+// w (rho~ + rho (3 c.u + 4.5 (c.u)^2 - 1.5 u^2)).
+template <int MODEL, class ST>
+__device__ __forceinline__ void collide_bulk_dev(const typename ST::R F[9], const StepArgs &a,
+                                                 typename ST::R M[9]) {
+  using R = typename ST::R;
+  if constexpr (!ST::SHIFT) {
+    collide_bulk<MODEL, R>(F, a, M);
+  } else if constexpr (MODEL == 3) {
+    const R om = (R)a.omega;
+    R a13 = F[1] + F[3], a24 = F[2] + F[4];
+    R a14 = a13 + a24;
+    R p57 = F[5] + F[7], p68 = F[6] + F[8];
+    R a58 = p57 + p68;
+    R rt = (F[0] + a14) + a58;
+    R rho = (R)a.rho0 + rt;
+    R m1 = R(2) * a58 - a14 - R(4) * F[0];
+    R m2 = (R(4) * F[0] + a58) - R(2) * a14;
+    R d13 = F[1] - F[3], d24 = F[2] - F[4];
+    R e57 = F[5] - F[7], e86 = F[8] - F[6];
+    R x58 = e57 + e86, y58 = e57 - e86;
+    R jx = d13 + x58, jy = d24 + y58;
+    R m4 = x58 - R(2) * d13, m6 = y58 - R(2) * d24;
+    R m7 = a13 - a24, m8 = p57 - p68;
+    R inv = R(1) / rho;
+    R jj = jx * jx + jy * jy;
+    R d1 = R(1.4) * (m1 + R(2) * rt - R(3) * jj);
+    R d2 = R(1.4) * (m2 - rt + R(3) * jj);
+    R d4 = R(1.2) * (m4 + jx);
+    R d6 = R(1.2) * (m6 + jy);
+    R d7 = om * (m7 - (jx * jx - jy * jy) * inv);
+    R d8 = om * (m8 - jx * jy * inv);
+    const R c = R(1.0 / 36.0);
+    R ax = -d1 - R(2) * d2;
+    R dg = R(2) * d1 + d2;
+    R X = R(-6) * d4, Y = R(-6) * d6, P = R(9) * d7;
+    R Xd = R(3) * d4, Yd = R(3) * d6, Q = R(9) * d8;
+    M[0] = F[0] - c * (R(4) * (d2 - d1));
+    M[1] = F[1] - c * (ax + X + P);
+    M[2] = F[2] - c * (ax + Y - P);
+    M[3] = F[3] - c * (ax - X + P);
+    M[4] = F[4] - c * (ax - Y - P);
+    M[5] = F[5] - c * (dg + Xd + Yd + Q);
+    M[6] = F[6] - c * (dg - Xd + Yd - Q);
+    M[7] = F[7] - c * (dg - Xd - Yd + Q);
+    M[8] = F[8] - c * (dg + Xd - Yd - Q);
+  } else {
+    R rt = ((F[0] + F[1]) + (F[2] + F[3])) + ((F[4] + F[5]) + (F[6] + F[7])) + F[8];
+    R jx = (F[1] - F[3]) + (F[5] - F[6]) + (F[8] - F[7]);
+    R jy = (F[2] - F[4]) + (F[5] - F[7]) + (F[6] - F[8]);
+    R rho = (R)a.rho0 + rt;
+    R inv = R(1) / rho;
+    R u = jx * inv, v = jy * inv;
+    R T1 = u * u + v * v;
+    R feq[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      R T2 = u * CX[k] + v * CY[k];
+      feq[k] = wgt<R>(k) * (rt + rho * (R(3) * T2 + R(4.5) * T2 * T2 - R(1.5) * T1));
+    }
+    if (MODEL == 1) {
+      const R om = (R)a.omega;
+#pragma unroll
+      for (int k = 0; k < 9; k++) M[k] = fmaf(om, feq[k] - F[k], F[k]);
+    } else {
+      const R om = (R)a.omega, omA = (R)a.omegaA;
+#pragma unroll
+      for (int k = 0; k < 9; k++) {
+        const int o = OPP[k];
+        R sp = R(0.5) * ((F[k] + F[o]) - (feq[k] + feq[o]));
+        R sm = R(0.5) * ((F[k] - F[o]) - (feq[k] - feq[o]));
+        M[k] = F[k] - om * sp - omA * sm;
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------ boundary conditions
 
 // F of a special node after streaming and the inlet / wall treatments of
@@ -408,6 +566,11 @@ __device__ __forceinline__ void collide_bulk(const R F[9], const StepArgs &a, R 
 // when OUTLET is set (serial/Iterate.c:525-546).  Any node class is accepted:
 // solid returns 0 (UpdateF copied the never-written METAF), bulk returns the
 // plain pull.  `acc` reads METAF of the current state.
+//
+// With an accessor in deviation form (ACC::dev) F is returned as deviations
+// d_k = F_k - w_k rho0.  Every treatment keeps its form because it only
+// copies or combines populations of equal weight with coefficients summing to
+// one; the density sums gain rho0 (the weights in each sum add up to 1).
 template <bool OUTLET, class R, class ACC>
 __device__ void boundary_F(const StepArgs &a, const ACC &acc, long long node, R F[9]);
 
@@ -419,10 +582,12 @@ __device__ __noinline__ void boundary_F_noout(const StepArgs &a, const ACC &acc,
 
 template <bool OUTLET, class R, class ACC>
 __device__ void boundary_F(const StepArgs &a, const ACC &acc, long long node, R F[9]) {
+  constexpr bool DEV = ACC::dev;
+  const R rho0 = DEV ? (R)a.rho0 : R(0);
   const uint8_t c = a.cls[node];
   if (c == CLS_SOLID) {
 #pragma unroll
-    for (int k = 0; k < 9; k++) F[k] = R(0);
+    for (int k = 0; k < 9; k++) F[k] = DEV ? -wgt<R>(k) * rho0 : R(0);
     return;
   }
   if (c != CLS_SPECIAL) {
@@ -441,12 +606,15 @@ __device__ void boundary_F(const StepArgs &a, const ACC &acc, long long node, R 
   // InletBC, serial/BoundaryConditions.c:25-50
   if (fl & FL_LID) {
     R rhoN = F[0] + F[1] + F[3] + R(2) * (F[2] + F[6] + F[5]);
+    if (DEV) rhoN = rho0 + rhoN;
     F[4] = F[2];
     F[8] = F[6] + rhoN * uo / R(6.0);
     F[7] = F[5] - rhoN * uo / R(6.0);
   }
   if (fl & FL_WEST) {
-    R rhoW = (F[0] + F[2] + F[4] + R(2.0) * (F[3] + F[6] + F[7])) / (R(1.0) - uo);
+    R sW = F[0] + F[2] + F[4] + R(2.0) * (F[3] + F[6] + F[7]);
+    if (DEV) sW = rho0 + sW;
+    R rhoW = sW / (R(1.0) - uo);
     F[1] = F[3] + R(2) * rhoW * uo / R(3);
     F[5] = F[7] + rhoW * uo / R(6);
     F[8] = F[6] + rhoW * uo / R(6);
@@ -475,7 +643,9 @@ __device__ void boundary_F(const StepArgs &a, const ACC &acc, long long node, R 
   if (OUTLET && (fl & FL_EAST)) {
     if (a.outlet == 1) {
       // OutletBoundaries, serial/BoundaryConditions.c:70-81
-      R rhoE = (F[0] + F[2] + F[4] + R(2.0) * (F[1] + F[5] + F[8])) / (R(1) - uo);
+      R sE = F[0] + F[2] + F[4] + R(2.0) * (F[1] + F[5] + F[8]);
+      if (DEV) sE = rho0 + sE;
+      R rhoE = sE / (R(1) - uo);
       F[3] = F[1] - R(2) * rhoE * uo / R(3.0);
       F[7] = F[5] - rhoE * uo / R(6.0);
       F[6] = F[8] - rhoE * uo / R(6.0);
@@ -491,7 +661,9 @@ __device__ void boundary_F(const StepArgs &a, const ACC &acc, long long node, R 
     } else if (a.outlet == 4) {
       // constant-pressure east outlet (Zou-He density condition; not in the reference)
       const R ro = (R)a.rho_out;
-      R ux = R(-1.0) + (F[0] + F[2] + F[4] + R(2.0) * (F[1] + F[5] + F[8])) / ro;
+      R sP = F[0] + F[2] + F[4] + R(2.0) * (F[1] + F[5] + F[8]);
+      if (DEV) sP = rho0 + sP;
+      R ux = R(-1.0) + sP / ro;
       R ru = ro * ux;
       R d24 = R(0.5) * (F[2] - F[4]);
       F[3] = F[1] - (R(2.0) / R(3.0)) * ru;
@@ -502,18 +674,100 @@ __device__ void boundary_F(const StepArgs &a, const ACC &acc, long long node, R 
 }
 
 // Full treatment of a special node as one out-of-line call (keeps the bulk
-// path's register budget small).  Returns F and the macroscopic fields
-// (V = 0 on east-outlet cells, serial/CellFunctions.c:483-486).
+// path's register budget small).  Returns F (in the accessor's form) and the
+// macroscopic fields (V = 0 on east-outlet cells,
+// serial/CellFunctions.c:483-486).
 template <class R, class ACC>
 __device__ __noinline__ void special_node(const StepArgs &a, const ACC &acc, long long node,
                                           R F[9], R *mac) {
   boundary_F<true, R, ACC>(a, acc, node, F);
   R rho, u, v;
-  moments<R>(F, rho, u, v);
+  if constexpr (ACC::dev) {
+    R rt = ((F[0] + F[1]) + (F[2] + F[3])) + ((F[4] + F[5]) + (F[6] + F[7])) + F[8];
+    R jx = (F[1] - F[3]) + (F[5] - F[6]) + (F[8] - F[7]);
+    R jy = (F[2] - F[4]) + (F[5] - F[7]) + (F[6] - F[8]);
+    rho = (R)a.rho0 + rt;
+    R inv = R(1) / rho;
+    u = jx * inv;
+    v = jy * inv;
+  } else {
+    moments<R>(F, rho, u, v);
+  }
   if (a.rec[a.aux[node]].flags & FL_EAST) v = R(0.0);
   mac[0] = rho;
   mac[1] = u;
   mac[2] = v;
+}
+
+// Collision of deviations d = F - w rho0 with given rho, u, v (the special
+// nodes of the shifted storages, where v may be forced to 0).  Same operators
+// as collide<>, written for d: f_eq - w rho0 = w ((rho - rho0) + rho (3 c.u +
+// 4.5 (c.u)^2 - 1.5 u^2)); MRT rows 0..2 gain the rho0 M w terms.
+template <int MODEL>
+__device__ __forceinline__ void collide_dev(const float F[9], float rho, float u, float v,
+                                            const StepArgs &a, float M[9]) {
+  const float rho0 = (float)a.rho0, rt = rho - rho0;
+  if (MODEL == 3) {
+    const float om = (float)a.omega;
+    float a13 = F[1] + F[3], a24 = F[2] + F[4];
+    float a14 = a13 + a24;
+    float p57 = F[5] + F[7], p68 = F[6] + F[8];
+    float a58 = p57 + p68;
+    float m0 = (F[0] + a14) + a58;
+    float m1 = 2.f * a58 - a14 - 4.f * F[0];
+    float m2 = (4.f * F[0] + a58) - 2.f * a14;
+    float d13 = F[1] - F[3], d24 = F[2] - F[4];
+    float e57 = F[5] - F[7], e86 = F[8] - F[6];
+    float x58 = e57 + e86, y58 = e57 - e86;
+    float m3 = d13 + x58, m5 = d24 + y58;
+    float m4 = x58 - 2.f * d13, m6 = y58 - 2.f * d24;
+    float m7 = a13 - a24, m8 = p57 - p68;
+    const float ru = rho * u, rv = rho * v, rrq = rho * rho * (u * u + v * v);
+    // m(F) - meq with m(F) = m(d) + rho0 (1, -2, 1, 0, ...)
+    float d0 = m0 - rt;
+    float d1 = 1.4f * (m1 + 2.f * rt - 3.f * rrq);
+    float d2 = 1.4f * (m2 - rt + 3.f * rrq);
+    float d3 = m3 - ru;
+    float d4 = 1.2f * (m4 + ru);
+    float d5 = m5 - rv;
+    float d6 = 1.2f * (m6 + rv);
+    float d7 = om * (m7 - rho * (u * u - v * v));
+    float d8 = om * (m8 - ru * v);
+    const float c = 1.f / 36.f;
+    float ax = 4.f * d0 - d1 - 2.f * d2;
+    float dg = 4.f * d0 + 2.f * d1 + d2;
+    float X = 6.f * (d3 - d4), Y = 6.f * (d5 - d6), P = 9.f * d7;
+    float Xd = 6.f * d3 + 3.f * d4, Yd = 6.f * d5 + 3.f * d6, Q = 9.f * d8;
+    M[0] = F[0] - c * (4.f * ((d0 - d1) + d2));
+    M[1] = F[1] - c * (ax + X + P);
+    M[2] = F[2] - c * (ax + Y - P);
+    M[3] = F[3] - c * (ax - X + P);
+    M[4] = F[4] - c * (ax - Y - P);
+    M[5] = F[5] - c * (dg + Xd + Yd + Q);
+    M[6] = F[6] - c * (dg - Xd + Yd - Q);
+    M[7] = F[7] - c * (dg - Xd - Yd + Q);
+    M[8] = F[8] - c * (dg + Xd - Yd - Q);
+  } else {
+    const float T1 = u * u + v * v;
+    float feq[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      const float T2 = u * CX[k] + v * CY[k];
+      feq[k] = wgt<float>(k) * (rt + rho * (3.f * T2 + 4.5f * T2 * T2 - 1.5f * T1));
+    }
+    const float om = (float)a.omega, omA = (float)a.omegaA;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      if (MODEL == 1) {
+        M[k] = fmaf(om, feq[k] - F[k], F[k]);
+      } else {
+        const int o = OPP[k];
+        float sp = 0.5f * ((F[k] + F[o]) - (feq[k] + feq[o]));
+        float sm = 0.5f * ((F[k] - F[o]) - (feq[k] - feq[o]));
+        M[k] = F[k] - om * sp - omA * sm;
+      }
+    }
+  }
 }
 
 // ------------------------------------------------------------------- kernels
@@ -558,14 +812,39 @@ __device__ __forceinline__ void collide_store(const StepArgs &a, long long node,
   store_node<ST, PH>(a, node, c, M);
 }
 
-// Collision and store of a node without boundary work.
+// Store of a bulk node's post-collision populations given in the storage's
+// bulk form (deviations for shifted storage); the AA side buffer keeps
+// absolute values.
+template <class ST, int PH>
+__device__ __forceinline__ void store_node_dev(const StepArgs &a, long long node, uint8_t c,
+                                               const typename ST::R M[9]) {
+  using T = typename ST::T;
+  T *d = (T *)a.dst;
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    long long i;
+    if (PH == PH_AB) i = (long long)k * a.plane + node;
+    else if (PH == PH_AA_A) i = (long long)k * a.plane + node + nb(k, a.pitch);
+    else i = (long long)OPP[k] * a.plane + node;
+    st_dev<ST>(d + i, k, M[k], a);
+  }
+  if (PH != PH_AB && c != CLS_BULK) {
+    uint32_t sbi = a.aux[node];
+    if (c == CLS_SPECIAL) sbi = a.rec[sbi].sb;
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+      a.sb_dst[(size_t)sbi * 9 + k] = (double)M[k] + (ST::SHIFT ? wgt<double>(k) * a.rho0 : 0.0);
+  }
+}
+
+// Collision and store of a node without boundary work (F in bulk form).
 template <class ST, int MODEL, int PH>
 __device__ __forceinline__ void bulk_store(const StepArgs &a, long long node, uint8_t c,
                                            const typename ST::R F[9]) {
   using R = typename ST::R;
   R M[9];
-  collide_bulk<MODEL, R>(F, a, M);
-  store_node<ST, PH>(a, node, c, M);
+  collide_bulk_dev<MODEL, ST>(F, a, M);
+  store_node_dev<ST, PH>(a, node, c, M);
 }
 
 // Index of the pulled F[k](node) in the state of layout PH.
@@ -586,16 +865,23 @@ __device__ __forceinline__ void step_one(const StepArgs &a, long long node, uint
   R F[9], rho, u, v;
   if (c != CLS_SPECIAL) {
 #pragma unroll
-    for (int k = 0; k < 9; k++) F[k] = ST::ld(s + pull_index<PH>(k, node, a), k, a);
+    for (int k = 0; k < 9; k++) F[k] = ld_dev<ST>(s + pull_index<PH>(k, node, a), k, a);
     bulk_store<ST, MODEL, PH>(a, node, c, F);
     return;
   } else {
+    constexpr bool SH = ST::SHIFT;
     R mac[3];
-    if constexpr (PH == PH_AB) special_node<R>(a, AccMain<ST, PH_AB>(a, a.src), node, F, mac);
-    else special_node<R>(a, AccSide<ST>(a, nullptr), node, F, mac);
+    if constexpr (PH == PH_AB) special_node<R>(a, AccMain<ST, PH_AB, SH>(a, a.src), node, F, mac);
+    else special_node<R>(a, AccSide<ST, SH>(a, nullptr), node, F, mac);
     rho = mac[0];
     u = mac[1];
     v = mac[2];
+    if constexpr (SH) {
+      R M[9];
+      collide_dev<MODEL>(F, rho, u, v, a, M);
+      store_node_dev<ST, PH>(a, node, c, M);
+      return;
+    }
   }
   collide_store<ST, MODEL, PH>(a, node, c, F, rho, u, v);
 }
@@ -604,12 +890,10 @@ __device__ __forceinline__ void step_one(const StepArgs &a, long long node, uint
 // along x; each thread updates NPT consecutive rows of its column.  When all
 // NPT nodes are free of boundary work their 9*NPT loads are issued before any
 // arithmetic (more bytes in flight per thread).
-template <class ST, int MODEL, int PH, int BX, int NPT>
-__global__ void __launch_bounds__(BX) k_step(const __grid_constant__ StepArgs a) {
+template <class ST, int MODEL, int PH, int NPT>
+__device__ __forceinline__ void step_column(const StepArgs &a, int x, int y0) {
   using R = typename ST::R;
   using T = typename ST::T;
-  const int x = blockIdx.x * BX + threadIdx.x;
-  const int y0 = blockIdx.y * NPT;
   if (x >= a.n) return;
   uint8_t c[NPT];
   bool bulk = true;
@@ -632,13 +916,18 @@ __global__ void __launch_bounds__(BX) k_step(const __grid_constant__ StepArgs a)
     const long long node = (long long)(y0 + j) * a.pitch + x;
 #pragma unroll
     for (int k = 0; k < 9; k++)
-      F[j][k] = (c[j] != CLS_SOLID) ? ST::ld(s + pull_index<PH>(k, node, a), k, a) : R(0);
+      F[j][k] = (c[j] != CLS_SOLID) ? ld_dev<ST>(s + pull_index<PH>(k, node, a), k, a) : R(0);
   }
 #pragma unroll
   for (int j = 0; j < NPT; j++) {
     if (c[j] == CLS_SOLID) continue;
     bulk_store<ST, MODEL, PH>(a, (long long)(y0 + j) * a.pitch + x, c[j], F[j]);
   }
+}
+
+template <class ST, int MODEL, int PH, int BX, int NPT>
+__global__ void __launch_bounds__(BX) k_step(const __grid_constant__ StepArgs a) {
+  step_column<ST, MODEL, PH, NPT>(a, blockIdx.x * BX + threadIdx.x, blockIdx.y * NPT);
 }
 
 // Fused step over x-chunks: each thread owns V consecutive nodes of NPT rows
@@ -699,19 +988,19 @@ __global__ void __launch_bounds__(BX) k_step_vec(const __grid_constant__ StepArg
       VecIO<T, V>::load(s + base, raw);
       R val[V];
 #pragma unroll
-      for (int i = 0; i < V; i++) val[i] = ST::cvt(raw[i], k, a);
+      for (int i = 0; i < V; i++) val[i] = ST::cvt_dev(raw[i], k, a);
       if (sx == 0) {
 #pragma unroll
         for (int i = 0; i < V; i++) F[j][i][k] = val[i];
       } else if (sx == 1) {
         R edge = __shfl_up_sync(FULL, val[V - 1], 1);
-        if (lane == 0) edge = x0 > 0 ? ST::ld(s + base - 1, k, a) : R(0);
+        if (lane == 0) edge = x0 > 0 ? ld_dev<ST>(s + base - 1, k, a) : R(0);
         F[j][0][k] = edge;
 #pragma unroll
         for (int i = 1; i < V; i++) F[j][i][k] = val[i - 1];
       } else {
         R edge = __shfl_down_sync(FULL, val[0], 1);
-        if (lane == 31) edge = ST::ld(s + base + V, k, a);
+        if (lane == 31) edge = ld_dev<ST>(s + base + V, k, a);
         F[j][V - 1][k] = edge;
 #pragma unroll
         for (int i = 0; i < V - 1; i++) F[j][i][k] = val[i + 1];
@@ -728,7 +1017,7 @@ __global__ void __launch_bounds__(BX) k_step_vec(const __grid_constant__ StepArg
       rowfluid = rowfluid || cl[j][i] != CLS_SOLID;
       R M[9];
       if (cl[j][i] != CLS_SOLID) {
-        collide_bulk<MODEL, R>(F[j][i], a, M);
+        collide_bulk_dev<MODEL, ST>(F[j][i], a, M);
       } else {
 #pragma unroll
         for (int k = 0; k < 9; k++) M[k] = R(0);
@@ -738,7 +1027,8 @@ __global__ void __launch_bounds__(BX) k_step_vec(const __grid_constant__ StepArg
       if (PH != PH_AB && cl[j][i] == CLS_BULK_REC) {
         const uint32_t sbi = a.aux[(long long)y * a.pitch + x0 + i];
 #pragma unroll
-        for (int k = 0; k < 9; k++) a.sb_dst[(size_t)sbi * 9 + k] = (double)M[k];
+        for (int k = 0; k < 9; k++)
+          a.sb_dst[(size_t)sbi * 9 + k] = (double)M[k] + (ST::SHIFT ? wgt<double>(k) * a.rho0 : 0.0);
       }
     }
     if (!rowfluid) continue;
@@ -750,11 +1040,11 @@ __global__ void __launch_bounds__(BX) k_step_vec(const __grid_constant__ StepArg
 #pragma unroll
         for (int i = 0; i < V; i++)
           if (cl[j][i] != CLS_SOLID)
-            ST::st(d + (long long)k * a.plane + node0 + i + nb(k, a.pitch), k, F[j][i][k], a);
+            st_dev<ST>(d + (long long)k * a.plane + node0 + i + nb(k, a.pitch), k, F[j][i][k], a);
       } else {
         T raw[V];
 #pragma unroll
-        for (int i = 0; i < V; i++) raw[i] = ST::pack(F[j][i][k], k, a);
+        for (int i = 0; i < V; i++) raw[i] = ST::pack_dev(F[j][i][k], k, a);
         const int plane = (PH == PH_AB) ? k : OPP[k];
         VecIO<T, V>::store(d + (long long)plane * a.plane + node0, raw);
       }
@@ -776,13 +1066,13 @@ __device__ __forceinline__ void unpack2(uint32_t w, int k, const StepArgs &a, fl
   using T = typename ST::T;
   T t[2];
   memcpy(t, &w, 4);
-  lo = ST::cvt(t[0], k, a);
-  hi = ST::cvt(t[1], k, a);
+  lo = ST::cvt_dev(t[0], k, a);
+  hi = ST::cvt_dev(t[1], k, a);
 }
 template <class ST>
 __device__ __forceinline__ uint32_t pack2(float lo, float hi, int k, const StepArgs &a) {
   using T = typename ST::T;
-  T t[2] = {ST::pack(lo, k, a), ST::pack(hi, k, a)};
+  T t[2] = {ST::pack_dev(lo, k, a), ST::pack_dev(hi, k, a)};
   uint32_t w;
   memcpy(&w, t, 4);
   return w;
@@ -873,10 +1163,10 @@ __global__ void __launch_bounds__(128) k_step_h2(const __grid_constant__ StepArg
       unpack2<ST>(word, k, a, F0[k], F1[k]);
     }
     float M0[9], M1[9];
-    if (cl[j][0] != CLS_SOLID) collide_bulk<MODEL, float>(F0, a, M0);
+    if (cl[j][0] != CLS_SOLID) collide_bulk_dev<MODEL, ST>(F0, a, M0);
     else
       for (int k = 0; k < 9; k++) M0[k] = 0.f;
-    if (cl[j][1] != CLS_SOLID) collide_bulk<MODEL, float>(F1, a, M1);
+    if (cl[j][1] != CLS_SOLID) collide_bulk_dev<MODEL, ST>(F1, a, M1);
     else
       for (int k = 0; k < 9; k++) M1[k] = 0.f;
     const long long node0 = (long long)y * a.pitch + x0;
@@ -886,15 +1176,16 @@ __global__ void __launch_bounds__(128) k_step_h2(const __grid_constant__ StepArg
         const uint32_t sbi = a.aux[node0 + i];
         const float *M = i ? M1 : M0;
 #pragma unroll
-        for (int k = 0; k < 9; k++) a.sb_dst[(size_t)sbi * 9 + k] = (double)M[k];
+        for (int k = 0; k < 9; k++)
+          a.sb_dst[(size_t)sbi * 9 + k] = (double)M[k] + wgt<double>(k) * a.rho0;
       }
 #pragma unroll
     for (int k = 0; k < 9; k++) {
       if (PH == PH_AA_A) {
         // neighbour write x + e_k, element-wise for fluid nodes
-        if (cl[j][0] != CLS_SOLID) ST::st(d + (long long)k * a.plane + node0 + nb(k, a.pitch), k, M0[k], a);
+        if (cl[j][0] != CLS_SOLID) st_dev<ST>(d + (long long)k * a.plane + node0 + nb(k, a.pitch), k, M0[k], a);
         if (cl[j][1] != CLS_SOLID)
-          ST::st(d + (long long)k * a.plane + node0 + 1 + nb(k, a.pitch), k, M1[k], a);
+          st_dev<ST>(d + (long long)k * a.plane + node0 + 1 + nb(k, a.pitch), k, M1[k], a);
       } else {
         const int plane = (PH == PH_AB) ? k : OPP[k];
         __stcs((unsigned *)(d + (long long)plane * a.plane + node0), pack2<ST>(M0[k], M1[k], k, a));
@@ -1064,7 +1355,7 @@ __global__ void __launch_bounds__(TX * TY / RPT, 3) k_step_tma(const __grid_cons
 #pragma unroll
       for (int k = 0; k < 9; k++) {
         const int dx = (PH == PH_AA_B) ? 0 : -CX[k];
-        F[k] = ST::cvt(sb[(k * TY + j) * W + H + col + dx], k, a);
+        F[k] = ST::cvt_dev(sb[(k * TY + j) * W + H + col + dx], k, a);
       }
       bulk_store<ST, MODEL, PH>(a, node, c, F);
     }
@@ -1164,7 +1455,8 @@ __global__ void __launch_bounds__(128) k_finish(const __grid_constant__ StepArgs
 #pragma unroll
   for (int i = 0; i < NSUM; i++) acc[i] = 0.0, part[i] = R(0);
   const T *src = (const T *)a.src;
-  AccMain<ST, L> acc_m(a, a.src);
+  constexpr bool SH = ST::SHIFT;  // populations handled as deviations, see moments_form
+  AccMain<ST, L, SH> acc_m(a, a.src);
   int chunk = 0;
   for (int y = blockIdx.y; y < a.m && x < a.n; y += gridDim.y) {
     const long long node = (long long)y * a.pitch + x;
@@ -1185,10 +1477,10 @@ __global__ void __launch_bounds__(128) k_finish(const __grid_constant__ StepArgs
       // bulk: all neighbours fluid, plain loads in the state's layout
 #pragma unroll
       for (int k = 0; k < 9; k++) {
-        F[k] = ST::ld(src + slot_of<L>(k, node - nb(k, a.pitch), a), k, a);
-        M[k] = ST::ld(src + slot_of<L>(k, node, a), k, a);
+        F[k] = ST::cvt_dev(__ldg(src + slot_of<L>(k, node - nb(k, a.pitch), a)), k, a);
+        M[k] = ST::cvt_dev(__ldg(src + slot_of<L>(k, node, a)), k, a);
       }
-      moments<R>(F, rho, u, v);
+      moments_form<ST>(F, a, rho, u, v);
     } else {
       R mac[3];
       special_node<R>(a, acc_m, node, F, mac);
@@ -1205,9 +1497,9 @@ __global__ void __launch_bounds__(128) k_finish(const __grid_constant__ StepArgs
       l2 += dk * dk;
     }
     if (o.f)
-      for (int k = 0; k < 9; k++) o.f[cell * 9 + k] = (double)F[k];
+      for (int k = 0; k < 9; k++) o.f[cell * 9 + k] = (double)F[k] + (SH ? wgt<double>(k) * a.rho0 : 0.0);
     if (o.metaf)
-      for (int k = 0; k < 9; k++) o.metaf[cell * 9 + k] = (double)M[k];
+      for (int k = 0; k < 9; k++) o.metaf[cell * 9 + k] = (double)M[k] + (SH ? wgt<double>(k) * a.rho0 : 0.0);
     if (o.rho) o.rho[cell] = (double)rho;
     if (o.u) o.u[cell] = (double)u;
     if (o.v) o.v[cell] = (double)v;
@@ -1232,7 +1524,7 @@ __global__ void __launch_bounds__(128) k_finish(const __grid_constant__ StepArgs
         const uint32_t wall = (r.flags >> FL_WALL_SHIFT) & 0x1FFu;
         for (int k = 1; k < 9; k++)
           if ((wall >> k) & 1u) {
-            double g = (double)M[k] + (double)F[OPP[k]];
+            double g = (double)M[k] + (double)F[OPP[k]] + (SH ? 2.0 * wgt<double>(k) * a.rho0 : 0.0);
             acc[S_FX] += g * CX[k];
             acc[S_FY] += g * CY[k];
           }

@@ -1,0 +1,85 @@
+"""GPU: batched stepping (lbm_batch_*) against single-domain contexts."""
+import numpy as np
+import pytest
+
+import cases
+import parallellbmcranfield_gb300 as G
+
+pytestmark = pytest.mark.gpu
+
+BASE = dict(uavg=0.05, vavg=0.0, rho_ini=1.0, inlet_profile=2, curved_boundaries=1,
+            outlet_profile=2)
+
+
+def batch_cases(model):
+    return [
+        (G.Mesh.cavity(30), dict(BASE, viscosity=0.03, collision_model=model)),
+        (G.Mesh.cavity(57), dict(BASE, viscosity=0.05, collision_model=model)),
+        (G.Mesh.channel(60, 20, [(15.0, 10.4, 4.0)]),
+         dict(BASE, uavg=0.04, viscosity=0.04, inlet_profile=1, outlet_profile=1,
+              collision_model=model)),
+        (G.Mesh.cavity(131), dict(BASE, viscosity=0.02, collision_model=model)),
+    ]
+
+
+def single(mesh, params, precision, iterations):
+    s = G.Solver(mesh, precision=precision, **params)
+    n, m = mesh.shape
+    N = n * m
+    s.set_state(None, np.full(N, float(np.float32(params["rho_ini"]))), np.zeros(N), np.zeros(N))
+    s.step(iterations)
+    out = s.fields()
+    s.close()
+    return out
+
+
+@pytest.mark.parametrize("model", [1, 2, 3])
+def test_batch_equals_single_contexts_fp64(model):
+    """FP64: each case of a batch is bitwise the single-domain result."""
+    cs = batch_cases(model)
+    b = G.Batch(cs, precision="fp64")
+    b.set_rest()
+    r = b.run(60, check_every=20, tol=-1.0)  # tol < 0: nobody converges
+    assert (r["steps"] == 60).all()
+    for c, (mesh, params) in enumerate(cs):
+        got = b.fields(c)
+        want = single(mesh, params, G.FP64, 61)  # set_rest + 60 fused steps = 61 iterations
+        for k in got:
+            assert np.array_equal(got[k], want[k]), (c, k)
+    b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16dev"])
+def test_batch_tiles_and_autotune(precision):
+    cs = batch_cases(2)
+    ref = None
+    rep = G.Batch(cs, precision=precision).autotune(2)
+    assert 0 <= rep["variant"] < 4 and len(rep["ms"]) == 4
+    for tile in range(4):
+        b = G.Batch(cs, precision=precision)
+        b.set_tile(tile)
+        b.set_rest()
+        r = b.run(40, check_every=40, tol=-1.0)
+        assert (r["steps"] == 40).all()
+        f = b.fields(3)
+        if ref is None:
+            ref = f
+        else:
+            assert np.abs(f["u"] - ref["u"]).max() < 1e-3 * np.abs(ref["u"]).max()
+        b.close()
+
+
+def test_batch_convergence_freezes_cases():
+    """Low-Re cavities converge at different times; a converged case stops."""
+    cs = [(G.Mesh.cavity(side), dict(BASE, viscosity=nu, collision_model=2))
+          for side, nu in ((16, 0.2), (24, 0.2), (40, 0.3))]
+    b = G.Batch(cs, precision="fp32")
+    r = b.run(200000, check_every=100, tol=1e-6)
+    assert (r["converged"] == 1).all(), r
+    assert (r["du_rel"] <= 1e-6).all()
+    # a smaller cavity converges in fewer steps than a larger one at similar Re
+    assert r["steps"][0] < r["steps"][2]
+    # frozen cases keep their converged state
+    f1 = b.fields(0)
+    b.close()
+    assert np.isfinite(f1["u"]).all()

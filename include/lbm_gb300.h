@@ -187,6 +187,10 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
 void lbm_batch_destroy(lbm_batch *b);
 /* Every case at rest: f = f_eq(rho_ini, 0, 0), then its first collision. */
 lbm_status lbm_batch_set_rest(lbm_batch *b);
+/* Case c restarts from f = f_eq(rho, u, v) (arrays of that case's n*m
+ * cells); its counters and convergence state are reset. */
+lbm_status lbm_batch_set_state(lbm_batch *b, int32_t case_index, const double *rho,
+                               const double *u, const double *v);
 /* Fixes the batched step's tile shape (0..3: 128x1, 64x4, 128x2, 128x4 threads x rows). */
 lbm_status lbm_batch_set_tile(lbm_batch *b, int32_t tile_variant);
 /* Times the batched step's tile shapes and keeps the fastest (before stepping). */
@@ -205,6 +209,50 @@ lbm_status lbm_batch_get_fields(lbm_batch *b, int32_t case_index, double *rho, d
 lbm_status lbm_batch_dims(const lbm_batch *b, int32_t case_index, int32_t *n, int32_t *m);
 lbm_status lbm_batch_info(const lbm_batch *b, int64_t *nodes, int64_t *fluid_nodes,
                           int32_t *tile_variant, int64_t *device_bytes);
+
+/* ---------------------------------------------------------------------------
+ * Surrogate network for warm starts (no counterpart in the reference): a
+ * 4-level convolutional encoder-decoder with skip connections (channels base,
+ * 2 base, 4 base, 4 base; 3x3 convolutions, ReLU, 2x2 average pooling,
+ * nearest upsampling, a 1x1 output layer) from in_channels input maps to
+ * out_channels output maps on a height x width grid.  BF16 weights and
+ * activations, FP32 accumulation on the tensor cores, FP32 master weights
+ * trained with Adam; all kernels are this library's own.  Tensors are NHWC
+ * FP32 on the host: x[b][y][x][c].  Parameters: for each of the 15 layers in
+ * forward order W[cout][Kp] (Kp = taps*cin rounded up to 32, k = tap*cin + ci,
+ * zero padding) followed by b[cout].
+ * ------------------------------------------------------------------------ */
+typedef struct lbm_sg lbm_sg;
+typedef struct lbm_sg_config {
+  int32_t height, width;   /* multiples of 8, >= 16 */
+  int32_t in_channels, out_channels;
+  int32_t base;            /* channels of the first level (multiple of 8) */
+  int32_t max_batch;
+  float lr, beta1, beta2, eps;  /* Adam */
+  uint64_t seed;           /* weight initialisation */
+  int32_t device;
+} lbm_sg_config;
+lbm_status lbm_sg_create(const lbm_sg_config *cfg, lbm_sg **out);
+void lbm_sg_destroy(lbm_sg *s);
+lbm_status lbm_sg_num_params(const lbm_sg *s, int64_t *n);
+lbm_status lbm_sg_get_params(lbm_sg *s, float *out);
+lbm_status lbm_sg_set_params(lbm_sg *s, const float *in);
+/* y[batch][H][W][out] = net(x[batch][H][W][in]) */
+lbm_status lbm_sg_forward(lbm_sg *s, int32_t batch, const float *x, float *y);
+/* Masked mean-squared-error loss and its gradient (no update): loss = sum over
+ * cells and outputs of mask * (y - target)^2 / (sum mask * out_channels);
+ * mask NULL = all ones; grads (NULL = not copied) receives num_params floats. */
+lbm_status lbm_sg_loss_grads(lbm_sg *s, int32_t batch, const float *x, const float *target,
+                             const float *mask, double *loss, float *grads);
+/* One Adam update from the gradients of the last lbm_sg_loss_grads. */
+lbm_status lbm_sg_adam_step(lbm_sg *s);
+/* Keeps count samples (x, target, mask) on the device for lbm_sg_train. */
+lbm_status lbm_sg_set_dataset(lbm_sg *s, int32_t count, const float *x, const float *y,
+                              const float *mask);
+/* Adam steps over order[0..n) in batches (a trailing partial batch is
+ * dropped); mean_loss = mean batch loss. */
+lbm_status lbm_sg_train(lbm_sg *s, int32_t batch, const int32_t *order, int32_t n,
+                        double *mean_loss);
 
 /* ---------------------------------------------------------------------------
  * Mesh helpers (the reference's readers, serial/FileIO.c:14-289, and a

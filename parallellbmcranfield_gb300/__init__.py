@@ -59,9 +59,12 @@ EXPORTS = ["lbm_status_string", "lbm_last_error", "lbm_create", "lbm_destroy", "
            "lbm_set_state", "lbm_step", "lbm_get_fields", "lbm_check", "lbm_check_noalloc",
            "lbm_get_info", "lbm_autotune",
            "lbm_inspect_mesh", "lbm_batch_create", "lbm_batch_destroy", "lbm_batch_set_rest", "lbm_batch_set_tile",
+           "lbm_batch_set_state",
            "lbm_batch_autotune", "lbm_batch_run", "lbm_batch_get_fields", "lbm_batch_dims",
            "lbm_batch_info", "lbm_mesh_read", "lbm_mesh_cavity", "lbm_mesh_channel", "lbm_mesh_write",
-           "lbm_mesh_free"]
+           "lbm_mesh_free", "lbm_sg_create", "lbm_sg_destroy", "lbm_sg_num_params",
+           "lbm_sg_get_params", "lbm_sg_set_params", "lbm_sg_forward", "lbm_sg_loss_grads",
+           "lbm_sg_adam_step", "lbm_sg_set_dataset", "lbm_sg_train"]
 
 _lib = None
 
@@ -97,6 +100,7 @@ def load():
     L.lbm_batch_destroy.restype = None
     L.lbm_batch_set_rest.argtypes = [vp]
     L.lbm_batch_set_tile.argtypes = [vp, i32]
+    L.lbm_batch_set_state.argtypes = [vp, i32, dp, dp, dp]
     L.lbm_batch_autotune.argtypes = [vp, i32, C.c_char_p, C.c_size_t]
     L.lbm_batch_run.argtypes = [vp, C.c_int64, i32, C.c_double, dp, dp, dp, C.POINTER(C.c_double)]
     L.lbm_batch_get_fields.argtypes = [vp, i32, dp, dp, dp]
@@ -322,6 +326,11 @@ class Batch:
     def set_rest(self):
         _check(self.L.lbm_batch_set_rest(self.h), "lbm_batch_set_rest")
 
+    def set_state(self, case, rho, u, v):
+        arrs = [np.ascontiguousarray(a, np.float64) for a in (rho, u, v)]
+        _check(self.L.lbm_batch_set_state(self.h, int(case), *[_ptr(a) for a in arrs]),
+               "lbm_batch_set_state")
+
     def set_tile(self, variant):
         _check(self.L.lbm_batch_set_tile(self.h, int(variant)), "lbm_batch_set_tile")
 
@@ -357,6 +366,105 @@ class Batch:
     def close(self):
         if getattr(self, "h", None):
             self.L.lbm_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+
+class lbm_sg_config(C.Structure):
+    _fields_ = [("height", C.c_int32), ("width", C.c_int32), ("in_channels", C.c_int32),
+                ("out_channels", C.c_int32), ("base", C.c_int32), ("max_batch", C.c_int32),
+                ("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
+                ("seed", C.c_uint64), ("device", C.c_int32)]
+
+
+def _load_sg(L):
+    vp, i32, dp = C.c_void_p, C.c_int32, C.c_void_p
+    if getattr(L, "_sg_ready", False):
+        return L
+    L.lbm_sg_create.argtypes = [C.POINTER(lbm_sg_config), C.POINTER(vp)]
+    L.lbm_sg_destroy.argtypes = [vp]
+    L.lbm_sg_destroy.restype = None
+    L.lbm_sg_num_params.argtypes = [vp, C.POINTER(C.c_int64)]
+    L.lbm_sg_get_params.argtypes = [vp, dp]
+    L.lbm_sg_set_params.argtypes = [vp, dp]
+    L.lbm_sg_forward.argtypes = [vp, i32, dp, dp]
+    L.lbm_sg_loss_grads.argtypes = [vp, i32, dp, dp, dp, C.POINTER(C.c_double), dp]
+    L.lbm_sg_adam_step.argtypes = [vp]
+    L.lbm_sg_set_dataset.argtypes = [vp, i32, dp, dp, dp]
+    L.lbm_sg_train.argtypes = [vp, i32, dp, i32, C.POINTER(C.c_double)]
+    for n in ("lbm_sg_create", "lbm_sg_num_params", "lbm_sg_get_params", "lbm_sg_set_params",
+              "lbm_sg_forward", "lbm_sg_loss_grads", "lbm_sg_adam_step", "lbm_sg_set_dataset",
+              "lbm_sg_train"):
+        getattr(L, n).restype = C.c_int
+    L._sg_ready = True
+    return L
+
+
+class Surrogate:
+    """The warm-start network (wraps lbm_sg): NHWC float32 arrays on the host."""
+
+    def __init__(self, height=256, width=256, in_channels=4, out_channels=3, base=32,
+                 max_batch=8, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8, seed=0, device=0):
+        L = self.L = _load_sg(load())
+        self.cfg = lbm_sg_config(height, width, in_channels, out_channels, base, max_batch, lr,
+                                 beta1, beta2, eps, seed, device)
+        self.h = C.c_void_p()
+        _check(L.lbm_sg_create(C.byref(self.cfg), C.byref(self.h)), "lbm_sg_create")
+        n = C.c_int64()
+        _check(L.lbm_sg_num_params(self.h, C.byref(n)), "lbm_sg_num_params")
+        self.num_params = n.value
+
+    def params(self):
+        out = np.zeros(self.num_params, np.float32)
+        _check(self.L.lbm_sg_get_params(self.h, _ptr(out)), "lbm_sg_get_params")
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.num_params
+        _check(self.L.lbm_sg_set_params(self.h, _ptr(p)), "lbm_sg_set_params")
+
+    def forward(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        B = x.shape[0]
+        c = self.cfg
+        y = np.zeros((B, c.height, c.width, c.out_channels), np.float32)
+        for i in range(0, B, c.max_batch):
+            xb = np.ascontiguousarray(x[i:i + c.max_batch])
+            yb = np.zeros((len(xb), c.height, c.width, c.out_channels), np.float32)
+            _check(self.L.lbm_sg_forward(self.h, len(xb), _ptr(xb), _ptr(yb)), "lbm_sg_forward")
+            y[i:i + len(xb)] = yb
+        return y
+
+    def loss_grads(self, x, t, m=None):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        m = None if m is None else np.ascontiguousarray(m, np.float32)
+        loss = C.c_double()
+        g = np.zeros(self.num_params, np.float32)
+        _check(self.L.lbm_sg_loss_grads(self.h, x.shape[0], _ptr(x), _ptr(t), _ptr(m),
+                                        C.byref(loss), _ptr(g)), "lbm_sg_loss_grads")
+        return loss.value, g
+
+    def adam_step(self):
+        _check(self.L.lbm_sg_adam_step(self.h), "lbm_sg_adam_step")
+
+    def set_dataset(self, x, y, m):
+        self._ds = [np.ascontiguousarray(a, np.float32) for a in (x, y, m)]
+        _check(self.L.lbm_sg_set_dataset(self.h, len(x), *[_ptr(a) for a in self._ds]),
+               "lbm_sg_set_dataset")
+
+    def train(self, order, batch):
+        order = np.ascontiguousarray(order, np.int32)
+        loss = C.c_double()
+        _check(self.L.lbm_sg_train(self.h, int(batch), _ptr(order), len(order), C.byref(loss)),
+               "lbm_sg_train")
+        return loss.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.lbm_sg_destroy(self.h)
             self.h = None
 
     __del__ = close

@@ -38,7 +38,21 @@ __global__ void __launch_bounds__(BX) k_batch_step(const BatchCase *cases, const
     const int4 tl = tiles[t];
     if (!active[tl.x]) continue;
     const StepArgs &a = cases[tl.x].args[gpar[tl.x] & 1];
-    step_column<ST, MODEL, PH_AB, NPT>(a, tl.y * BX + threadIdx.x, tl.z * NPT);
+    step_column<ST, MODEL, PH_AB, NPT, true>(a, tl.y * BX + threadIdx.x, tl.z * NPT);
+  }
+}
+
+// The nodes with boundary work of every case, one thread each (x: case,
+// y: linear node index), after or alongside k_batch_step in the same step.
+template <class ST, int MODEL>
+__global__ void __launch_bounds__(128) k_batch_special(const BatchCase *cases, const int2 *list,
+                                                       int nlist, const int *active,
+                                                       const int *gpar) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nlist; i += gridDim.x * blockDim.x) {
+    const int2 e = list[i];
+    if (!active[e.x]) continue;
+    const StepArgs &a = cases[e.x].args[gpar[e.x] & 1];
+    step_one<ST, MODEL, PH_AB>(a, (long long)e.y, (uint8_t)CLS_SPECIAL);
   }
 }
 
@@ -128,6 +142,7 @@ static __global__ void k_batch_converge(int ncases, BatchState s, double tol) {
 
 struct BatchKernels {
   const void *step[4][BVAR];  // [model 1..3][tile shape]
+  const void *special[4];     // [model 1..3]
   const void *du;
   const void *advance;
   const void *converge;

@@ -58,6 +58,8 @@ struct lbm_batch {
   int ntiles[lbm::BVAR] = {};
   int4 *d_rows = nullptr;
   int nrows = 0;
+  int2 *d_special = nullptr;  // (case, node) of every node with boundary work
+  int nspecial = 0;
   int variant = 1;
   cudaStream_t stream = nullptr;
   const lbm::KernelSet *ks = nullptr;
@@ -152,6 +154,12 @@ lbm_status launch_steps(lbm_batch *b, int k) {
                     &b->s.gpar};
     cudaError_t e = cudaLaunchKernel(fn, dim3(grid), dim3(bx), args, 0, b->stream);
     if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
+    if (b->nspecial > 0) {
+      void *sargs[] = {&b->d_cases, &b->d_special, &b->nspecial, &b->s.active, &b->s.gpar};
+      const int sg = std::min((b->nspecial + 127) / 128, 152 * 16);
+      e = cudaLaunchKernel(b->bk->special[b->model], dim3(sg), dim3(128), sargs, 0, b->stream);
+      if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch special: ") + cudaGetErrorString(e));
+    }
     void *aargs[] = {&b->nc, &b->s};
     e = cudaLaunchKernel(b->bk->advance, dim3((b->nc + 255) / 256), dim3(256), aargs, 0, b->stream);
     if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch advance: ") + cudaGetErrorString(e));
@@ -237,6 +245,7 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
   b->hcases.resize(ncases);
   std::vector<std::vector<int4>> tiles(lbm::BVAR);
   std::vector<int4> rows;
+  std::vector<int2> specials;
   const size_t es = (size_t)b->ks->elem_size;
   const double w[9] = {4. / 9., 1. / 9., 1. / 9., 1. / 9., 1. / 9., 1. / 36., 1. / 36., 1. / 36., 1. / 36.};
   for (int c = 0; c < ncases; c++) {
@@ -303,6 +312,7 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
     }
     for (int y = 0; y < P.m; y++)
       for (int tx = 0; tx < (P.n + 127) / 128; tx++) rows.push_back(make_int4(c, tx, y, 0));
+    for (const lbm::BRec &r : P.rec) specials.push_back(make_int2(c, (int)r.node));
   }
   if ((st = balloc(b, &b->d_cases, (size_t)ncases)) != LBM_OK) return bail(st);
   cudaMemcpy(b->d_cases, b->hcases.data(), ncases * sizeof(lbm::BatchCase), cudaMemcpyHostToDevice);
@@ -311,6 +321,10 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
     if ((st = balloc(b, &b->d_tiles[v], tiles[v].size())) != LBM_OK) return bail(st);
     cudaMemcpy(b->d_tiles[v], tiles[v].data(), tiles[v].size() * sizeof(int4), cudaMemcpyHostToDevice);
   }
+  b->nspecial = (int)specials.size();
+  if ((st = balloc(b, &b->d_special, specials.size())) != LBM_OK) return bail(st);
+  if (!specials.empty())
+    cudaMemcpy(b->d_special, specials.data(), specials.size() * sizeof(int2), cudaMemcpyHostToDevice);
   b->nrows = (int)rows.size();
   if ((st = balloc(b, &b->d_rows, rows.size())) != LBM_OK) return bail(st);
   cudaMemcpy(b->d_rows, rows.data(), rows.size() * sizeof(int4), cudaMemcpyHostToDevice);
@@ -355,6 +369,40 @@ lbm_status lbm_batch_set_rest(lbm_batch *b) {
   if (!b) return fail(LBM_INVALID, "null argument");
   LBM_BCK(cudaSetDevice(b->device));
   return set_rest(b);
+}
+
+lbm_status lbm_batch_set_state(lbm_batch *b, int32_t c, const double *rho, const double *u,
+                               const double *v) {
+  if (!b || c < 0 || c >= b->nc || !rho || !u || !v) return fail(LBM_INVALID, "bad argument");
+  LBM_BCK(cudaSetDevice(b->device));
+  lbm_status st;
+  if (!b->have_state && (st = set_rest(b)) != LBM_OK) return st;
+  const CaseDev &d = b->cases[c];
+  const size_t N = (size_t)d.n * d.m;
+  double *dm = nullptr;
+  LBM_BCK(cudaMallocAsync((void **)&dm, 3 * N * 8, b->stream));
+  LBM_BCK(cudaMemcpyAsync(dm, rho, N * 8, cudaMemcpyHostToDevice, b->stream));
+  LBM_BCK(cudaMemcpyAsync(dm + N, u, N * 8, cudaMemcpyHostToDevice, b->stream));
+  LBM_BCK(cudaMemcpyAsync(dm + 2 * N, v, N * 8, cudaMemcpyHostToDevice, b->stream));
+  // f = f_eq(rho, u, v), first collision into buffer 0; the case restarts
+  lbm::StepArgs a = b->hcases[c].args[1];
+  a.dst = d.pop[0];
+  const double *f0 = nullptr, *pr = dm, *pu = dm + N, *pv = dm + 2 * N;
+  void *args[] = {&a, (void *)&f0, (void *)&pr, (void *)&pu, (void *)&pv};
+  dim3 grid((unsigned)((d.n + 127) / 128), (unsigned)d.m);
+  cudaError_t e = cudaLaunchKernel(b->ks->init[b->model][0], grid, dim3(128), args, 0, b->stream);
+  cudaFreeAsync(dm, b->stream);
+  if (e != cudaSuccess) return fail(LBM_CUDA, std::string("init launch: ") + cudaGetErrorString(e));
+  const int one = 1, zero = 0;
+  const long long zl = 0, neg = -1;
+  LBM_BCK(cudaMemcpyAsync(b->s.active + c, &one, sizeof one, cudaMemcpyHostToDevice, b->stream));
+  LBM_BCK(cudaMemcpyAsync(b->s.gpar + c, &zero, sizeof zero, cudaMemcpyHostToDevice, b->stream));
+  LBM_BCK(cudaMemcpyAsync(b->s.steps + c, &zl, sizeof zl, cudaMemcpyHostToDevice, b->stream));
+  LBM_BCK(cudaMemcpyAsync(b->s.have_prev + c, &zero, sizeof zero, cudaMemcpyHostToDevice, b->stream));
+  LBM_BCK(cudaMemcpyAsync(b->s.bad + c, &zero, sizeof zero, cudaMemcpyHostToDevice, b->stream));
+  LBM_BCK(cudaMemcpyAsync(b->s.conv_at + c, &neg, sizeof neg, cudaMemcpyHostToDevice, b->stream));
+  LBM_BCK(cudaStreamSynchronize(b->stream));
+  return LBM_OK;
 }
 
 lbm_status lbm_batch_autotune(lbm_batch *b, int32_t steps_per_trial, char *report,

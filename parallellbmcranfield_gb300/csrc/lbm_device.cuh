@@ -890,7 +890,10 @@ __device__ __forceinline__ void step_one(const StepArgs &a, long long node, uint
 // along x; each thread updates NPT consecutive rows of its column.  When all
 // NPT nodes are free of boundary work their 9*NPT loads are issued before any
 // arithmetic (more bytes in flight per thread).
-template <class ST, int MODEL, int PH, int NPT>
+// One column of NPT nodes.  With SKIP_SPECIAL the nodes with boundary work
+// are left out (another pass updates them from a compact list), so that a
+// warp never waits on one lane's boundary treatment.
+template <class ST, int MODEL, int PH, int NPT, bool SKIP_SPECIAL = false>
 __device__ __forceinline__ void step_column(const StepArgs &a, int x, int y0) {
   using R = typename ST::R;
   using T = typename ST::T;
@@ -901,6 +904,7 @@ __device__ __forceinline__ void step_column(const StepArgs &a, int x, int y0) {
   for (int j = 0; j < NPT; j++) {
     const int y = y0 + j;
     c[j] = (y < a.m) ? a.cls[(long long)y * a.pitch + x] : (uint8_t)CLS_SOLID;
+    if (SKIP_SPECIAL && c[j] == CLS_SPECIAL) c[j] = CLS_SOLID;
     bulk = bulk && c[j] != CLS_SPECIAL;
   }
   if (NPT == 1 || !bulk) {

@@ -1,0 +1,770 @@
+// Surrogate network for warm starts: a 4-level convolutional encoder-decoder
+// (U-Net with skip connections) mapping (geometry mask, boundary-velocity
+// map, Re, velocity scale) on an H x W grid to the steady (rho, u, v).
+//
+// Everything runs in this file's kernels: activations and weights in BF16
+// (NHWC), every product on the tensor cores (mma.sync m16n8k16 BF16 with FP32
+// accumulation) through an explicit im2col + GEMM formulation, FP32 master
+// weights, bias/ReLU/pool/upsample/concat/loss kernels and Adam.
+//
+// Convolution as GEMM (pixels p = B*H*W rows, K = 9*Cin padded to 32):
+//   forward       Y[p][co]   = relu(sum_k A[p][k] Wt[co][k] + b[co]),  A = im2col(X)
+//   input grad    dX[p][ci]  = sum_k A'[p][k] Wd[ci][k],  A' = im2col(dZ), Wd = flipped W
+//   weight grad   dW[co][k]  = sum_p dZ[p][co] A[p][k]   (split-K over p, FP32 atomics)
+// The GEMM kernel takes both operands K-contiguous (A[M][K], Bt[N][K]).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "lbm_internal.h"
+
+using lbm::fail;
+typedef __nv_bfloat16 bf16;
+
+namespace {
+
+// ------------------------------------------------------------------ kernels
+
+constexpr int GBM = 128, GBN = 64, GBK = 32, GPAD = 8;
+
+enum Epi : int {
+  EPI_BIAS_RELU_BF16 = 0,  // forward conv with ReLU
+  EPI_BIAS_BF16 = 1,       // forward conv without activation (output layer)
+  EPI_BF16 = 2,            // plain product to BF16 (input gradients)
+  EPI_ATOMIC_F32 = 3       // split-K accumulation into FP32 (weight gradients)
+};
+
+struct GemmArgs {
+  const bf16 *A;   // [M][K]
+  const bf16 *Bt;  // [N][K]
+  int M, N, K;     // K multiple of GBK
+  int kchunk;      // K range per blockIdx.z (multiple of GBK)
+  const float *bias;
+  bf16 *out_bf16;  // [M][N]
+  float *out_f32;  // [M][N]
+};
+
+__device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], const uint32_t b[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// C[M][N] = A[M][K] x Bt[N][K]^T.  256 threads: 8 warps as 4 (M) x 2 (N), each
+// warp 32 x 32 = 2 m16 x 4 n8 tiles; K in steps of 32 staged in shared memory.
+template <int EPI>
+__global__ void __launch_bounds__(256) k_gemm(const GemmArgs g) {
+  __shared__ __align__(16) bf16 As[GBM][GBK + GPAD];
+  __shared__ __align__(16) bf16 Bs[GBN][GBK + GPAD];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = warp & 3, wn = warp >> 2;
+  const int m0 = blockIdx.x * GBM, n0 = blockIdx.y * GBN;
+  const int kbeg = blockIdx.z * g.kchunk;
+  const int kend = min(g.K, kbeg + g.kchunk);
+  float acc[2][4][4];
+#pragma unroll
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+      for (int r = 0; r < 4; r++) acc[i][j][r] = 0.f;
+  const int gq = lane >> 2, tq = lane & 3;
+  for (int k0 = kbeg; k0 < kend; k0 += GBK) {
+    // A tile: 128 rows x 32 k = 512 chunks of 8 bf16
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+      const int ch = tid + it * 256, r = ch >> 2, c8 = (ch & 3) * 8;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (m0 + r < g.M) v = *(const uint4 *)(g.A + (size_t)(m0 + r) * g.K + k0 + c8);
+      *(uint4 *)&As[r][c8] = v;
+    }
+    {
+      const int r = tid >> 2, c8 = (tid & 3) * 8;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (n0 + r < g.N) v = *(const uint4 *)(g.Bt + (size_t)(n0 + r) * g.K + k0 + c8);
+      *(uint4 *)&Bs[r][c8] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < GBK; kk += 16) {
+      uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+      for (int i = 0; i < 2; i++) {
+        const int r = wm * 32 + i * 16 + gq;
+        af[i][0] = *(const uint32_t *)&As[r][kk + 2 * tq];
+        af[i][1] = *(const uint32_t *)&As[r + 8][kk + 2 * tq];
+        af[i][2] = *(const uint32_t *)&As[r][kk + 2 * tq + 8];
+        af[i][3] = *(const uint32_t *)&As[r + 8][kk + 2 * tq + 8];
+      }
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int c = wn * 32 + j * 8 + gq;
+        bfr[j][0] = *(const uint32_t *)&Bs[c][kk + 2 * tq];
+        bfr[j][1] = *(const uint32_t *)&Bs[c][kk + 2 * tq + 8];
+      }
+#pragma unroll
+      for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) mma_bf16(acc[i][j], af[i], bfr[j]);
+    }
+    __syncthreads();
+  }
+  // epilogue: c0,c1 at (row gq, cols 2tq, 2tq+1), c2,c3 at row gq+8
+#pragma unroll
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int row = m0 + wm * 32 + i * 16 + gq + h * 8;
+        if (row >= g.M) continue;
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+          const int col = n0 + wn * 32 + j * 8 + 2 * tq + e;
+          if (col >= g.N) continue;
+          float v = acc[i][j][h * 2 + e];
+          const size_t o = (size_t)row * g.N + col;
+          if (EPI == EPI_BIAS_RELU_BF16) g.out_bf16[o] = __float2bfloat16_rn(fmaxf(v + g.bias[col], 0.f));
+          else if (EPI == EPI_BIAS_BF16) g.out_bf16[o] = __float2bfloat16_rn(v + g.bias[col]);
+          else if (EPI == EPI_BF16) g.out_bf16[o] = __float2bfloat16_rn(v);
+          else atomicAdd(g.out_f32 + o, v);
+        }
+      }
+}
+
+// im2col of a taps = 9 (3x3, pad 1) or taps = 1 convolution:
+// A[p][r*C + c] = X[p + offset r][c], zero outside the image and in the K
+// padding (k >= taps*C).  X is [B][H][W][C], A is [B*H*W][Kp].
+__global__ void k_im2col(const bf16 *X, bf16 *A, int B, int H, int W, int C, int taps, int Kp) {
+  const size_t total = (size_t)B * H * W * Kp;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(i % Kp);
+    const size_t p = i / Kp;
+    bf16 v = __float2bfloat16_rn(0.f);
+    if (k < taps * C) {
+      const int r = k / C, c = k - r * C;
+      if (taps == 1) {
+        v = X[p * C + c];
+      } else {
+        const int x = (int)(p % W), y = (int)((p / W) % H), b = (int)(p / ((size_t)W * H));
+        const int xx = x + r % 3 - 1, yy = y + r / 3 - 1;
+        if (xx >= 0 && xx < W && yy >= 0 && yy < H) v = X[(((size_t)b * H + yy) * W + xx) * C + c];
+      }
+    }
+    A[i] = v;
+  }
+}
+
+// Transpose of a [R][Cc] BF16 matrix into [Cc][ldo] (ldo >= R; columns R..ldo-1 zero).
+__global__ void k_transpose(const bf16 *in, bf16 *out, int R, int Cc, int ldo) {
+  __shared__ bf16 t[32][33];
+  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+  for (int i = threadIdx.y; i < 32; i += 8) {
+    const int r = r0 + i, c = c0 + threadIdx.x;
+    t[i][threadIdx.x] = (r < R && c < Cc) ? in[(size_t)r * Cc + c] : __float2bfloat16_rn(0.f);
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += 8) {
+    const int c = c0 + i, r = r0 + threadIdx.x;
+    if (c < Cc && r < ldo) out[(size_t)c * ldo + r] = t[threadIdx.x][i];
+  }
+}
+
+__device__ __forceinline__ float bf(bf16 v) { return __bfloat162float(v); }
+
+// dZ = dY * (Y > 0) for ReLU layers (in place on dY).
+__global__ void k_relu_back(bf16 *dY, const bf16 *Y, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    if (!(bf(Y[i]) > 0.f)) dY[i] = __float2bfloat16_rn(0.f);
+}
+
+// db[c] += sum over pixels of dZ[p][c].
+__global__ void k_bias_grad(const bf16 *dZ, float *db, size_t P, int C) {
+  const int c = blockIdx.y * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  float s = 0.f;
+  for (size_t p = blockIdx.x; p < P; p += gridDim.x) s += bf(dZ[p * C + c]);
+  atomicAdd(db + c, s);
+}
+
+// 2x2 average pool (NHWC) and its gradient.
+__global__ void k_pool(const bf16 *X, bf16 *Y, int B, int H, int W, int C) {
+  const size_t total = (size_t)B * (H / 2) * (W / 2) * C;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    size_t q = i / C;
+    const int x = (int)(q % (W / 2)), y = (int)((q / (W / 2)) % (H / 2)), b = (int)(q / ((size_t)(W / 2) * (H / 2)));
+    const size_t base = (((size_t)b * H + 2 * y) * W + 2 * x) * C + c;
+    const float s = bf(X[base]) + bf(X[base + C]) + bf(X[base + (size_t)W * C]) + bf(X[base + (size_t)W * C + C]);
+    Y[i] = __float2bfloat16_rn(0.25f * s);
+  }
+}
+// Gradient of the pool, written into channels [coff, coff+C) of a [.., Ctot] tensor (adds when acc).
+__global__ void k_pool_back(const bf16 *dY, bf16 *dX, int B, int H, int W, int C, int Ctot, int coff, int accum) {
+  const size_t total = (size_t)B * H * W * C;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    size_t q = i / C;
+    const int x = (int)(q % W), y = (int)((q / W) % H), b = (int)(q / ((size_t)W * H));
+    const float g = 0.25f * bf(dY[(((size_t)b * (H / 2) + y / 2) * (W / 2) + x / 2) * C + c]);
+    bf16 *o = dX + q * Ctot + coff + c;
+    *o = __float2bfloat16_rn(accum ? bf(*o) + g : g);
+  }
+}
+
+// Nearest 2x upsample of X [B][h][w][C] into channels [0, C) of Y [B][2h][2w][Ctot].
+__global__ void k_upsample(const bf16 *X, bf16 *Y, int B, int h, int w, int C, int Ctot) {
+  const size_t total = (size_t)B * 2 * h * 2 * w * C;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    size_t q = i / C;
+    const int x = (int)(q % (2 * w)), y = (int)((q / (2 * w)) % (2 * h)), b = (int)(q / ((size_t)4 * w * h));
+    Y[q * Ctot + c] = X[(((size_t)b * h + y / 2) * w + x / 2) * C + c];
+  }
+}
+// Gradient of the upsample: dX[b][y][x][c] = sum of the 4 children in channels [0, C) of dY.
+__global__ void k_upsample_back(const bf16 *dY, bf16 *dX, int B, int h, int w, int C, int Ctot) {
+  const size_t total = (size_t)B * h * w * C;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    size_t q = i / C;
+    const int x = (int)(q % w), y = (int)((q / w) % h), b = (int)(q / ((size_t)w * h));
+    const size_t W2 = 2 * w;
+    const size_t base = (((size_t)b * 2 * h + 2 * y) * W2 + 2 * x) * Ctot + c;
+    const float s = bf(dY[base]) + bf(dY[base + Ctot]) + bf(dY[base + W2 * Ctot]) + bf(dY[base + W2 * Ctot + Ctot]);
+    dX[i] = __float2bfloat16_rn(s);
+  }
+}
+
+// Copy X [P][C] into channels [coff, coff+C) of Y [P][Ctot] (and the reverse).
+__global__ void k_copy_ch(const bf16 *X, bf16 *Y, size_t P, int C, int Ctot, int coff) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < P * C; i += (size_t)gridDim.x * blockDim.x)
+    Y[(i / C) * Ctot + coff + i % C] = X[i];
+}
+// dX[p][c] += dY[p][coff + c] (gradient of a skip tensor used in a concat).
+__global__ void k_add_ch(const bf16 *dY, bf16 *dX, size_t P, int C, int Ctot, int coff) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < P * C; i += (size_t)gridDim.x * blockDim.x)
+    dX[i] = __float2bfloat16_rn(bf(dX[i]) + bf(dY[(i / C) * Ctot + coff + i % C]));
+}
+
+__global__ void k_f32_to_bf16(const float *x, bf16 *y, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] = __float2bfloat16_rn(x[i]);
+}
+__global__ void k_bf16_to_f32(const bf16 *x, float *y, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] = __bfloat162float(x[i]);
+}
+
+// Masked mean-squared error: loss = sum m (y - t)^2 / (sum m * C); dY in BF16.
+__global__ void k_mse(const bf16 *Y, const float *T, const float *mask, bf16 *dY, size_t P, int C,
+                      double inv_count, double *loss) {
+  double s = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < P * C; i += (size_t)gridDim.x * blockDim.x) {
+    const float m = mask ? mask[i / C] : 1.f;
+    const float d = bf(Y[i]) - T[i];
+    s += (double)m * d * d;
+    dY[i] = __float2bfloat16_rn((float)(2.0 * inv_count) * m * d);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, s * inv_count);
+}
+
+// Adam on FP32 master weights.
+__global__ void k_adam(float *w, const float *g, float *m, float *v, size_t n, float lr, float b1,
+                       float b2, float eps, float c1, float c2) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+// BF16 copies of one layer's FP32 master weights W[co][Kp] (k = r*Cin + ci,
+// zero beyond taps*Cin): Wt = W for the forward product, and the flipped,
+// transposed Wd[ci][k'] (k' = r*Cout + co, r -> taps-1-r) for the input gradient.
+__global__ void k_weights(const float *W, bf16 *Wt, bf16 *Wd, int Cout, int Cin, int taps, int Kp,
+                          int Kpd) {
+  const int n = Cout * Kp;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    Wt[i] = __float2bfloat16_rn(W[i]);
+  const int nd = Cin * Kpd;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nd; i += gridDim.x * blockDim.x) {
+    const int ci = i / Kpd, k = i % Kpd;
+    float v = 0.f;
+    if (k < taps * Cout) {
+      const int r = k / Cout, co = k % Cout;
+      v = W[(size_t)co * Kp + (taps - 1 - r) * Cin + ci];
+    }
+    Wd[i] = __float2bfloat16_rn(v);
+  }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------- network
+
+namespace {
+
+int rup(int x, int a) { return (x + a - 1) / a * a; }
+int grid_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 32); }
+
+struct Conv {
+  int cin, cout, taps, Kp, Kpd;
+  bool relu;
+  size_t woff, boff;  // master weights W[cout][Kp] and bias b[cout] in the parameter vector
+  bf16 *Wt, *Wd;
+};
+
+struct Act {
+  int h = 0, w = 0, c = 0;
+  bf16 *x = nullptr, *dx = nullptr;
+};
+
+// activation ids
+enum {
+  A_IN, A_E0A, A_E0, A_P0, A_E1A, A_E1, A_P1, A_E2A, A_E2, A_P2, A_E3A, A_E3, A_C2, A_D2A, A_D2,
+  A_C1, A_D1A, A_D1, A_C0, A_D0A, A_D0, A_OUT, A_COUNT
+};
+
+}  // namespace
+
+struct lbm_sg {
+  lbm_sg_config cfg{};
+  std::vector<Conv> conv;
+  Act act[A_COUNT];
+  size_t nparam = 0;
+  float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
+  bf16 *col = nullptr, *colT = nullptr, *dzT = nullptr;
+  float *tgt = nullptr, *msk = nullptr, *xin = nullptr, *yout = nullptr;
+  double *loss = nullptr;
+  int64_t step = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<void *> allocs;
+  float *ds_x = nullptr, *ds_y = nullptr, *ds_m = nullptr;
+  int ds_count = 0;
+};
+
+namespace {
+
+template <class T>
+lbm_status salloc(lbm_sg *s, T **p, size_t count) {
+  cudaError_t e = cudaMalloc((void **)p, std::max<size_t>(count * sizeof(T), 16));
+  if (e != cudaSuccess)
+    return fail(LBM_NOMEM, std::string("surrogate cudaMalloc: ") + cudaGetErrorString(e));
+  s->allocs.push_back((void *)*p);
+  return LBM_OK;
+}
+
+void sfree(lbm_sg *s) {
+  for (void *p : s->allocs) cudaFree(p);
+  s->allocs.clear();
+  if (s->stream) cudaStreamDestroy(s->stream);
+  s->stream = nullptr;
+}
+
+lbm_status gemm(lbm_sg *s, int epi, const bf16 *A, const bf16 *Bt, int M, int N, int K,
+                const float *bias, bf16 *ob, float *of, int splits) {
+  GemmArgs g;
+  g.A = A;
+  g.Bt = Bt;
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.kchunk = rup((K + splits - 1) / splits, GBK);
+  g.bias = bias;
+  g.out_bf16 = ob;
+  g.out_f32 = of;
+  dim3 grid((M + GBM - 1) / GBM, (N + GBN - 1) / GBN, (K + g.kchunk - 1) / g.kchunk);
+  void *args[] = {&g};
+  const void *fn = epi == EPI_BIAS_RELU_BF16 ? (const void *)k_gemm<EPI_BIAS_RELU_BF16>
+                 : epi == EPI_BIAS_BF16       ? (const void *)k_gemm<EPI_BIAS_BF16>
+                 : epi == EPI_BF16            ? (const void *)k_gemm<EPI_BF16>
+                                              : (const void *)k_gemm<EPI_ATOMIC_F32>;
+  cudaError_t e = cudaLaunchKernel(fn, grid, dim3(256), args, 0, s->stream);
+  if (e != cudaSuccess) return fail(LBM_CUDA, std::string("surrogate gemm: ") + cudaGetErrorString(e));
+  return LBM_OK;
+}
+
+void refresh_weights(lbm_sg *s) {
+  for (const Conv &c : s->conv)
+    k_weights<<<64, 256, 0, s->stream>>>(s->w + c.woff, c.Wt, c.Wd, c.cout, c.cin, c.taps, c.Kp, c.Kpd);
+}
+
+lbm_status conv_fwd(lbm_sg *s, int li, int xi, int yi, int B) {
+  const Conv &c = s->conv[li];
+  const Act &X = s->act[xi];
+  Act &Y = s->act[yi];
+  const int M = B * X.h * X.w;
+  const size_t n = (size_t)M * c.Kp;
+  k_im2col<<<grid_for(n), 256, 0, s->stream>>>(X.x, s->col, B, X.h, X.w, X.c, c.taps, c.Kp);
+  return gemm(s, c.relu ? EPI_BIAS_RELU_BF16 : EPI_BIAS_BF16, s->col, c.Wt, M, c.cout, c.Kp,
+              s->w + c.boff, Y.x, nullptr, 1);
+}
+
+// Given Y.dx (gradient of the layer output), accumulates the weight and bias
+// gradients and, when need_dx, writes the input gradient into X.dx.
+lbm_status conv_bwd(lbm_sg *s, int li, int xi, int yi, int B, bool need_dx) {
+  const Conv &c = s->conv[li];
+  Act &X = s->act[xi];
+  Act &Y = s->act[yi];
+  const int M = B * X.h * X.w, Mp = rup(M, GBK);
+  const size_t ny = (size_t)M * c.cout;
+  if (c.relu) k_relu_back<<<grid_for(ny), 256, 0, s->stream>>>(Y.dx, Y.x, ny);
+  k_bias_grad<<<dim3(256, (c.cout + 127) / 128), 128, 0, s->stream>>>(Y.dx, s->g + c.boff, (size_t)M, c.cout);
+  k_im2col<<<grid_for((size_t)M * c.Kp), 256, 0, s->stream>>>(X.x, s->col, B, X.h, X.w, X.c, c.taps, c.Kp);
+  k_transpose<<<dim3((c.Kp + 31) / 32, Mp / 32), dim3(32, 8), 0, s->stream>>>(s->col, s->colT, M, c.Kp, Mp);
+  k_transpose<<<dim3((c.cout + 31) / 32, Mp / 32), dim3(32, 8), 0, s->stream>>>(Y.dx, s->dzT, M, c.cout, Mp);
+  const int splits = std::max(1, std::min(256, Mp / 4096));
+  lbm_status st = gemm(s, EPI_ATOMIC_F32, s->dzT, s->colT, c.cout, c.Kp, Mp, nullptr, nullptr,
+                       s->g + c.woff, splits);
+  if (st != LBM_OK || !need_dx) return st;
+  k_im2col<<<grid_for((size_t)M * c.Kpd), 256, 0, s->stream>>>(Y.dx, s->col, B, X.h, X.w, c.cout, c.taps, c.Kpd);
+  return gemm(s, EPI_BF16, s->col, c.Wd, M, c.cin, c.Kpd, nullptr, X.dx, nullptr, 1);
+}
+
+lbm_status forward(lbm_sg *s, int B) {
+  lbm_status st;
+  const int b = s->cfg.base;
+  auto cf = [&](int li, int xi, int yi) { return conv_fwd(s, li, xi, yi, B); };
+  auto pool = [&](int xi, int yi) {
+    const Act &X = s->act[xi];
+    const size_t n = (size_t)B * (X.h / 2) * (X.w / 2) * X.c;
+    k_pool<<<grid_for(n), 256, 0, s->stream>>>(X.x, s->act[yi].x, B, X.h, X.w, X.c);
+  };
+  auto cat = [&](int lowi, int skipi, int yi) {
+    const Act &L = s->act[lowi], &K = s->act[skipi];
+    Act &Y = s->act[yi];
+    const size_t n = (size_t)B * Y.h * Y.w * L.c;
+    k_upsample<<<grid_for(n), 256, 0, s->stream>>>(L.x, Y.x, B, L.h, L.w, L.c, Y.c);
+    const size_t P = (size_t)B * Y.h * Y.w;
+    k_copy_ch<<<grid_for(P * K.c), 256, 0, s->stream>>>(K.x, Y.x, P, K.c, Y.c, L.c);
+  };
+  (void)b;
+  if ((st = cf(0, A_IN, A_E0A)) || (st = cf(1, A_E0A, A_E0))) return st;
+  pool(A_E0, A_P0);
+  if ((st = cf(2, A_P0, A_E1A)) || (st = cf(3, A_E1A, A_E1))) return st;
+  pool(A_E1, A_P1);
+  if ((st = cf(4, A_P1, A_E2A)) || (st = cf(5, A_E2A, A_E2))) return st;
+  pool(A_E2, A_P2);
+  if ((st = cf(6, A_P2, A_E3A)) || (st = cf(7, A_E3A, A_E3))) return st;
+  cat(A_E3, A_E2, A_C2);
+  if ((st = cf(8, A_C2, A_D2A)) || (st = cf(9, A_D2A, A_D2))) return st;
+  cat(A_D2, A_E1, A_C1);
+  if ((st = cf(10, A_C1, A_D1A)) || (st = cf(11, A_D1A, A_D1))) return st;
+  cat(A_D1, A_E0, A_C0);
+  if ((st = cf(12, A_C0, A_D0A)) || (st = cf(13, A_D0A, A_D0))) return st;
+  return cf(14, A_D0, A_OUT);
+}
+
+lbm_status backward(lbm_sg *s, int B) {
+  lbm_status st;
+  auto cb = [&](int li, int xi, int yi, bool need) { return conv_bwd(s, li, xi, yi, B, need); };
+  // concat split: low part -> upsample gradient into the low tensor (write),
+  // skip part -> skip tensor gradient (write)
+  auto uncat = [&](int lowi, int skipi, int yi) {
+    const Act &L = s->act[lowi], &K = s->act[skipi], &Y = s->act[yi];
+    const size_t nl = (size_t)B * L.h * L.w * L.c;
+    k_upsample_back<<<grid_for(nl), 256, 0, s->stream>>>(Y.dx, L.dx, B, L.h, L.w, L.c, Y.c);
+    const size_t P = (size_t)B * Y.h * Y.w;
+    cudaMemsetAsync(K.dx, 0, P * K.c * sizeof(bf16), s->stream);
+    k_add_ch<<<grid_for(P * K.c), 256, 0, s->stream>>>(Y.dx, K.dx, P, K.c, Y.c, L.c);
+  };
+  auto unpool = [&](int xi, int yi) {  // adds the pool gradient into X.dx
+    const Act &X = s->act[xi];
+    const size_t n = (size_t)B * X.h * X.w * X.c;
+    k_pool_back<<<grid_for(n), 256, 0, s->stream>>>(s->act[yi].dx, s->act[xi].dx, B, X.h, X.w, X.c, X.c, 0, 1);
+  };
+  if ((st = cb(14, A_D0, A_OUT, true)) || (st = cb(13, A_D0A, A_D0, true)) ||
+      (st = cb(12, A_C0, A_D0A, true)))
+    return st;
+  uncat(A_D1, A_E0, A_C0);
+  if ((st = cb(11, A_D1A, A_D1, true)) || (st = cb(10, A_C1, A_D1A, true))) return st;
+  uncat(A_D2, A_E1, A_C1);
+  if ((st = cb(9, A_D2A, A_D2, true)) || (st = cb(8, A_C2, A_D2A, true))) return st;
+  uncat(A_E3, A_E2, A_C2);
+  if ((st = cb(7, A_E3A, A_E3, true)) || (st = cb(6, A_P2, A_E3A, true))) return st;
+  unpool(A_E2, A_P2);
+  if ((st = cb(5, A_E2A, A_E2, true)) || (st = cb(4, A_P1, A_E2A, true))) return st;
+  unpool(A_E1, A_P1);
+  if ((st = cb(3, A_E1A, A_E1, true)) || (st = cb(2, A_P0, A_E1A, true))) return st;
+  unpool(A_E0, A_P0);
+  if ((st = cb(1, A_E0A, A_E0, true)) || (st = cb(0, A_IN, A_E0A, false))) return st;
+  return LBM_OK;
+}
+
+// Loss and gradients of one batch whose FP32 inputs are at s->xin, targets at
+// s->tgt and masks at s->msk (device).
+lbm_status loss_grads(lbm_sg *s, int B, double *loss_out) {
+  const lbm_sg_config &c = s->cfg;
+  const size_t P = (size_t)B * c.height * c.width;
+  k_f32_to_bf16<<<grid_for(P * c.in_channels), 256, 0, s->stream>>>(s->xin, s->act[A_IN].x, P * c.in_channels);
+  lbm_status st = forward(s, B);
+  if (st != LBM_OK) return st;
+  cudaMemsetAsync(s->g, 0, s->nparam * sizeof(float), s->stream);
+  cudaMemsetAsync(s->loss, 0, sizeof(double), s->stream);
+  // mean over masked cells and output channels
+  std::vector<float> hm;
+  double count = 0;
+  {
+    hm.resize(P);
+    cudaMemcpyAsync(hm.data(), s->msk, P * sizeof(float), cudaMemcpyDeviceToHost, s->stream);
+    cudaStreamSynchronize(s->stream);
+    for (float x : hm) count += x;
+  }
+  const double inv = count > 0 ? 1.0 / (count * c.out_channels) : 0.0;
+  k_mse<<<grid_for(P * c.out_channels), 256, 0, s->stream>>>(s->act[A_OUT].x, s->tgt, s->msk, s->act[A_OUT].dx, P,
+                                                           c.out_channels, inv, s->loss);
+  if ((st = backward(s, B)) != LBM_OK) return st;
+  double h = 0;
+  cudaMemcpyAsync(&h, s->loss, sizeof h, cudaMemcpyDeviceToHost, s->stream);
+  if (cudaStreamSynchronize(s->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+    return fail(LBM_CUDA, "surrogate step failed");
+  if (loss_out) *loss_out = h;
+  return LBM_OK;
+}
+
+void adam(lbm_sg *s) {
+  s->step++;
+  const lbm_sg_config &c = s->cfg;
+  const float c1 = 1.f - std::pow(c.beta1, (float)s->step), c2 = 1.f - std::pow(c.beta2, (float)s->step);
+  k_adam<<<grid_for(s->nparam), 256, 0, s->stream>>>(s->w, s->g, s->m, s->v, s->nparam, c.lr, c.beta1,
+                                                     c.beta2, c.eps, c1, c2);
+  refresh_weights(s);
+}
+
+}  // namespace
+
+extern "C" {
+
+lbm_status lbm_sg_create(const lbm_sg_config *cfg, lbm_sg **out) {
+  if (!cfg || !out) return fail(LBM_INVALID, "null argument");
+  *out = nullptr;
+  const int H = cfg->height, W = cfg->width, b = cfg->base;
+  if (H < 16 || W < 16 || H % 8 || W % 8 || b < 8 || b % 8 || cfg->in_channels < 1 ||
+      cfg->out_channels < 1 || cfg->out_channels > 64 || cfg->max_batch < 1)
+    return fail(LBM_INVALID, "surrogate: H, W multiples of 8 (>= 16), base multiple of 8");
+  lbm_sg *s = new lbm_sg();
+  s->cfg = *cfg;
+  auto bail = [&](lbm_status st) {
+    sfree(s);
+    delete s;
+    return st;
+  };
+  if (cudaSetDevice(cfg->device) != cudaSuccess) return bail(fail(LBM_CUDA, "cudaSetDevice failed"));
+  cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  const int ci = cfg->in_channels, co = cfg->out_channels;
+  // (cin, cout, taps, relu) in forward order
+  const int L[15][4] = {{ci, b, 9, 1},          {b, b, 9, 1},          {b, 2 * b, 9, 1},
+                        {2 * b, 2 * b, 9, 1},   {2 * b, 4 * b, 9, 1},  {4 * b, 4 * b, 9, 1},
+                        {4 * b, 4 * b, 9, 1},   {4 * b, 4 * b, 9, 1},  {8 * b, 4 * b, 9, 1},
+                        {4 * b, 4 * b, 9, 1},   {6 * b, 2 * b, 9, 1},  {2 * b, 2 * b, 9, 1},
+                        {3 * b, b, 9, 1},       {b, b, 9, 1},          {b, co, 1, 0}};
+  size_t off = 0;
+  for (auto &l : L) {
+    Conv c;
+    c.cin = l[0];
+    c.cout = l[1];
+    c.taps = l[2];
+    c.relu = l[3] != 0;
+    c.Kp = rup(c.taps * c.cin, GBK);
+    c.Kpd = rup(c.taps * c.cout, GBK);
+    c.woff = off;
+    off += (size_t)c.cout * c.Kp;
+    c.boff = off;
+    off += c.cout;
+    s->conv.push_back(c);
+  }
+  s->nparam = off;
+  lbm_status st;
+  if ((st = salloc(s, &s->w, off)) || (st = salloc(s, &s->g, off)) || (st = salloc(s, &s->m, off)) ||
+      (st = salloc(s, &s->v, off)))
+    return bail(st);
+  for (Conv &c : s->conv)
+    if ((st = salloc(s, &c.Wt, (size_t)c.cout * c.Kp)) || (st = salloc(s, &c.Wd, (size_t)c.cin * c.Kpd)))
+      return bail(st);
+  // He-normal initial weights (padding columns and biases zero)
+  std::vector<float> hw(off, 0.f);
+  std::mt19937_64 rng(cfg->seed);
+  for (const Conv &c : s->conv) {
+    std::normal_distribution<float> nd(0.f, std::sqrt(2.f / (c.taps * c.cin)));
+    for (int o = 0; o < c.cout; o++)
+      for (int k = 0; k < c.taps * c.cin; k++) hw[c.woff + (size_t)o * c.Kp + k] = nd(rng);
+  }
+  cudaMemcpy(s->w, hw.data(), off * sizeof(float), cudaMemcpyHostToDevice);
+  cudaMemset(s->m, 0, off * sizeof(float));
+  cudaMemset(s->v, 0, off * sizeof(float));
+  // activations
+  const int B = cfg->max_batch;
+  const int sh[A_COUNT][3] = {
+      {0, 0, ci},     {0, 0, b},      {0, 0, b},      {1, 1, b},      {1, 1, 2 * b},
+      {1, 1, 2 * b},  {2, 2, 2 * b},  {2, 2, 4 * b},  {2, 2, 4 * b},  {3, 3, 4 * b},
+      {3, 3, 4 * b},  {3, 3, 4 * b},  {2, 2, 8 * b},  {2, 2, 4 * b},  {2, 2, 4 * b},
+      {1, 1, 6 * b},  {1, 1, 2 * b},  {1, 1, 2 * b},  {0, 0, 3 * b},  {0, 0, b},
+      {0, 0, b},      {0, 0, co}};
+  size_t max_col = 0, max_colT = 0, max_dz = 0;
+  for (int a = 0; a < A_COUNT; a++) {
+    Act &A = s->act[a];
+    A.h = H >> sh[a][0];
+    A.w = W >> sh[a][1];
+    A.c = sh[a][2];
+    const size_t n = (size_t)B * A.h * A.w * A.c;
+    if ((st = salloc(s, &A.x, n)) || (st = salloc(s, &A.dx, n))) return bail(st);
+  }
+  const int xs[15] = {A_IN, A_E0A, A_P0, A_E1A, A_P1, A_E2A, A_P2, A_E3A, A_C2, A_D2A, A_C1, A_D1A, A_C0, A_D0A, A_D0};
+  for (int li = 0; li < 15; li++) {
+    const Conv &c = s->conv[li];
+    const Act &X = s->act[xs[li]];
+    const size_t M = (size_t)B * X.h * X.w, Mp = (size_t)rup((int)M, GBK);
+    max_col = std::max(max_col, M * std::max(c.Kp, c.Kpd));
+    max_colT = std::max(max_colT, Mp * c.Kp);
+    max_dz = std::max(max_dz, Mp * c.cout);
+  }
+  const size_t P = (size_t)B * H * W;
+  if ((st = salloc(s, &s->col, max_col)) || (st = salloc(s, &s->colT, max_colT)) ||
+      (st = salloc(s, &s->dzT, max_dz)) || (st = salloc(s, &s->tgt, P * co)) ||
+      (st = salloc(s, &s->msk, P)) || (st = salloc(s, &s->xin, P * ci)) ||
+      (st = salloc(s, &s->yout, P * co)) || (st = salloc(s, &s->loss, 1)))
+    return bail(st);
+  refresh_weights(s);
+  if (cudaStreamSynchronize(s->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+    return bail(fail(LBM_CUDA, "surrogate set-up failed"));
+  *out = s;
+  return LBM_OK;
+}
+
+void lbm_sg_destroy(lbm_sg *s) {
+  if (!s) return;
+  sfree(s);
+  delete s;
+}
+
+lbm_status lbm_sg_num_params(const lbm_sg *s, int64_t *n) {
+  if (!s || !n) return fail(LBM_INVALID, "null argument");
+  *n = (int64_t)s->nparam;
+  return LBM_OK;
+}
+
+lbm_status lbm_sg_get_params(lbm_sg *s, float *out) {
+  if (!s || !out) return fail(LBM_INVALID, "null argument");
+  if (cudaMemcpy(out, s->w, s->nparam * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return fail(LBM_CUDA, "surrogate parameter read-back");
+  return LBM_OK;
+}
+
+lbm_status lbm_sg_set_params(lbm_sg *s, const float *in) {
+  if (!s || !in) return fail(LBM_INVALID, "null argument");
+  if (cudaMemcpy(s->w, in, s->nparam * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+    return fail(LBM_CUDA, "surrogate parameter upload");
+  refresh_weights(s);
+  cudaStreamSynchronize(s->stream);
+  return LBM_OK;
+}
+
+lbm_status lbm_sg_forward(lbm_sg *s, int32_t batch, const float *x, float *y) {
+  if (!s || !x || !y || batch < 1 || batch > s->cfg.max_batch) return fail(LBM_INVALID, "bad batch");
+  const lbm_sg_config &c = s->cfg;
+  const size_t P = (size_t)batch * c.height * c.width;
+  cudaMemcpyAsync(s->xin, x, P * c.in_channels * sizeof(float), cudaMemcpyHostToDevice, s->stream);
+  k_f32_to_bf16<<<grid_for(P * c.in_channels), 256, 0, s->stream>>>(s->xin, s->act[A_IN].x, P * c.in_channels);
+  lbm_status st = forward(s, batch);
+  if (st != LBM_OK) return st;
+  k_bf16_to_f32<<<grid_for(P * c.out_channels), 256, 0, s->stream>>>(s->act[A_OUT].x, s->yout, P * c.out_channels);
+  cudaMemcpyAsync(y, s->yout, P * c.out_channels * sizeof(float), cudaMemcpyDeviceToHost, s->stream);
+  if (cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(LBM_CUDA, "surrogate forward failed");
+  return LBM_OK;
+}
+
+lbm_status lbm_sg_loss_grads(lbm_sg *s, int32_t batch, const float *x, const float *target,
+                             const float *mask, double *loss, float *grads) {
+  if (!s || !x || !target || batch < 1 || batch > s->cfg.max_batch) return fail(LBM_INVALID, "bad batch");
+  const lbm_sg_config &c = s->cfg;
+  const size_t P = (size_t)batch * c.height * c.width;
+  cudaMemcpyAsync(s->xin, x, P * c.in_channels * sizeof(float), cudaMemcpyHostToDevice, s->stream);
+  cudaMemcpyAsync(s->tgt, target, P * c.out_channels * sizeof(float), cudaMemcpyHostToDevice, s->stream);
+  if (mask) cudaMemcpyAsync(s->msk, mask, P * sizeof(float), cudaMemcpyHostToDevice, s->stream);
+  else {
+    std::vector<float> ones(P, 1.f);
+    cudaMemcpyAsync(s->msk, ones.data(), P * sizeof(float), cudaMemcpyHostToDevice, s->stream);
+    cudaStreamSynchronize(s->stream);
+  }
+  lbm_status st = loss_grads(s, batch, loss);
+  if (st != LBM_OK) return st;
+  if (grads && cudaMemcpy(grads, s->g, s->nparam * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return fail(LBM_CUDA, "surrogate gradient read-back");
+  return LBM_OK;
+}
+
+lbm_status lbm_sg_set_dataset(lbm_sg *s, int32_t count, const float *x, const float *y,
+                              const float *mask) {
+  if (!s || count < 1 || !x || !y || !mask) return fail(LBM_INVALID, "bad dataset");
+  const lbm_sg_config &c = s->cfg;
+  const size_t P = (size_t)c.height * c.width;
+  lbm_status st;
+  if (s->ds_x) {
+    cudaFree(s->ds_x);
+    cudaFree(s->ds_y);
+    cudaFree(s->ds_m);
+    s->ds_x = s->ds_y = s->ds_m = nullptr;
+  }
+  if (cudaMalloc((void **)&s->ds_x, count * P * c.in_channels * sizeof(float)) != cudaSuccess ||
+      cudaMalloc((void **)&s->ds_y, count * P * c.out_channels * sizeof(float)) != cudaSuccess ||
+      cudaMalloc((void **)&s->ds_m, count * P * sizeof(float)) != cudaSuccess)
+    return fail(LBM_NOMEM, "surrogate dataset allocation");
+  (void)st;
+  cudaMemcpy(s->ds_x, x, count * P * c.in_channels * sizeof(float), cudaMemcpyHostToDevice);
+  cudaMemcpy(s->ds_y, y, count * P * c.out_channels * sizeof(float), cudaMemcpyHostToDevice);
+  cudaMemcpy(s->ds_m, mask, count * P * sizeof(float), cudaMemcpyHostToDevice);
+  s->ds_count = count;
+  return LBM_OK;
+}
+
+lbm_status lbm_sg_train(lbm_sg *s, int32_t batch, const int32_t *order, int32_t n, double *mean_loss) {
+  if (!s || !order || n < 1 || batch < 1 || batch > s->cfg.max_batch || !s->ds_x)
+    return fail(LBM_INVALID, "bad training call");
+  const lbm_sg_config &c = s->cfg;
+  const size_t P = (size_t)c.height * c.width;
+  double total = 0;
+  int steps = 0;
+  for (int i0 = 0; i0 + batch <= n; i0 += batch) {
+    for (int j = 0; j < batch; j++) {
+      const int idx = order[i0 + j];
+      if (idx < 0 || idx >= s->ds_count) return fail(LBM_INVALID, "sample index out of range");
+      cudaMemcpyAsync(s->xin + j * P * c.in_channels, s->ds_x + (size_t)idx * P * c.in_channels,
+                      P * c.in_channels * sizeof(float), cudaMemcpyDeviceToDevice, s->stream);
+      cudaMemcpyAsync(s->tgt + j * P * c.out_channels, s->ds_y + (size_t)idx * P * c.out_channels,
+                      P * c.out_channels * sizeof(float), cudaMemcpyDeviceToDevice, s->stream);
+      cudaMemcpyAsync(s->msk + j * P, s->ds_m + (size_t)idx * P, P * sizeof(float),
+                      cudaMemcpyDeviceToDevice, s->stream);
+    }
+    double l = 0;
+    lbm_status st = loss_grads(s, batch, &l);
+    if (st != LBM_OK) return st;
+    adam(s);
+    total += l;
+    steps++;
+  }
+  if (cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(LBM_CUDA, "surrogate training failed");
+  if (mean_loss) *mean_loss = steps ? total / steps : 0.0;
+  return LBM_OK;
+}
+
+lbm_status lbm_sg_adam_step(lbm_sg *s) {
+  if (!s) return fail(LBM_INVALID, "null argument");
+  adam(s);
+  if (cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(LBM_CUDA, "adam failed");
+  return LBM_OK;
+}
+
+}  // extern "C"

@@ -92,7 +92,8 @@ typedef struct lbm_ctx lbm_ctx;
 typedef struct lbm_diagnostics {
   int64_t iteration;   /* completed iterations */
   double l2_full;      /* ||F - METAF||_2 over fluid cells (the CUDA/UPC variants' residual) */
-  double du_rel;       /* ||(u,v) - (u,v)_prev|| / ||(u,v)|| since the previous lbm_check */
+  double du_rel;       /* relative change per step: ||(u,v) - (u,v)_prev|| / ||(u,v)|| since
+                          the previous lbm_check, divided by the iterations in between */
   double mass;         /* sum rho over fluid cells */
   double momentum[2];  /* sum rho u, sum rho v */
   double force[2];     /* momentum-exchange force on wall links of drag_lift_id cells */
@@ -197,8 +198,9 @@ lbm_status lbm_batch_set_tile(lbm_batch *b, int32_t tile_variant);
 lbm_status lbm_batch_autotune(lbm_batch *b, int32_t steps_per_trial, char *report,
                               size_t report_cap);
 /* Steps every unconverged case until all have converged or max_steps have run.
- * Every check_every steps each active case gets du_rel = ||(u,v) - (u,v)_prev||
- * / ||(u,v)|| against the previous check (FP64 sums); a case with du_rel <= tol
+ * Every check_every steps each active case gets the relative change per step
+ * du_rel = ||(u,v) - (u,v)_prev|| / (check_every ||(u,v)||) against the previous
+ * check (FP64 sums), so tol does not depend on check_every; a case with du_rel <= tol
  * stops stepping.  Per case (any pointer may be NULL): fused steps run (the
  * completed iterations are one more), the last du_rel, converged (1 yes, 0 no,
  * -1 NaN seen); seconds = wall time of the loop.  LBM_DIVERGED if a case saw NaN. */
@@ -225,7 +227,7 @@ lbm_status lbm_batch_info(const lbm_batch *b, int64_t *nodes, int64_t *fluid_nod
 typedef struct lbm_sg lbm_sg;
 typedef struct lbm_sg_config {
   int32_t height, width;   /* multiples of 8, >= 16 */
-  int32_t in_channels, out_channels;
+  int32_t in_channels, out_channels;  /* out_channels <= 8 or a multiple of 8 (<= 64) */
   int32_t base;            /* channels of the first level (multiple of 8) */
   int32_t max_batch;
   float lr, beta1, beta2, eps;  /* Adam */
@@ -244,6 +246,8 @@ lbm_status lbm_sg_forward(lbm_sg *s, int32_t batch, const float *x, float *y);
  * mask NULL = all ones; grads (NULL = not copied) receives num_params floats. */
 lbm_status lbm_sg_loss_grads(lbm_sg *s, int32_t batch, const float *x, const float *target,
                              const float *mask, double *loss, float *grads);
+/* Learning rate of the following Adam updates (schedules). */
+lbm_status lbm_sg_set_lr(lbm_sg *s, float lr);
 /* One Adam update from the gradients of the last lbm_sg_loss_grads. */
 lbm_status lbm_sg_adam_step(lbm_sg *s);
 /* Keeps count samples (x, target, mask) on the device for lbm_sg_train. */

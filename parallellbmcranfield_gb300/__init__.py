@@ -64,7 +64,7 @@ EXPORTS = ["lbm_status_string", "lbm_last_error", "lbm_create", "lbm_destroy", "
            "lbm_batch_info", "lbm_mesh_read", "lbm_mesh_cavity", "lbm_mesh_channel", "lbm_mesh_write",
            "lbm_mesh_free", "lbm_sg_create", "lbm_sg_destroy", "lbm_sg_num_params",
            "lbm_sg_get_params", "lbm_sg_set_params", "lbm_sg_forward", "lbm_sg_loss_grads",
-           "lbm_sg_adam_step", "lbm_sg_set_dataset", "lbm_sg_train"]
+           "lbm_sg_adam_step", "lbm_sg_set_dataset", "lbm_sg_train", "lbm_sg_set_lr"]
 
 _lib = None
 
@@ -391,11 +391,12 @@ def _load_sg(L):
     L.lbm_sg_forward.argtypes = [vp, i32, dp, dp]
     L.lbm_sg_loss_grads.argtypes = [vp, i32, dp, dp, dp, C.POINTER(C.c_double), dp]
     L.lbm_sg_adam_step.argtypes = [vp]
+    L.lbm_sg_set_lr.argtypes = [vp, C.c_float]
     L.lbm_sg_set_dataset.argtypes = [vp, i32, dp, dp, dp]
     L.lbm_sg_train.argtypes = [vp, i32, dp, i32, C.POINTER(C.c_double)]
     for n in ("lbm_sg_create", "lbm_sg_num_params", "lbm_sg_get_params", "lbm_sg_set_params",
               "lbm_sg_forward", "lbm_sg_loss_grads", "lbm_sg_adam_step", "lbm_sg_set_dataset",
-              "lbm_sg_train"):
+              "lbm_sg_train", "lbm_sg_set_lr"):
         getattr(L, n).restype = C.c_int
     L._sg_ready = True
     return L
@@ -449,6 +450,9 @@ class Surrogate:
 
     def adam_step(self):
         _check(self.L.lbm_sg_adam_step(self.h), "lbm_sg_adam_step")
+
+    def set_lr(self, lr):
+        _check(self.L.lbm_sg_set_lr(self.h, float(lr)), "lbm_sg_set_lr")
 
     def set_dataset(self, x, y, m):
         self._ds = [np.ascontiguousarray(a, np.float32) for a in (x, y, m)]

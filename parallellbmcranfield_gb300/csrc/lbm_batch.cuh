@@ -122,12 +122,14 @@ __global__ void __launch_bounds__(128) k_batch_du(const BatchCase *cases, const 
   }
 }
 
-// Per-case convergence decision after k_batch_du.
-static __global__ void k_batch_converge(int ncases, BatchState s, double tol) {
+// Per-case convergence decision after k_batch_du.  du_rel is the relative
+// change per step: ||(u,v) - (u,v)_prev|| / ||(u,v)|| over the check interval,
+// times inv_span = 1 / (steps in the interval).
+static __global__ void k_batch_converge(int ncases, BatchState s, double tol, double inv_span) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncases || !s.active[c]) return;
   const double uu = s.acc[2 * c + 1];
-  const double du = uu > 0 ? sqrt(s.acc[2 * c] / uu) : INFINITY;
+  const double du = uu > 0 ? sqrt(s.acc[2 * c] / uu) * inv_span : INFINITY;
   s.du_last[c] = s.have_prev[c] ? du : INFINITY;
   if (s.bad[c]) {
     s.active[c] = 0;  // diverged: frozen, reported by the host

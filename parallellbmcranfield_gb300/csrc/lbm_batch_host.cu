@@ -167,12 +167,13 @@ lbm_status launch_steps(lbm_batch *b, int k) {
   return LBM_OK;
 }
 
-lbm_status launch_check(lbm_batch *b, double tol) {
+lbm_status launch_check(lbm_batch *b, int k, double tol) {
   const int grid = std::min(b->nrows, persistent_blocks(b->bk->du, 128, b->device));
   void *args[] = {&b->d_cases, &b->d_rows, &b->nrows, &b->s};
   cudaError_t e = cudaLaunchKernel(b->bk->du, dim3(grid), dim3(128), args, 0, b->stream);
   if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch du: ") + cudaGetErrorString(e));
-  void *cargs[] = {&b->nc, &b->s, &tol};
+  double inv_span = 1.0 / k;
+  void *cargs[] = {&b->nc, &b->s, &tol, &inv_span};
   e = cudaLaunchKernel(b->bk->converge, dim3((b->nc + 255) / 256), dim3(256), cargs, 0, b->stream);
   if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch converge: ") + cudaGetErrorString(e));
   return LBM_OK;
@@ -189,7 +190,7 @@ lbm_status ensure_graph(lbm_batch *b, int k, double tol) {
   cudaGraph_t g;
   LBM_BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   lbm_status s = launch_steps(b, k);
-  if (s == LBM_OK) s = launch_check(b, tol);
+  if (s == LBM_OK) s = launch_check(b, k, tol);
   cudaError_t e = cudaStreamEndCapture(b->stream, &g);
   if (s != LBM_OK) return s;
   if (e != cudaSuccess) return fail(LBM_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));

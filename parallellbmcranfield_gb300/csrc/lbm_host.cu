@@ -44,6 +44,7 @@ struct lbm_ctx {
   double *d_rho0 = nullptr, *d_u0 = nullptr, *d_v0 = nullptr;
   float *d_uprev = nullptr, *d_vprev = nullptr;
   bool have_prev = false;
+  int64_t prev_iter = 0;     // iteration of the previous lbm_check (du_rel interval)
   double *d_partial = nullptr, *d_sums = nullptr;
   double *d_hist = nullptr;
   int hist_cap = 0;
@@ -543,8 +544,10 @@ lbm_status lbm_check(lbm_ctx *ctx, lbm_diagnostics *out) {
   out->force[0] = h[lbm::S_FX];
   out->force[1] = h[lbm::S_FY];
   out->max_speed = h[lbm::S_VMAX];
-  out->du_rel = ctx->have_prev ? std::sqrt(h[lbm::S_DU] / h[lbm::S_UU]) : INFINITY;
+  const int64_t span = std::max<int64_t>(1, ctx->iter - ctx->prev_iter);
+  out->du_rel = ctx->have_prev ? std::sqrt(h[lbm::S_DU] / h[lbm::S_UU]) / (double)span : INFINITY;
   ctx->have_prev = true;
+  ctx->prev_iter = ctx->iter;
   if (h[lbm::S_NAN] > 0 || h[lbm::S_MASS] != h[lbm::S_MASS])
     return fail(LBM_DIVERGED, "NaN in the macroscopic fields");
   return LBM_OK;

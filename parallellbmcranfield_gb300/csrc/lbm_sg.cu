@@ -30,7 +30,7 @@ namespace {
 
 // ------------------------------------------------------------------ kernels
 
-constexpr int GBM = 128, GBN = 64, GBK = 32, GPAD = 8;
+constexpr int GBM = 128, GBK = 32, GPAD = 8, GSTAGES = 3;
 
 enum Epi : int {
   EPI_BIAS_RELU_BF16 = 0,  // forward conv with ReLU
@@ -40,7 +40,9 @@ enum Epi : int {
 };
 
 struct GemmArgs {
-  const bf16 *A;   // [M][K]
+  const bf16 *A;   // [M][K] (explicit operand)
+  const bf16 *X;   // [B][H][W][C] source of the implicit im2col operand
+  int H, W, C, taps;
   const bf16 *Bt;  // [N][K]
   int M, N, K;     // K multiple of GBK
   int kchunk;      // K range per blockIdx.z (multiple of GBK)
@@ -57,17 +59,208 @@ __device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], const 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
+// 16-byte global -> shared copy; with pred false the 16 bytes are zero-filled
+// and nothing is read (src-size 0).
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, bool pred) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  const int n = pred ? 16 : 0;
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(n));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+// Four transposed 8x8 BF16 matrices from shared memory (one row address per lane).
+__device__ __forceinline__ void ldsm_x4_t(uint32_t r[4], const void *row) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(row);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(sa));
+}
+
 // C[M][N] = A[M][K] x Bt[N][K]^T.  256 threads: 8 warps as 4 (M) x 2 (N), each
-// warp 32 x 32 = 2 m16 x 4 n8 tiles; K in steps of 32 staged in shared memory.
-template <int EPI>
+// warp 32 x BN/2; K in tiles of 32 through a GSTAGES-deep cp.async ring.  With
+// GATHER the A operand is the im2col of X, formed while loading: row p is a
+// pixel, column k = r*C + c is channel c of the pixel at tap offset r (3x3,
+// pad 1, or 1x1); C is a multiple of GBK, so one K tile lies within one tap.
+template <int EPI, bool GATHER, int BN>
 __global__ void __launch_bounds__(256) k_gemm(const GemmArgs g) {
-  __shared__ __align__(16) bf16 As[GBM][GBK + GPAD];
-  __shared__ __align__(16) bf16 Bs[GBN][GBK + GPAD];
+  constexpr int NJ = BN / 16;  // n8 tiles per warp
+  __shared__ __align__(16) bf16 As[GSTAGES][GBM][GBK + GPAD];
+  __shared__ __align__(16) bf16 Bs[GSTAGES][BN][GBK + GPAD];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wm = warp & 3, wn = warp >> 2;
-  const int m0 = blockIdx.x * GBM, n0 = blockIdx.y * GBN;
+  const int m0 = blockIdx.x * GBM, n0 = blockIdx.y * BN;
   const int kbeg = blockIdx.z * g.kchunk;
   const int kend = min(g.K, kbeg + g.kchunk);
+  const int nk = (kend - kbeg) / GBK;
+  // the two A chunks (row, 8-column group) this thread loads in every stage
+  int arow[2], ac8[2], ay[2] = {0, 0}, ax[2] = {0, 0};
+  bool aok[2];
+#pragma unroll
+  for (int it = 0; it < 2; it++) {
+    const int ch = tid + it * 256;
+    arow[it] = ch >> 2;
+    ac8[it] = (ch & 3) * 8;
+    const int p = m0 + arow[it];
+    aok[it] = p < g.M;
+    if (GATHER) {
+      ax[it] = p % g.W;
+      ay[it] = (p / g.W) % g.H;
+    }
+  }
+  auto load = [&](int stage, int k0) {
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+      const int p = m0 + arow[it];
+      const bf16 *src = g.Bt;  // any valid address when nothing is read
+      bool ok = aok[it];
+      if (GATHER) {
+        const int r = k0 / g.C, c0 = k0 - r * g.C;
+        const int dy = g.taps == 9 ? r / 3 - 1 : 0, dx = g.taps == 9 ? r % 3 - 1 : 0;
+        const int yy = ay[it] + dy, xx = ax[it] + dx;
+        ok = ok && yy >= 0 && yy < g.H && xx >= 0 && xx < g.W;
+        if (ok) src = g.X + (size_t)(p + dy * g.W + dx) * g.C + c0 + ac8[it];
+      } else if (ok) {
+        src = g.A + (size_t)p * g.K + k0 + ac8[it];
+      }
+      cp_async16(&As[stage][arow[it]][ac8[it]], src, ok);
+    }
+    if (tid < BN * 4) {
+      const int r = tid >> 2, c8 = (tid & 3) * 8;
+      const bool ok = n0 + r < g.N;
+      cp_async16(&Bs[stage][r][c8], ok ? g.Bt + (size_t)(n0 + r) * g.K + k0 + c8 : g.Bt, ok);
+    }
+  };
+  float acc[2][NJ][4];
+#pragma unroll
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int j = 0; j < NJ; j++)
+#pragma unroll
+      for (int r = 0; r < 4; r++) acc[i][j][r] = 0.f;
+  const int gq = lane >> 2, tq = lane & 3;
+#pragma unroll
+  for (int st = 0; st < GSTAGES - 1; st++) {
+    if (st < nk) load(st, kbeg + st * GBK);
+    cp_async_commit();
+  }
+  for (int kt = 0; kt < nk; kt++) {
+    cp_async_wait<GSTAGES - 2>();
+    __syncthreads();
+    if (kt + GSTAGES - 1 < nk) load((kt + GSTAGES - 1) % GSTAGES, kbeg + (kt + GSTAGES - 1) * GBK);
+    cp_async_commit();
+    const int stg = kt % GSTAGES;
+#pragma unroll
+    for (int kk = 0; kk < GBK; kk += 16) {
+      uint32_t af[2][4], bfr[NJ][2];
+#pragma unroll
+      for (int i = 0; i < 2; i++) {
+        const int r = wm * 32 + i * 16 + gq;
+        af[i][0] = *(const uint32_t *)&As[stg][r][kk + 2 * tq];
+        af[i][1] = *(const uint32_t *)&As[stg][r + 8][kk + 2 * tq];
+        af[i][2] = *(const uint32_t *)&As[stg][r][kk + 2 * tq + 8];
+        af[i][3] = *(const uint32_t *)&As[stg][r + 8][kk + 2 * tq + 8];
+      }
+#pragma unroll
+      for (int j = 0; j < NJ; j++) {
+        const int c = wn * (BN / 2) + j * 8 + gq;
+        bfr[j][0] = *(const uint32_t *)&Bs[stg][c][kk + 2 * tq];
+        bfr[j][1] = *(const uint32_t *)&Bs[stg][c][kk + 2 * tq + 8];
+      }
+#pragma unroll
+      for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < NJ; j++) mma_bf16(acc[i][j], af[i], bfr[j]);
+    }
+  }
+  cp_async_wait<0>();
+  // epilogue: c0,c1 at (row gq, cols 2tq, 2tq+1), c2,c3 at row gq+8
+#pragma unroll
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int j = 0; j < NJ; j++)
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int row = m0 + wm * 32 + i * 16 + gq + h * 8;
+        if (row >= g.M) continue;
+        const int col = n0 + wn * (BN / 2) + j * 8 + 2 * tq;
+        const size_t o = (size_t)row * g.N + col;
+        float v0 = acc[i][j][h * 2], v1 = acc[i][j][h * 2 + 1];
+        if (EPI == EPI_ATOMIC_F32) {
+          if (col < g.N) atomicAdd(g.out_f32 + o, v0);
+          if (col + 1 < g.N) atomicAdd(g.out_f32 + o + 1, v1);
+          continue;
+        }
+        if (EPI != EPI_BF16) {
+          if (col < g.N) v0 += g.bias[col];
+          if (col + 1 < g.N) v1 += g.bias[col + 1];
+        }
+        if (EPI == EPI_BIAS_RELU_BF16) {
+          v0 = fmaxf(v0, 0.f);
+          v1 = fmaxf(v1, 0.f);
+        }
+        if (col + 1 < g.N && (g.N & 1) == 0) {
+          *(__nv_bfloat162 *)(g.out_bf16 + o) = __floats2bfloat162_rn(v0, v1);
+        } else {
+          if (col < g.N) g.out_bf16[o] = __float2bfloat16_rn(v0);
+          if (col + 1 < g.N) g.out_bf16[o + 1] = __float2bfloat16_rn(v1);
+        }
+      }
+}
+
+// Weight gradient of a convolution without im2col in memory:
+// dW[co][k] += sum over pixels p of dZ[p][co] * X[p at tap r(k)][c(k)],
+// k = r*C + c < taps*C, C and Cout multiples of 8.  128 threads as 2 (Cout) x
+// 2 (k) warps of 32 x 32; K runs over pixels in tiles of 32 (split over
+// blockIdx.z, FP32 atomics into dW whose rows are ldw long).  Both tiles are
+// held pixel-major in shared memory and read with transposing ldmatrix.
+constexpr int DWM = 64, DWN = 64, DWK = 32, DWPAD = 8;
+__global__ void __launch_bounds__(128) k_gemm_dw(const bf16 *dZ, const bf16 *X, float *dW, int P,
+                                                 int H, int W, int C, int taps, int Cout, int ldw,
+                                                 int pchunk) {
+  __shared__ __align__(16) bf16 Zs[GSTAGES][DWK][DWM + DWPAD];
+  __shared__ __align__(16) bf16 Xs[GSTAGES][DWK][DWN + DWPAD];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = warp & 1, wn = warp >> 1;
+  const int m0 = blockIdx.x * DWM, n0 = blockIdx.y * DWN;
+  const int pbeg = blockIdx.z * pchunk, pend = min(P, pbeg + pchunk);
+  const int nk = (pend - pbeg + DWK - 1) / DWK;
+  const int KC = taps * C;
+  // per thread: two (pixel row, 8-column group) chunks of each tile
+  int zr[2], zc[2], xdy[2], xdx[2], xcol[2];
+  bool zok[2], xok[2];
+#pragma unroll
+  for (int it = 0; it < 2; it++) {
+    const int ch = tid + it * 128;
+    zr[it] = ch >> 3;
+    zc[it] = (ch & 7) * 8;
+    zok[it] = m0 + zc[it] < Cout;
+    const int k = n0 + zc[it];
+    xok[it] = k < KC;
+    const int r = xok[it] ? k / C : 0;
+    xdy[it] = taps == 9 ? r / 3 - 1 : 0;
+    xdx[it] = taps == 9 ? r % 3 - 1 : 0;
+    xcol[it] = k - r * C;
+  }
+  auto load = [&](int stage, int p0) {
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+      const int p = p0 + zr[it];
+      const bool pin = p < pend;
+      const bool zk = pin && zok[it];
+      cp_async16(&Zs[stage][zr[it]][zc[it]], zk ? dZ + (size_t)p * Cout + m0 + zc[it] : dZ, zk);
+      bool xk = pin && xok[it];
+      const bf16 *src = X;
+      if (xk) {
+        const int x = p % W, y = (p / W) % H;
+        const int yy = y + xdy[it], xx = x + xdx[it];
+        xk = yy >= 0 && yy < H && xx >= 0 && xx < W;
+        if (xk) src = X + (size_t)(p + xdy[it] * W + xdx[it]) * C + xcol[it];
+      }
+      cp_async16(&Xs[stage][zr[it]][zc[it]], src, xk);
+    }
+  };
   float acc[2][4][4];
 #pragma unroll
   for (int i = 0; i < 2; i++)
@@ -75,48 +268,41 @@ __global__ void __launch_bounds__(256) k_gemm(const GemmArgs g) {
     for (int j = 0; j < 4; j++)
 #pragma unroll
       for (int r = 0; r < 4; r++) acc[i][j][r] = 0.f;
-  const int gq = lane >> 2, tq = lane & 3;
-  for (int k0 = kbeg; k0 < kend; k0 += GBK) {
-    // A tile: 128 rows x 32 k = 512 chunks of 8 bf16
 #pragma unroll
-    for (int it = 0; it < 2; it++) {
-      const int ch = tid + it * 256, r = ch >> 2, c8 = (ch & 3) * 8;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (m0 + r < g.M) v = *(const uint4 *)(g.A + (size_t)(m0 + r) * g.K + k0 + c8);
-      *(uint4 *)&As[r][c8] = v;
-    }
-    {
-      const int r = tid >> 2, c8 = (tid & 3) * 8;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (n0 + r < g.N) v = *(const uint4 *)(g.Bt + (size_t)(n0 + r) * g.K + k0 + c8);
-      *(uint4 *)&Bs[r][c8] = v;
-    }
+  for (int st = 0; st < GSTAGES - 1; st++) {
+    if (st < nk) load(st, pbeg + st * DWK);
+    cp_async_commit();
+  }
+  const int l8 = lane & 7, lb3 = (lane >> 3) & 1, lb4 = (lane >> 4) & 1;
+  for (int kt = 0; kt < nk; kt++) {
+    cp_async_wait<GSTAGES - 2>();
     __syncthreads();
+    if (kt + GSTAGES - 1 < nk) load((kt + GSTAGES - 1) % GSTAGES, pbeg + (kt + GSTAGES - 1) * DWK);
+    cp_async_commit();
+    const int stg = kt % GSTAGES;
 #pragma unroll
-    for (int kk = 0; kk < GBK; kk += 16) {
+    for (int kk = 0; kk < DWK; kk += 16) {
       uint32_t af[2][4], bfr[4][2];
 #pragma unroll
-      for (int i = 0; i < 2; i++) {
-        const int r = wm * 32 + i * 16 + gq;
-        af[i][0] = *(const uint32_t *)&As[r][kk + 2 * tq];
-        af[i][1] = *(const uint32_t *)&As[r + 8][kk + 2 * tq];
-        af[i][2] = *(const uint32_t *)&As[r][kk + 2 * tq + 8];
-        af[i][3] = *(const uint32_t *)&As[r + 8][kk + 2 * tq + 8];
-      }
+      for (int i = 0; i < 2; i++)  // A[m][k] = Zs[k][m]: matrices (m, k), (m+8, k), (m, k+8), (m+8, k+8)
+        ldsm_x4_t(af[i], &Zs[stg][kk + l8 + lb4 * 8][wm * 32 + i * 16 + lb3 * 8]);
 #pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const int c = wn * 32 + j * 8 + gq;
-        bfr[j][0] = *(const uint32_t *)&Bs[c][kk + 2 * tq];
-        bfr[j][1] = *(const uint32_t *)&Bs[c][kk + 2 * tq + 8];
+      for (int j = 0; j < 4; j += 2) {  // B[k][n] = Xs[k][n]: (k, n), (k+8, n), (k, n+8), (k+8, n+8)
+        uint32_t r[4];
+        ldsm_x4_t(r, &Xs[stg][kk + l8 + lb3 * 8][wn * 32 + j * 8 + lb4 * 8]);
+        bfr[j][0] = r[0];
+        bfr[j][1] = r[1];
+        bfr[j + 1][0] = r[2];
+        bfr[j + 1][1] = r[3];
       }
 #pragma unroll
       for (int i = 0; i < 2; i++)
 #pragma unroll
         for (int j = 0; j < 4; j++) mma_bf16(acc[i][j], af[i], bfr[j]);
     }
-    __syncthreads();
   }
-  // epilogue: c0,c1 at (row gq, cols 2tq, 2tq+1), c2,c3 at row gq+8
+  cp_async_wait<0>();
+  const int gq = lane >> 2, tq = lane & 3;
 #pragma unroll
   for (int i = 0; i < 2; i++)
 #pragma unroll
@@ -124,19 +310,49 @@ __global__ void __launch_bounds__(256) k_gemm(const GemmArgs g) {
 #pragma unroll
       for (int h = 0; h < 2; h++) {
         const int row = m0 + wm * 32 + i * 16 + gq + h * 8;
-        if (row >= g.M) continue;
+        if (row >= Cout) continue;
 #pragma unroll
         for (int e = 0; e < 2; e++) {
           const int col = n0 + wn * 32 + j * 8 + 2 * tq + e;
-          if (col >= g.N) continue;
-          float v = acc[i][j][h * 2 + e];
-          const size_t o = (size_t)row * g.N + col;
-          if (EPI == EPI_BIAS_RELU_BF16) g.out_bf16[o] = __float2bfloat16_rn(fmaxf(v + g.bias[col], 0.f));
-          else if (EPI == EPI_BIAS_BF16) g.out_bf16[o] = __float2bfloat16_rn(v + g.bias[col]);
-          else if (EPI == EPI_BF16) g.out_bf16[o] = __float2bfloat16_rn(v);
-          else atomicAdd(g.out_f32 + o, v);
+          if (col < KC) atomicAdd(dW + (size_t)row * ldw + col, acc[i][j][h * 2 + e]);
         }
       }
+}
+
+// dZ = dY * (Y > 0) for ReLU layers (in place, when RELU) and db[c] += sum
+// over pixels of dZ[p][c]; C a multiple of 8, each thread 8 channels of a pixel.
+template <bool RELU>
+__global__ void __launch_bounds__(256) k_relu_bias_back(bf16 *dY, const bf16 *Y, float *db, size_t P, int C) {
+  __shared__ float sh[256][9];
+  const int G = C / 8;              // channel groups of a pixel
+  const int per = blockDim.x / G;   // pixels per block pass
+  const int grp = threadIdx.x % G, pl = threadIdx.x / G;
+  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (pl < per) {
+    for (size_t p = (size_t)blockIdx.x * per + pl; p < P; p += (size_t)gridDim.x * per) {
+      uint4 d = *(const uint4 *)(dY + p * C + grp * 8);
+      bf16 *dv = (bf16 *)&d;
+      if (RELU) {
+        const uint4 y = *(const uint4 *)(Y + p * C + grp * 8);
+        const bf16 *yv = (const bf16 *)&y;
+#pragma unroll
+        for (int e = 0; e < 8; e++)
+          if (!(__bfloat162float(yv[e]) > 0.f)) dv[e] = __float2bfloat16_rn(0.f);
+        *(uint4 *)(dY + p * C + grp * 8) = d;
+      }
+#pragma unroll
+      for (int e = 0; e < 8; e++) acc[e] += __bfloat162float(dv[e]);
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < 8; e++) sh[threadIdx.x][e] = acc[e];
+  __syncthreads();
+  if (threadIdx.x < C) {
+    const int gi = threadIdx.x / 8, e = threadIdx.x % 8;
+    float s = 0.f;
+    for (int t = gi; t < per * G; t += G) s += sh[t][e];
+    atomicAdd(db + threadIdx.x, s);
+  }
 }
 
 // im2col of a taps = 9 (3x3, pad 1) or taps = 1 convolution:
@@ -186,13 +402,20 @@ __global__ void k_relu_back(bf16 *dY, const bf16 *Y, size_t n) {
     if (!(bf(Y[i]) > 0.f)) dY[i] = __float2bfloat16_rn(0.f);
 }
 
-// db[c] += sum over pixels of dZ[p][c].
+// db[c] += sum over pixels of dZ[p][c] for C <= 8 channels (the output
+// layer): per-thread sums over a pixel stride, then a warp reduction.
 __global__ void k_bias_grad(const bf16 *dZ, float *db, size_t P, int C) {
-  const int c = blockIdx.y * blockDim.x + threadIdx.x;
-  if (c >= C) return;
-  float s = 0.f;
-  for (size_t p = blockIdx.x; p < P; p += gridDim.x) s += bf(dZ[p * C + c]);
-  atomicAdd(db + c, s);
+  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < P; p += (size_t)gridDim.x * blockDim.x)
+#pragma unroll
+    for (int c = 0; c < 8; c++)
+      if (c < C) acc[c] += bf(dZ[p * C + c]);
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    float v = acc[c];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && c < C) atomicAdd(db + c, v);
+  }
 }
 
 // 2x2 average pool (NHWC) and its gradient.
@@ -264,12 +487,23 @@ __global__ void k_bf16_to_f32(const bf16 *x, float *y, size_t n) {
     y[i] = __bfloat162float(x[i]);
 }
 
+// Sum of the loss mask (FP64, one atomic per warp).
+__global__ void k_mask_sum(const float *mask, size_t P, double *out) {
+  double s = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < P; i += (size_t)gridDim.x * blockDim.x)
+    s += mask[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
 // Masked mean-squared error: loss = sum m (y - t)^2 / (sum m * C); dY in BF16.
+// msum = sum of the mask (k_mask_sum).
 __global__ void k_mse(const bf16 *Y, const float *T, const float *mask, bf16 *dY, size_t P, int C,
-                      double inv_count, double *loss) {
+                      const double *msum, double *loss) {
+  const double inv_count = *msum > 0 ? 1.0 / (*msum * C) : 0.0;
   double s = 0.0;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < P * C; i += (size_t)gridDim.x * blockDim.x) {
-    const float m = mask ? mask[i / C] : 1.f;
+    const float m = mask[i / C];
     const float d = bf(Y[i]) - T[i];
     s += (double)m * d * d;
     dY[i] = __float2bfloat16_rn((float)(2.0 * inv_count) * m * d);
@@ -374,10 +608,23 @@ void sfree(lbm_sg *s) {
   s->stream = nullptr;
 }
 
+template <int EPI, bool GATHER>
+const void *gemm_fn(int bn) {
+  return bn == 32 ? (const void *)k_gemm<EPI, GATHER, 32> : (const void *)k_gemm<EPI, GATHER, 64>;
+}
+
+// C = A x Bt^T with A explicit ([M][K]) or, when X is given, the implicit
+// im2col of X ([M pixels][H][W][C], K = taps * C).
 lbm_status gemm(lbm_sg *s, int epi, const bf16 *A, const bf16 *Bt, int M, int N, int K,
-                const float *bias, bf16 *ob, float *of, int splits) {
+                const float *bias, bf16 *ob, float *of, int splits, const bf16 *X = nullptr,
+                int H = 0, int W = 0, int C = 0, int taps = 0) {
   GemmArgs g;
   g.A = A;
+  g.X = X;
+  g.H = H;
+  g.W = W;
+  g.C = C;
+  g.taps = taps;
   g.Bt = Bt;
   g.M = M;
   g.N = N;
@@ -386,12 +633,25 @@ lbm_status gemm(lbm_sg *s, int epi, const bf16 *A, const bf16 *Bt, int M, int N,
   g.bias = bias;
   g.out_bf16 = ob;
   g.out_f32 = of;
-  dim3 grid((M + GBM - 1) / GBM, (N + GBN - 1) / GBN, (K + g.kchunk - 1) / g.kchunk);
+  const int bn = N <= 32 ? 32 : 64;
+  dim3 grid((M + GBM - 1) / GBM, (N + bn - 1) / bn, (K + g.kchunk - 1) / g.kchunk);
   void *args[] = {&g};
-  const void *fn = epi == EPI_BIAS_RELU_BF16 ? (const void *)k_gemm<EPI_BIAS_RELU_BF16>
-                 : epi == EPI_BIAS_BF16       ? (const void *)k_gemm<EPI_BIAS_BF16>
-                 : epi == EPI_BF16            ? (const void *)k_gemm<EPI_BF16>
-                                              : (const void *)k_gemm<EPI_ATOMIC_F32>;
+  const bool ga = X != nullptr;
+  const void *fn = nullptr;
+  switch (epi) {
+    case EPI_BIAS_RELU_BF16:
+      fn = ga ? gemm_fn<EPI_BIAS_RELU_BF16, true>(bn) : gemm_fn<EPI_BIAS_RELU_BF16, false>(bn);
+      break;
+    case EPI_BIAS_BF16:
+      fn = ga ? gemm_fn<EPI_BIAS_BF16, true>(bn) : gemm_fn<EPI_BIAS_BF16, false>(bn);
+      break;
+    case EPI_BF16:
+      fn = ga ? gemm_fn<EPI_BF16, true>(bn) : gemm_fn<EPI_BF16, false>(bn);
+      break;
+    default:
+      fn = gemm_fn<EPI_ATOMIC_F32, false>(bn);
+      break;
+  }
   cudaError_t e = cudaLaunchKernel(fn, grid, dim3(256), args, 0, s->stream);
   if (e != cudaSuccess) return fail(LBM_CUDA, std::string("surrogate gemm: ") + cudaGetErrorString(e));
   return LBM_OK;
@@ -402,15 +662,21 @@ void refresh_weights(lbm_sg *s) {
     k_weights<<<64, 256, 0, s->stream>>>(s->w + c.woff, c.Wt, c.Wd, c.cout, c.cin, c.taps, c.Kp, c.Kpd);
 }
 
+// The implicit im2col needs whole K tiles inside one tap.
+bool gather_ok(int C) { return C % GBK == 0; }
+
 lbm_status conv_fwd(lbm_sg *s, int li, int xi, int yi, int B) {
   const Conv &c = s->conv[li];
   const Act &X = s->act[xi];
   Act &Y = s->act[yi];
   const int M = B * X.h * X.w;
+  const int epi = c.relu ? EPI_BIAS_RELU_BF16 : EPI_BIAS_BF16;
+  if (gather_ok(X.c))
+    return gemm(s, epi, nullptr, c.Wt, M, c.cout, c.Kp, s->w + c.boff, Y.x, nullptr, 1, X.x, X.h,
+                X.w, X.c, c.taps);
   const size_t n = (size_t)M * c.Kp;
   k_im2col<<<grid_for(n), 256, 0, s->stream>>>(X.x, s->col, B, X.h, X.w, X.c, c.taps, c.Kp);
-  return gemm(s, c.relu ? EPI_BIAS_RELU_BF16 : EPI_BIAS_BF16, s->col, c.Wt, M, c.cout, c.Kp,
-              s->w + c.boff, Y.x, nullptr, 1);
+  return gemm(s, epi, s->col, c.Wt, M, c.cout, c.Kp, s->w + c.boff, Y.x, nullptr, 1);
 }
 
 // Given Y.dx (gradient of the layer output), accumulates the weight and bias
@@ -421,15 +687,38 @@ lbm_status conv_bwd(lbm_sg *s, int li, int xi, int yi, int B, bool need_dx) {
   Act &Y = s->act[yi];
   const int M = B * X.h * X.w, Mp = rup(M, GBK);
   const size_t ny = (size_t)M * c.cout;
-  if (c.relu) k_relu_back<<<grid_for(ny), 256, 0, s->stream>>>(Y.dx, Y.x, ny);
-  k_bias_grad<<<dim3(256, (c.cout + 127) / 128), 128, 0, s->stream>>>(Y.dx, s->g + c.boff, (size_t)M, c.cout);
-  k_im2col<<<grid_for((size_t)M * c.Kp), 256, 0, s->stream>>>(X.x, s->col, B, X.h, X.w, X.c, c.taps, c.Kp);
-  k_transpose<<<dim3((c.Kp + 31) / 32, Mp / 32), dim3(32, 8), 0, s->stream>>>(s->col, s->colT, M, c.Kp, Mp);
-  k_transpose<<<dim3((c.cout + 31) / 32, Mp / 32), dim3(32, 8), 0, s->stream>>>(Y.dx, s->dzT, M, c.cout, Mp);
-  const int splits = std::max(1, std::min(256, Mp / 4096));
-  lbm_status st = gemm(s, EPI_ATOMIC_F32, s->dzT, s->colT, c.cout, c.Kp, Mp, nullptr, nullptr,
-                       s->g + c.woff, splits);
+  if (c.cout % 8 == 0) {
+    const int G = c.cout / 8, per = 256 / G;
+    const int grid = (int)std::min<size_t>(((size_t)M + per - 1) / per, 152 * 8);
+    if (c.relu)
+      k_relu_bias_back<true><<<grid, 256, 0, s->stream>>>(Y.dx, Y.x, s->g + c.boff, (size_t)M, c.cout);
+    else
+      k_relu_bias_back<false><<<grid, 256, 0, s->stream>>>(Y.dx, Y.x, s->g + c.boff, (size_t)M, c.cout);
+  } else {
+    if (c.cout > 8) return fail(LBM_INVALID, "surrogate: output channels must be <= 8 or a multiple of 8");
+    if (c.relu) k_relu_back<<<grid_for(ny), 256, 0, s->stream>>>(Y.dx, Y.x, ny);
+    k_bias_grad<<<grid_for((size_t)M), 256, 0, s->stream>>>(Y.dx, s->g + c.boff, (size_t)M, c.cout);
+  }
+  lbm_status st = LBM_OK;
+  if (X.c % 8 == 0 && c.cout % 8 == 0 && c.Kp == c.taps * X.c) {
+    const int bm = (c.cout + DWM - 1) / DWM, bn = (c.Kp + DWN - 1) / DWN;
+    const int splits = std::max(1, std::min(M / (DWK * 8), (152 * 6) / (bm * bn) + 1));
+    const int pchunk = rup((M + splits - 1) / splits, DWK);
+    dim3 grid(bm, bn, (M + pchunk - 1) / pchunk);
+    k_gemm_dw<<<grid, 128, 0, s->stream>>>(Y.dx, X.x, s->g + c.woff, M, X.h, X.w, X.c, c.taps,
+                                           c.cout, c.Kp, pchunk);
+  } else {
+    k_im2col<<<grid_for((size_t)M * c.Kp), 256, 0, s->stream>>>(X.x, s->col, B, X.h, X.w, X.c, c.taps, c.Kp);
+    k_transpose<<<dim3((c.Kp + 31) / 32, Mp / 32), dim3(32, 8), 0, s->stream>>>(s->col, s->colT, M, c.Kp, Mp);
+    k_transpose<<<dim3((c.cout + 31) / 32, Mp / 32), dim3(32, 8), 0, s->stream>>>(Y.dx, s->dzT, M, c.cout, Mp);
+    const int splits = std::max(1, std::min(256, Mp / 4096));
+    st = gemm(s, EPI_ATOMIC_F32, s->dzT, s->colT, c.cout, c.Kp, Mp, nullptr, nullptr, s->g + c.woff,
+              splits);
+  }
   if (st != LBM_OK || !need_dx) return st;
+  if (gather_ok(c.cout))
+    return gemm(s, EPI_BF16, nullptr, c.Wd, M, c.cin, c.Kpd, nullptr, X.dx, nullptr, 1, Y.dx, X.h,
+                X.w, c.cout, c.taps);
   k_im2col<<<grid_for((size_t)M * c.Kpd), 256, 0, s->stream>>>(Y.dx, s->col, B, X.h, X.w, c.cout, c.taps, c.Kpd);
   return gemm(s, EPI_BF16, s->col, c.Wd, M, c.cin, c.Kpd, nullptr, X.dx, nullptr, 1);
 }
@@ -513,19 +802,10 @@ lbm_status loss_grads(lbm_sg *s, int B, double *loss_out) {
   lbm_status st = forward(s, B);
   if (st != LBM_OK) return st;
   cudaMemsetAsync(s->g, 0, s->nparam * sizeof(float), s->stream);
-  cudaMemsetAsync(s->loss, 0, sizeof(double), s->stream);
-  // mean over masked cells and output channels
-  std::vector<float> hm;
-  double count = 0;
-  {
-    hm.resize(P);
-    cudaMemcpyAsync(hm.data(), s->msk, P * sizeof(float), cudaMemcpyDeviceToHost, s->stream);
-    cudaStreamSynchronize(s->stream);
-    for (float x : hm) count += x;
-  }
-  const double inv = count > 0 ? 1.0 / (count * c.out_channels) : 0.0;
+  cudaMemsetAsync(s->loss, 0, 2 * sizeof(double), s->stream);  // loss, mask sum
+  k_mask_sum<<<grid_for(P), 256, 0, s->stream>>>(s->msk, P, s->loss + 1);
   k_mse<<<grid_for(P * c.out_channels), 256, 0, s->stream>>>(s->act[A_OUT].x, s->tgt, s->msk, s->act[A_OUT].dx, P,
-                                                           c.out_channels, inv, s->loss);
+                                                           c.out_channels, s->loss + 1, s->loss);
   if ((st = backward(s, B)) != LBM_OK) return st;
   double h = 0;
   cudaMemcpyAsync(&h, s->loss, sizeof h, cudaMemcpyDeviceToHost, s->stream);
@@ -553,8 +833,10 @@ lbm_status lbm_sg_create(const lbm_sg_config *cfg, lbm_sg **out) {
   *out = nullptr;
   const int H = cfg->height, W = cfg->width, b = cfg->base;
   if (H < 16 || W < 16 || H % 8 || W % 8 || b < 8 || b % 8 || cfg->in_channels < 1 ||
-      cfg->out_channels < 1 || cfg->out_channels > 64 || cfg->max_batch < 1)
-    return fail(LBM_INVALID, "surrogate: H, W multiples of 8 (>= 16), base multiple of 8");
+      cfg->out_channels < 1 || cfg->out_channels > 64 || (cfg->out_channels > 8 && cfg->out_channels % 8) ||
+      cfg->max_batch < 1)
+    return fail(LBM_INVALID,
+                "surrogate: H, W multiples of 8 (>= 16), base multiple of 8, outputs <= 8 or a multiple of 8");
   lbm_sg *s = new lbm_sg();
   s->cfg = *cfg;
   auto bail = [&](lbm_status st) {
@@ -635,7 +917,7 @@ lbm_status lbm_sg_create(const lbm_sg_config *cfg, lbm_sg **out) {
   if ((st = salloc(s, &s->col, max_col)) || (st = salloc(s, &s->colT, max_colT)) ||
       (st = salloc(s, &s->dzT, max_dz)) || (st = salloc(s, &s->tgt, P * co)) ||
       (st = salloc(s, &s->msk, P)) || (st = salloc(s, &s->xin, P * ci)) ||
-      (st = salloc(s, &s->yout, P * co)) || (st = salloc(s, &s->loss, 1)))
+      (st = salloc(s, &s->yout, P * co)) || (st = salloc(s, &s->loss, 2)))
     return bail(st);
   refresh_weights(s);
   if (cudaStreamSynchronize(s->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess)
@@ -757,6 +1039,12 @@ lbm_status lbm_sg_train(lbm_sg *s, int32_t batch, const int32_t *order, int32_t 
   }
   if (cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(LBM_CUDA, "surrogate training failed");
   if (mean_loss) *mean_loss = steps ? total / steps : 0.0;
+  return LBM_OK;
+}
+
+lbm_status lbm_sg_set_lr(lbm_sg *s, float lr) {
+  if (!s || !(lr > 0.f)) return fail(LBM_INVALID, "bad learning rate");
+  s->cfg.lr = lr;
   return LBM_OK;
 }
 

@@ -8,11 +8,11 @@ from oracle import sg_oracle as SO
 CIN, COUT, BASE, H = 4, 3, 8, 16
 
 
-def sample(seed=1, B=2):
+def sample(seed=1, B=2, h=H, cin=CIN):
     rng = np.random.default_rng(seed)
-    x = rng.normal(size=(B, H, H, CIN))
-    t = rng.normal(size=(B, H, H, COUT)) * 0.5
-    m = (rng.random((B, H, H)) > 0.2).astype(np.float64)
+    x = rng.normal(size=(B, h, h, cin))
+    t = rng.normal(size=(B, h, h, COUT)) * 0.5
+    m = (rng.random((B, h, h)) > 0.2).astype(np.float64)
     return x, t, m
 
 
@@ -72,21 +72,25 @@ def test_bf16_rounding_helper():
 
 
 @pytest.mark.gpu
-def test_gpu_gradients_match_oracle():
+@pytest.mark.parametrize("cin,base,h", [(CIN, BASE, H), (7, 32, 32)])
+def test_gpu_gradients_match_oracle(cin, base, h):
+    """base 8: explicit im2col products for most layers; base 32 (the warm-start
+    network's width): implicit-im2col forward/input-gradient products and the
+    pixel-split weight-gradient kernel for every layer with 32k channels."""
     import parallellbmcranfield_gb300 as G
 
-    s = G.Surrogate(height=H, width=H, in_channels=CIN, out_channels=COUT, base=BASE, max_batch=2,
+    s = G.Surrogate(height=h, width=h, in_channels=cin, out_channels=COUT, base=base, max_batch=2,
                     seed=5)
     params = s.params().astype(np.float64)
-    x, t, m = sample(seed=2)
+    x, t, m = sample(seed=2, h=h, cin=cin)
     loss, g = s.loss_grads(x, t, m)
-    oloss, oy, og = SO.Net(params, CIN, COUT, BASE, bf16=True).loss_grads(x, t, m)
+    oloss, oy, og = SO.Net(params, cin, COUT, base, bf16=True).loss_grads(x, t, m)
     y = s.forward(x)
     assert np.abs(y - oy).max() <= 2e-2 * np.abs(oy).max()
     assert abs(loss - oloss) <= 2e-2 * oloss
     # per-layer relative L2 error of the weight gradients
     off = 0
-    for ci, co, taps, relu in SO.layer_table(CIN, COUT, BASE):
+    for ci, co, taps, relu in SO.layer_table(cin, COUT, base):
         n = co * SO.rup(taps * ci, 32) + co
         a, b = g[off:off + n], og[off:off + n]
         off += n
@@ -119,9 +123,65 @@ def test_pipeline_small(tmp_path):
     """Data generation -> training -> warm/cold comparison end to end, tiny."""
     from parallellbmcranfield_gb300 import surrogate as S
 
-    rep = S.main(["--cavities", "3", "--channels", "3", "--max-steps", "3000",
-                  "--check-every", "500", "--epochs", "2", "--batch", "2", "--eval", "2",
-                  "--out", str(tmp_path / "r.json")])
-    assert rep["cases"] == 6
+    rep = S.main(["--cavities", "3", "--channels", "3", "--max-steps", "30000",
+                  "--check-every", "100", "--gen-tol", "2e-4", "--tol", "2e-4", "--epochs", "2",
+                  "--batch", "2", "--eval", "2", "--out", str(tmp_path / "r.json")])
+    assert rep["cases"] == 6 and rep["steady"] == 6, rep
     assert np.isfinite(rep["training"]["loss_last"])
-    assert rep["warm_vs_cold"]["cases"] == 1  # 6 cases: 5 train, 1 test
+    assert rep["training"]["cases"] == 5  # 6 cases: 5 train, 1 test
+    ev = rep["warm_vs_cold"]
+    assert ev["cases"] == 1 and ev["converged_cold"] == 1 and ev["converged_warm"] == 1
+
+
+def test_pipeline_host_logic():
+    """Case draws, input maps and the prediction -> initial-field mapping (CPU)."""
+    from parallellbmcranfield_gb300 import surrogate as S
+
+    cases = S.make_cases(4, 4, seed=3)
+    assert [c["kind"] for c in cases] == ["cavity"] * 4 + ["channel"] * 4
+    for c in cases:
+        assert 0.05 <= c["U"] <= 0.1
+        assert c["params"]["viscosity"] > 0
+        if c["kind"] == "cavity":
+            assert 100 <= c["re"] <= 5000
+            assert abs(c["params"]["viscosity"] - c["U"] * S.SIDE / c["re"]) < 1e-12
+        else:
+            assert 0.05 <= c["params"]["viscosity"] <= 0.4
+            assert 1 <= len(c["spec"][3]) <= 3
+    for c in (cases[0], cases[4]):
+        mesh = S.build_mesh(c["spec"])
+        n, m = mesh.shape
+        x, mask = S.features(c, mesh)
+        assert x.shape == (S.GRID, S.GRID, S.IN_CH) and mask.shape == (S.GRID, S.GRID)
+        assert set(np.unique(mask)) <= {0.0, 1.0}
+        # distance map: zero on solid cells, >= 1/32 on fluid cells
+        assert (x[..., 6][mask == 0] == 0).all() and (x[..., 6][mask == 1] >= 1 / 32 - 1e-7).all()
+        assert x[0, 5, 4] == np.float32(5 / 256) and x[7, 0, 5] == np.float32(7 / 256)
+        # targets -> prediction -> fields round trip on fluid cells
+        rng = np.random.default_rng(0)
+        f = {k: rng.normal(size=n * m) * 0.01 for k in ("rho", "u", "v")}
+        f["rho"] = 1.0 + f["rho"] * c["U"] ** 2  # (rho - 1) / U^2 within the clip
+        y = S.targets(c, f, n, m)
+        rho, u, v = S.fields_from_prediction(c, y, n, m, mask)
+        fl = np.zeros((m, n), bool)
+        fl[:S.GRID, :S.GRID] = mask > 0
+        assert np.allclose(u.reshape(m, n)[fl], f["u"].reshape(m, n)[fl], rtol=1e-5, atol=1e-9)
+        assert np.allclose(v.reshape(m, n)[fl], f["v"].reshape(m, n)[fl], rtol=1e-5, atol=1e-9)
+        r = rho.reshape(m, n)[fl]
+        if c["kind"] == "cavity":  # closed box: mean density shifted to the cold start's 1
+            assert abs(r.mean() - 1.0) < 1e-12
+        else:
+            assert np.allclose(r, f["rho"].reshape(m, n)[fl], rtol=0, atol=1e-6)
+        assert (u.reshape(m, n)[~fl] == 0).all() and (rho.reshape(m, n)[~fl] == 1).all()
+    # mirrored channel: twice is the identity, v changes sign, position maps stay
+    rng = np.random.default_rng(1)
+    x = rng.normal(size=(S.GRID, S.GRID, S.IN_CH)).astype(np.float32)
+    y = rng.normal(size=(S.GRID, S.GRID, 3)).astype(np.float32)
+    m = (rng.random((S.GRID, S.GRID)) > 0.5).astype(np.float32)
+    xf, yf, mf = S.flip_channel(x, y, m)
+    assert (xf[..., 4:6] == x[..., 4:6]).all() and (xf[3, :, 0] == x[S.GRID - 4, :, 0]).all()
+    assert (yf[3, :, 2] == -y[S.GRID - 4, :, 2]).all() and (mf[3] == m[S.GRID - 4]).all()
+    x2, y2, m2 = S.flip_channel(xf, yf, mf)
+    assert (x2 == x).all() and (y2 == y).all() and (m2 == m).all()
+    assert S.cosine_lr(1e-3, 2e-5, 0, 10) == 1e-3
+    assert abs(S.cosine_lr(1e-3, 2e-5, 10, 10) - 2e-5) < 1e-12

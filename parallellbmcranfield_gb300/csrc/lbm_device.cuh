@@ -1065,21 +1065,87 @@ __global__ void __launch_bounds__(BX) k_step_vec(const __grid_constant__ StepArg
 // half-word beyond the warp themselves, also up front).  Warps that touch a
 // node with boundary work run the per-node path instead, so the shuffles
 // always involve the whole warp.  Only for 2-byte storage.
+// Packed FP32 pairs: the two nodes of a 32-bit word go through the bulk
+// collision together with the paired FP32 instructions of sm_100-class GPUs
+// (one FFMA2/FADD2/FMUL2 does the work of two scalar ones).
+__device__ __forceinline__ float2 bc2(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 add2(float2 x, float2 y) { return __fadd2_rn(x, y); }
+__device__ __forceinline__ float2 sub2(float2 x, float2 y) { return __ffma2_rn(y, bc2(-1.f), x); }
+__device__ __forceinline__ float2 mul2(float2 x, float2 y) { return __fmul2_rn(x, y); }
+__device__ __forceinline__ float2 fma2(float2 x, float2 y, float2 z) { return __ffma2_rn(x, y, z); }
+
+// Deviations of a word's two nodes (bulk form of a shifted 16-bit storage).
 template <class ST>
-__device__ __forceinline__ void unpack2(uint32_t w, int k, const StepArgs &a, float &lo, float &hi) {
-  using T = typename ST::T;
-  T t[2];
-  memcpy(t, &w, 4);
-  lo = ST::cvt_dev(t[0], k, a);
-  hi = ST::cvt_dev(t[1], k, a);
+__device__ __forceinline__ float2 unpack2v(uint32_t w, int k, const StepArgs &a) {
+  float2 f;
+  if constexpr (std::is_same<typename ST::T, __half>::value) {
+    __half2 h;
+    memcpy(&h, &w, 4);
+    f = __half22float2(h);
+  } else {
+    __nv_bfloat162 h;
+    memcpy(&h, &w, 4);
+    f = __bfloat1622float2(h);
+  }
+  return mul2(f, bc2(a.inv_scale[k]));
 }
 template <class ST>
-__device__ __forceinline__ uint32_t pack2(float lo, float hi, int k, const StepArgs &a) {
-  using T = typename ST::T;
-  T t[2] = {ST::pack_dev(lo, k, a), ST::pack_dev(hi, k, a)};
+__device__ __forceinline__ uint32_t pack2v(float2 d, int k, const StepArgs &a) {
+  const float2 sc = mul2(d, bc2(a.scale[k]));
   uint32_t w;
-  memcpy(&w, t, 4);
+  if constexpr (std::is_same<typename ST::T, __half>::value) {
+    const __half2 h = __float22half2_rn(sc);
+    memcpy(&w, &h, 4);
+  } else {
+    const __nv_bfloat162 h = __float22bfloat162_rn(sc);
+    memcpy(&w, &h, 4);
+  }
   return w;
+}
+
+// MRT bulk collision of two nodes in deviation form: the operator of
+// collide_bulk_dev (model 3) with its constants folded (1/36 and the 1.4 /
+// 1.2 rates into the moment differences) so that each population takes one
+// or two paired operations.  g1, g2: non-equilibrium energy moments, e4, e6:
+// heat-flux moments, h7, h8: stress moments.
+__device__ __forceinline__ void collide_mrt_pair(const float2 F[9], const StepArgs &a, float2 M[9]) {
+  const float2 a13 = add2(F[1], F[3]), a24 = add2(F[2], F[4]);
+  const float2 a14 = add2(a13, a24);
+  const float2 p57 = add2(F[5], F[7]), p68 = add2(F[6], F[8]);
+  const float2 a58 = add2(p57, p68);
+  const float2 rt = add2(add2(F[0], a14), a58);
+  const float2 rho = add2(bc2((float)a.rho0), rt);
+  const float2 m1 = fma2(bc2(-4.f), F[0], sub2(mul2(bc2(2.f), a58), a14));
+  const float2 m2 = fma2(bc2(-2.f), a14, fma2(bc2(4.f), F[0], a58));
+  const float2 d13 = sub2(F[1], F[3]), d24 = sub2(F[2], F[4]);
+  const float2 e57 = sub2(F[5], F[7]), e86 = sub2(F[8], F[6]);
+  const float2 x58 = add2(e57, e86), y58 = sub2(e57, e86);
+  const float2 jx = add2(d13, x58), jy = add2(d24, y58);
+  const float2 m4 = fma2(bc2(-2.f), d13, x58), m6 = fma2(bc2(-2.f), d24, y58);
+  const float2 m7 = sub2(a13, a24), m8 = sub2(p57, p68);
+  const float2 ninv = make_float2(__fdividef(-1.f, rho.x), __fdividef(-1.f, rho.y));
+  const float2 jj = fma2(jx, jx, mul2(jy, jy));
+  const float2 g1 = fma2(bc2(-3.f), jj, fma2(bc2(2.f), rt, m1));
+  const float2 g2 = fma2(bc2(3.f), jj, sub2(m2, rt));
+  const float2 e4 = add2(m4, jx), e6 = add2(m6, jy);
+  const float2 h7 = fma2(mul2(sub2(jx, jy), add2(jx, jy)), ninv, m7);
+  const float2 h8 = fma2(mul2(jx, jy), ninv, m8);
+  const float2 om4 = bc2(0.25f * (float)a.omega);
+  const float2 P = mul2(om4, h7), Q = mul2(om4, h8);
+  const float2 A = mul2(bc2(-1.4f / 36.f), fma2(bc2(2.f), g2, g1));  // c * (-d1 - 2 d2)
+  const float2 D = mul2(bc2(1.4f / 36.f), fma2(bc2(2.f), g1, g2));   // c * (2 d1 + d2)
+  const float2 Z = mul2(bc2(5.6f / 36.f), sub2(g2, g1));            // 4 c (d2 - d1)
+  const float2 ApP = add2(A, P), AmP = sub2(A, P), DpQ = add2(D, Q), DmQ = sub2(D, Q);
+  const float2 s46 = add2(e4, e6), t46 = sub2(e4, e6);
+  M[0] = sub2(F[0], Z);
+  M[1] = fma2(bc2(0.2f), e4, sub2(F[1], ApP));
+  M[3] = fma2(bc2(-0.2f), e4, sub2(F[3], ApP));
+  M[2] = fma2(bc2(0.2f), e6, sub2(F[2], AmP));
+  M[4] = fma2(bc2(-0.2f), e6, sub2(F[4], AmP));
+  M[5] = fma2(bc2(-0.1f), s46, sub2(F[5], DpQ));
+  M[7] = fma2(bc2(0.1f), s46, sub2(F[7], DpQ));
+  M[6] = fma2(bc2(0.1f), t46, sub2(F[6], DmQ));
+  M[8] = fma2(bc2(-0.1f), t46, sub2(F[8], DmQ));
 }
 
 // Edge half-word slot of a shifted plane: cx = +1 planes 1, 5, 8 (lane 0) and
@@ -1143,7 +1209,7 @@ __global__ void __launch_bounds__(128) k_step_h2(const __grid_constant__ StepArg
   for (int j = 0; j < NPT; j++) {
     const int y = y0 + j;
     if (!(y >= 1 && y < a.m - 1)) continue;
-    float F0[9], F1[9];
+    float2 F[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) {
       uint32_t word = w[j][k];
@@ -1164,35 +1230,49 @@ __global__ void __launch_bounds__(128) k_step_h2(const __grid_constant__ StepArg
         }
         word = __byte_perm(word, next, 0x5432);  // (x0+1, x0+2)
       }
-      unpack2<ST>(word, k, a, F0[k], F1[k]);
+      F[k] = unpack2v<ST>(word, k, a);
     }
-    float M0[9], M1[9];
-    if (cl[j][0] != CLS_SOLID) collide_bulk_dev<MODEL, ST>(F0, a, M0);
-    else
-      for (int k = 0; k < 9; k++) M0[k] = 0.f;
-    if (cl[j][1] != CLS_SOLID) collide_bulk_dev<MODEL, ST>(F1, a, M1);
-    else
-      for (int k = 0; k < 9; k++) M1[k] = 0.f;
+    float2 M[9];
+    if constexpr (MODEL == 3) {
+      collide_mrt_pair(F, a, M);
+    } else {
+      float F0[9], F1[9], M0[9], M1[9];
+#pragma unroll
+      for (int k = 0; k < 9; k++) {
+        F0[k] = F[k].x;
+        F1[k] = F[k].y;
+      }
+      collide_bulk_dev<MODEL, ST>(F0, a, M0);
+      collide_bulk_dev<MODEL, ST>(F1, a, M1);
+#pragma unroll
+      for (int k = 0; k < 9; k++) M[k] = make_float2(M0[k], M1[k]);
+    }
+    // a solid node of the pair keeps zero deviations
+    if (cl[j][0] == CLS_SOLID)
+#pragma unroll
+      for (int k = 0; k < 9; k++) M[k].x = 0.f;
+    if (cl[j][1] == CLS_SOLID)
+#pragma unroll
+      for (int k = 0; k < 9; k++) M[k].y = 0.f;
     const long long node0 = (long long)y * a.pitch + x0;
 #pragma unroll
     for (int i = 0; i < 2; i++)
       if (PH != PH_AB && cl[j][i] == CLS_BULK_REC) {
         const uint32_t sbi = a.aux[node0 + i];
-        const float *M = i ? M1 : M0;
 #pragma unroll
         for (int k = 0; k < 9; k++)
-          a.sb_dst[(size_t)sbi * 9 + k] = (double)M[k] + wgt<double>(k) * a.rho0;
+          a.sb_dst[(size_t)sbi * 9 + k] = (double)(i ? M[k].y : M[k].x) + wgt<double>(k) * a.rho0;
       }
 #pragma unroll
     for (int k = 0; k < 9; k++) {
       if (PH == PH_AA_A) {
         // neighbour write x + e_k, element-wise for fluid nodes
-        if (cl[j][0] != CLS_SOLID) st_dev<ST>(d + (long long)k * a.plane + node0 + nb(k, a.pitch), k, M0[k], a);
+        if (cl[j][0] != CLS_SOLID) st_dev<ST>(d + (long long)k * a.plane + node0 + nb(k, a.pitch), k, M[k].x, a);
         if (cl[j][1] != CLS_SOLID)
-          st_dev<ST>(d + (long long)k * a.plane + node0 + 1 + nb(k, a.pitch), k, M1[k], a);
+          st_dev<ST>(d + (long long)k * a.plane + node0 + 1 + nb(k, a.pitch), k, M[k].y, a);
       } else {
         const int plane = (PH == PH_AB) ? k : OPP[k];
-        __stcs((unsigned *)(d + (long long)plane * a.plane + node0), pack2<ST>(M0[k], M1[k], k, a));
+        __stcs((unsigned *)(d + (long long)plane * a.plane + node0), pack2v<ST>(M[k], k, a));
       }
     }
   }

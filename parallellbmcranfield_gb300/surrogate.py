@@ -10,12 +10,15 @@ Cases (256 x 256 node grids, MRT, FP32 storage, curved/half-way walls):
     diameter 16-64, parabolic inlet (peak U uniform in [0.05, 0.1]),
     constant-pressure outlet, nu log-uniform in [0.05, 0.4] (Re on the mean
     inlet speed and the largest diameter: about 1-90).
-Network input (7 maps): fluid mask, velocity-boundary cells, log(Re)/log(5000),
-U / 0.1, x / 256, y / 256 and the distance to the nearest solid cell / 32 (the
-last three give every cell its position, which 3x3 convolutions with zero
-padding do not see beyond their receptive field).  Output (3 maps):
-clip((rho - 1) / U^2, -8, 8) / 4, u / U, v / U on fluid cells (the clip keeps
-the pressure peaks at the lid corners from dominating the loss).
+Network input (8 maps): fluid mask, velocity-boundary cells, log(Re)/log(5000),
+U / 0.1, x / 256, y / 256, the distance to the nearest solid cell / 32 (these
+three give every cell its position, which 3x3 convolutions with zero padding do
+not see beyond their receptive field) and a gap-flow estimate g / U (channels:
+the inlet flow rate split over the fluid gaps of each column in proportion to
+gap width cubed, each gap carrying a parabolic profile; cavities: 0).  Output
+(3 maps): clip((rho - 1) / U^2, -8, 8) / 4, (u - g) / U, v / U on fluid cells
+(the clip keeps the pressure peaks at the lid corners from dominating the loss;
+the network corrects the gap-flow estimate rather than rebuilding it).
 
 The training targets are run to a tighter tolerance (gen_tol) than the
 comparison (tol) and serve as the converged reference against which both the
@@ -36,7 +39,7 @@ import parallellbmcranfield_gb300 as G
 
 GRID = 256
 SIDE = GRID - 2
-IN_CH = 7
+IN_CH = 8
 RHO_CLIP, RHO_SCALE = 8.0, 0.25
 
 
@@ -77,6 +80,27 @@ def build_mesh(spec):
     return G.Mesh.channel(spec[1], spec[2], spec[3])
 
 
+def gap_flow(case, fl):
+    """Gap-flow estimate of u / U on a GRID x GRID fluid mask (rows = y)."""
+    g = np.zeros((GRID, GRID), np.float32)
+    if case["kind"] != "channel":
+        return g
+    u_mean = case["params"]["uavg"]
+    q = u_mean * float(fl[:, 1].sum())  # inlet flow rate per unit depth
+    for x in range(GRID):
+        col = fl[:, x] > 0
+        if not col.any():
+            continue
+        edges = np.flatnonzero(np.diff(np.concatenate(([0], col.astype(np.int8), [0]))))
+        starts, ends = edges[0::2], edges[1::2]
+        h = (ends - starts).astype(np.float64)
+        share = q * h ** 3 / (h ** 3).sum()
+        for y0, hh, qq in zip(starts, h, share):
+            s = (np.arange(int(hh)) + 0.5) / hh
+            g[y0:y0 + int(hh), x] = 6.0 * (qq / hh) * s * (1.0 - s) / case["U"]
+    return g
+
+
 def features(case, mesh):
     """Input maps (GRID, GRID, IN_CH) and the fluid mask (GRID, GRID)."""
     from scipy.ndimage import distance_transform_edt
@@ -96,23 +120,27 @@ def features(case, mesh):
     x[..., 4] = (np.arange(GRID, dtype=np.float32) / GRID)[None, :]
     x[..., 5] = (np.arange(GRID, dtype=np.float32) / GRID)[:, None]
     x[..., 6] = distance_transform_edt(fl > 0) / 32.0
+    x[..., 7] = gap_flow(case, fl)
     return x, fl.copy()
 
 
-def targets(case, fields, n, m):
+def targets(case, fields, n, m, x):
+    """Network targets of a steady field; x: the case's input maps (the u
+    target is relative to the gap-flow estimate x[..., 7])."""
     U = case["U"]
     t = np.zeros((GRID, GRID, 3), np.float32)
     rho = (fields["rho"].reshape(m, n)[:GRID, :GRID] - 1.0) / (U * U)
     t[..., 0] = np.clip(rho, -RHO_CLIP, RHO_CLIP) * RHO_SCALE
-    t[..., 1] = fields["u"].reshape(m, n)[:GRID, :GRID] / U
+    t[..., 1] = fields["u"].reshape(m, n)[:GRID, :GRID] / U - x[..., 7]
     t[..., 2] = fields["v"].reshape(m, n)[:GRID, :GRID] / U
     return t
 
 
-def fields_from_prediction(case, y, n, m, mask):
-    """rho, u, v arrays of the case's n*m grid from a network output.  In a
-    closed cavity the mass is conserved, so the predicted density is shifted to
-    the mean the cold start has (1); open channels keep the prediction."""
+def fields_from_prediction(case, y, n, m, mask, x):
+    """rho, u, v arrays of the case's n*m grid from a network output (x: the
+    case's input maps).  In a closed cavity the mass is conserved, so the
+    predicted density is shifted to the mean the cold start has (1); open
+    channels keep the prediction."""
     U = case["U"]
     rho, u, v = np.ones((m, n)), np.zeros((m, n)), np.zeros((m, n))
     fl = mask > 0
@@ -120,7 +148,7 @@ def fields_from_prediction(case, y, n, m, mask):
     if case["kind"] == "cavity":
         r += 1.0 - r.mean()
     rho[:GRID, :GRID][fl] = r
-    u[:GRID, :GRID][fl] = y[..., 1][fl] * U
+    u[:GRID, :GRID][fl] = (y[..., 1][fl] + x[..., 7][fl]) * U
     v[:GRID, :GRID][fl] = y[..., 2][fl] * U
     return rho.ravel(), u.ravel(), v.ravel()
 
@@ -147,7 +175,7 @@ def generate(cases, max_steps, check_every, tol):
         n, m = mesh.shape
         f = b.fields(i)
         X.append(x)
-        Y.append(targets(c, f, n, m))
+        Y.append(targets(c, f, n, m, x))
         M.append(mask)
     b.close()
     return meshes, np.stack(X), np.stack(Y), np.stack(M), r, gen_s
@@ -205,13 +233,13 @@ def masked_mse(net, X, Y, M, idx):
     return float((w * (y - Y[idx]) ** 2).sum() / (w.sum() * 3)), y
 
 
-def velocity_error(case, fields, n, m, y_ref, mask):
+def velocity_error(case, fields, n, m, y_ref, mask, x):
     """Relative L2 error of (u, v) / U against the reference target maps."""
     U = case["U"]
     fl = mask > 0
     u = (fields["u"].reshape(m, n)[:GRID, :GRID] / U)[fl]
     v = (fields["v"].reshape(m, n)[:GRID, :GRID] / U)[fl]
-    ur, vr = y_ref[..., 1][fl], y_ref[..., 2][fl]
+    ur, vr = y_ref[..., 1][fl] + x[..., 7][fl], y_ref[..., 2][fl]
     return float(np.sqrt(((u - ur) ** 2 + (v - vr) ** 2).sum() / (ur ** 2 + vr ** 2).sum()))
 
 
@@ -226,7 +254,7 @@ def evaluate(net, cases, meshes, X, Y, M, idx, max_steps, check_every, tol):
     t0 = time.perf_counter()
     bc, rc = run_batch(sub, sub_m, max_steps, check_every, tol)
     cold_s = time.perf_counter() - t0
-    err_cold = [velocity_error(cases[i], bc.fields(j), *meshes[i].shape, Y[i], M[i])
+    err_cold = [velocity_error(cases[i], bc.fields(j), *meshes[i].shape, Y[i], M[i], X[i])
                 for j, i in enumerate(idx)]
     bc.close()
     t0 = time.perf_counter()
@@ -235,13 +263,13 @@ def evaluate(net, cases, meshes, X, Y, M, idx, max_steps, check_every, tol):
     init, err_pred = [], []
     for j, i in enumerate(idx):
         n, m = meshes[i].shape
-        rho, u, v = fields_from_prediction(cases[i], y[j], n, m, M[i])
+        rho, u, v = fields_from_prediction(cases[i], y[j], n, m, M[i], X[i])
         init.append((rho, u, v))
-        err_pred.append(velocity_error(cases[i], dict(u=u, v=v), n, m, Y[i], M[i]))
+        err_pred.append(velocity_error(cases[i], dict(u=u, v=v), n, m, Y[i], M[i], X[i]))
     t0 = time.perf_counter()
     bw, rw = run_batch(sub, sub_m, max_steps, check_every, tol, init=init)
     warm_s = time.perf_counter() - t0
-    err_warm = [velocity_error(cases[i], bw.fields(j), *meshes[i].shape, Y[i], M[i])
+    err_warm = [velocity_error(cases[i], bw.fields(j), *meshes[i].shape, Y[i], M[i], X[i])
                 for j, i in enumerate(idx)]
     bw.close()
     both = (rc["converged"] == 1) & (rw["converged"] == 1)
@@ -294,7 +322,7 @@ def main(argv=None):
     n_samples = len(Xt)
     net, hist, train_s = train(Xt, Yt, Mt, np.arange(len(Xt)), a.epochs, a.batch, a.lr, a.seed)
     del Xt, Yt, Mt
-    test_mse = masked_mse(net, X, Y, M, te[:64])[0] if len(te) else None
+    test_mse = masked_mse(net, X, Y, M, te)[0] if len(te) else None
     ev = evaluate(net, cases, meshes, X, Y, M, te[: a.eval], a.max_steps, a.check_every, a.tol)
     report = dict(
         cases=len(cases), cavities=a.cavities, channels=a.channels, steady=int(steady.sum()),

@@ -43,11 +43,11 @@ IN_CH = 8
 RHO_CLIP, RHO_SCALE = 8.0, 0.25
 
 
-def make_cases(n_cav, n_ch, seed):
+def make_cases(n_cav, n_ch, seed, cavity_re=(100.0, 5000.0)):
     rng = np.random.default_rng(seed)
     cases = []
     for _ in range(n_cav):
-        re = float(np.exp(rng.uniform(np.log(100), np.log(5000))))
+        re = float(np.exp(rng.uniform(np.log(cavity_re[0]), np.log(cavity_re[1]))))
         U = float(rng.uniform(0.05, 0.1))
         nu = U * SIDE / re
         cases.append(dict(kind="cavity", re=re, U=U, spec=("cavity", SIDE),
@@ -297,6 +297,7 @@ def evaluate(net, cases, meshes, X, Y, M, idx, max_steps, check_every, tol):
 def main(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--cavities", type=int, default=700)
+    p.add_argument("--cavity-re-max", type=float, default=5000.0)
     p.add_argument("--channels", type=int, default=1300)
     p.add_argument("--max-steps", type=int, default=600000)
     p.add_argument("--check-every", type=int, default=100)
@@ -310,7 +311,7 @@ def main(argv=None):
     p.add_argument("--seed", type=int, default=20240601)
     p.add_argument("--out", default=None)
     a = p.parse_args(argv)
-    cases = make_cases(a.cavities, a.channels, a.seed)
+    cases = make_cases(a.cavities, a.channels, a.seed, cavity_re=(100.0, a.cavity_re_max))
     meshes, X, Y, M, gen, gen_s = generate(cases, a.max_steps, a.check_every, a.gen_tol)
     rng = np.random.default_rng(a.seed + 1)
     order = rng.permutation(len(cases))

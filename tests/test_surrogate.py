@@ -133,6 +133,23 @@ def test_pipeline_small(tmp_path):
     assert ev["cases"] == 1 and ev["converged_cold"] == 1 and ev["converged_warm"] == 1
 
 
+@pytest.mark.gpu
+def test_warm_start_gains_over_cold_start(tmp_path):
+    """What the trained network gains: cavities at Re 100-400 (steady within a
+    few 10^4 steps), trained on the GPU, then the held-out cases iterated to
+    the same tolerance from rest and from the prediction.  The warm starts must
+    converge in clearly fewer steps, to fields as close to the reference."""
+    from parallellbmcranfield_gb300 import surrogate as S
+
+    rep = S.main(["--cavities", "30", "--channels", "0", "--cavity-re-max", "400",
+                  "--epochs", "80", "--batch", "4", "--eval", "8", "--lr", "2e-3",
+                  "--out", str(tmp_path / "r.json")])
+    ev = rep["warm_vs_cold"]
+    assert ev["cases"] >= 4 and ev["converged_cold"] == ev["converged_warm"] == ev["cases"], ev
+    assert ev["work_ratio"] >= 1.3, ev
+    assert ev["err_warm_median"] <= 2 * ev["err_cold_median"] + 1e-3, ev
+
+
 def test_pipeline_host_logic():
     """Case draws, input maps and the prediction -> initial-field mapping (CPU)."""
     from parallellbmcranfield_gb300 import surrogate as S

@@ -1103,49 +1103,83 @@ __device__ __forceinline__ uint32_t pack2v(float2 d, int k, const StepArgs &a) {
   return w;
 }
 
-// MRT bulk collision of two nodes in deviation form: the operator of
-// collide_bulk_dev (model 3) with its constants folded (1/36 and the 1.4 /
-// 1.2 rates into the moment differences) so that each population takes one
-// or two paired operations.  g1, g2: non-equilibrium energy moments, e4, e6:
-// heat-flux moments, h7, h8: stress moments.
-__device__ __forceinline__ void collide_mrt_pair(const float2 F[9], const StepArgs &a, float2 M[9]) {
-  const float2 a13 = add2(F[1], F[3]), a24 = add2(F[2], F[4]);
-  const float2 a14 = add2(a13, a24);
-  const float2 p57 = add2(F[5], F[7]), p68 = add2(F[6], F[8]);
+// The two stored 16-bit values of a word as floats, without the deviation
+// scale (raw storage units), and back.
+template <class ST>
+__device__ __forceinline__ float2 raw2(uint32_t w) {
+  if constexpr (std::is_same<typename ST::T, __half>::value) {
+    __half2 h;
+    memcpy(&h, &w, 4);
+    return __half22float2(h);
+  } else {
+    __nv_bfloat162 h;
+    memcpy(&h, &w, 4);
+    return __bfloat1622float2(h);
+  }
+}
+template <class ST>
+__device__ __forceinline__ uint32_t pack_raw2(float2 v) {
+  uint32_t w;
+  if constexpr (std::is_same<typename ST::T, __half>::value) {
+    const __half2 h = __float22half2_rn(v);
+    memcpy(&w, &h, 4);
+  } else {
+    const __nv_bfloat162 h = __float22bfloat162_rn(v);
+    memcpy(&w, &h, 4);
+  }
+  return w;
+}
+template <class ST>
+__device__ __forceinline__ typename ST::T to_raw(float v) {
+  if constexpr (std::is_same<typename ST::T, __half>::value) return __float2half_rn(v);
+  else return __float2bfloat16_rn(v);
+}
+
+// MRT bulk collision of two nodes (the operator of collide_bulk_dev, model 3,
+// constants folded) on packed FP32 pairs and raw storage values.  16-bit storage keeps
+// s_k = d_k * scale_k with scale_k = S / (w_k rho0), so in the unit
+// u0 = rho0 / (36 S) (= inv_scale[8]) the deviation is d_k / u0 = c_k s_k with
+// c_k = 36 w_k = 16, 4, 1: exact powers of two.  The operator is written in
+// that unit (its quadratic terms gain a factor u0, rho = rho0 + u0 * sum) and
+// the input factors c_k and output factors 1 / c_k are folded into its
+// constants, so neither the load nor the store scales anything:
+//   g1 = 4 (a58 + t14) - 32 s0 - 3 u0 jj,  g2 = 48 s0 - 12 t14 + 3 u0 jj,
+//   E4 = (m4 + jx) / 2,  E6 = (m6 + jy) / 2.
+__device__ __forceinline__ void collide_mrt_pair_raw(const float2 S[9], const StepArgs &a, float2 O[9]) {
+  const float u0 = a.inv_scale[8];
+  const float2 t13 = add2(S[1], S[3]), t24 = add2(S[2], S[4]);
+  const float2 t14 = add2(t13, t24);
+  const float2 p57 = add2(S[5], S[7]), p68 = add2(S[6], S[8]);
   const float2 a58 = add2(p57, p68);
-  const float2 rt = add2(add2(F[0], a14), a58);
-  const float2 rho = add2(bc2((float)a.rho0), rt);
-  const float2 m1 = fma2(bc2(-4.f), F[0], sub2(mul2(bc2(2.f), a58), a14));
-  const float2 m2 = fma2(bc2(-2.f), a14, fma2(bc2(4.f), F[0], a58));
-  const float2 d13 = sub2(F[1], F[3]), d24 = sub2(F[2], F[4]);
-  const float2 e57 = sub2(F[5], F[7]), e86 = sub2(F[8], F[6]);
+  const float2 rt = fma2(bc2(16.f), S[0], fma2(bc2(4.f), t14, a58));
+  const float2 rho = fma2(bc2(u0), rt, bc2((float)a.rho0));
+  const float2 u13 = sub2(S[1], S[3]), u24 = sub2(S[2], S[4]);
+  const float2 e57 = sub2(S[5], S[7]), e86 = sub2(S[8], S[6]);
   const float2 x58 = add2(e57, e86), y58 = sub2(e57, e86);
-  const float2 jx = add2(d13, x58), jy = add2(d24, y58);
-  const float2 m4 = fma2(bc2(-2.f), d13, x58), m6 = fma2(bc2(-2.f), d24, y58);
-  const float2 m7 = sub2(a13, a24), m8 = sub2(p57, p68);
-  const float2 ninv = make_float2(__fdividef(-1.f, rho.x), __fdividef(-1.f, rho.y));
+  const float2 jx = fma2(bc2(4.f), u13, x58), jy = fma2(bc2(4.f), u24, y58);
+  const float2 E4 = fma2(bc2(-2.f), u13, x58), E6 = fma2(bc2(-2.f), u24, y58);
+  const float2 w7 = sub2(t13, t24), m8 = sub2(p57, p68);
   const float2 jj = fma2(jx, jx, mul2(jy, jy));
-  const float2 g1 = fma2(bc2(-3.f), jj, fma2(bc2(2.f), rt, m1));
-  const float2 g2 = fma2(bc2(3.f), jj, sub2(m2, rt));
-  const float2 e4 = add2(m4, jx), e6 = add2(m6, jy);
-  const float2 h7 = fma2(mul2(sub2(jx, jy), add2(jx, jy)), ninv, m7);
+  const float2 ninv = make_float2(__fdividef(-u0, rho.x), __fdividef(-u0, rho.y));
+  const float2 g1 = fma2(bc2(-3.f * u0), jj, fma2(bc2(-32.f), S[0], mul2(bc2(4.f), add2(a58, t14))));
+  const float2 g2 = fma2(bc2(3.f * u0), jj, fma2(bc2(48.f), S[0], mul2(bc2(-12.f), t14)));
+  const float2 h7 = fma2(mul2(sub2(jx, jy), add2(jx, jy)), ninv, mul2(bc2(4.f), w7));
   const float2 h8 = fma2(mul2(jx, jy), ninv, m8);
-  const float2 om4 = bc2(0.25f * (float)a.omega);
-  const float2 P = mul2(om4, h7), Q = mul2(om4, h8);
-  const float2 A = mul2(bc2(-1.4f / 36.f), fma2(bc2(2.f), g2, g1));  // c * (-d1 - 2 d2)
-  const float2 D = mul2(bc2(1.4f / 36.f), fma2(bc2(2.f), g1, g2));   // c * (2 d1 + d2)
-  const float2 Z = mul2(bc2(5.6f / 36.f), sub2(g2, g1));            // 4 c (d2 - d1)
-  const float2 ApP = add2(A, P), AmP = sub2(A, P), DpQ = add2(D, Q), DmQ = sub2(D, Q);
-  const float2 s46 = add2(e4, e6), t46 = sub2(e4, e6);
-  M[0] = sub2(F[0], Z);
-  M[1] = fma2(bc2(0.2f), e4, sub2(F[1], ApP));
-  M[3] = fma2(bc2(-0.2f), e4, sub2(F[3], ApP));
-  M[2] = fma2(bc2(0.2f), e6, sub2(F[2], AmP));
-  M[4] = fma2(bc2(-0.2f), e6, sub2(F[4], AmP));
-  M[5] = fma2(bc2(-0.1f), s46, sub2(F[5], DpQ));
-  M[7] = fma2(bc2(0.1f), s46, sub2(F[7], DpQ));
-  M[6] = fma2(bc2(0.1f), t46, sub2(F[6], DmQ));
-  M[8] = fma2(bc2(-0.1f), t46, sub2(F[8], DmQ));
+  const float om = (float)a.omega;
+  const float2 P4 = mul2(bc2(om * (1.f / 16.f)), h7), Q = mul2(bc2(0.25f * om), h8);
+  const float2 A4 = mul2(bc2(-1.4f / 144.f), fma2(bc2(2.f), g2, g1));
+  const float2 D = mul2(bc2(1.4f / 36.f), fma2(bc2(2.f), g1, g2));
+  const float2 ApP = add2(A4, P4), AmP = sub2(A4, P4), DpQ = add2(D, Q), DmQ = sub2(D, Q);
+  const float2 S46 = add2(E4, E6), T46 = sub2(E4, E6);
+  O[0] = fma2(bc2(-5.6f / 576.f), sub2(g2, g1), S[0]);
+  O[1] = fma2(bc2(0.1f), E4, sub2(S[1], ApP));
+  O[3] = fma2(bc2(-0.1f), E4, sub2(S[3], ApP));
+  O[2] = fma2(bc2(0.1f), E6, sub2(S[2], AmP));
+  O[4] = fma2(bc2(-0.1f), E6, sub2(S[4], AmP));
+  O[5] = fma2(bc2(-0.2f), S46, sub2(S[5], DpQ));
+  O[7] = fma2(bc2(0.2f), S46, sub2(S[7], DpQ));
+  O[6] = fma2(bc2(0.2f), T46, sub2(S[6], DmQ));
+  O[8] = fma2(bc2(-0.2f), T46, sub2(S[8], DmQ));
 }
 
 // Edge half-word slot of a shifted plane: cx = +1 planes 1, 5, 8 (lane 0) and
@@ -1230,11 +1264,12 @@ __global__ void __launch_bounds__(128) k_step_h2(const __grid_constant__ StepArg
         }
         word = __byte_perm(word, next, 0x5432);  // (x0+1, x0+2)
       }
-      F[k] = unpack2v<ST>(word, k, a);
+      // MRT works on raw storage values (no scaling), other models on deviations
+      F[k] = MODEL == 3 ? raw2<ST>(word) : unpack2v<ST>(word, k, a);
     }
     float2 M[9];
     if constexpr (MODEL == 3) {
-      collide_mrt_pair(F, a, M);
+      collide_mrt_pair_raw(F, a, M);
     } else {
       float F0[9], F1[9], M0[9], M1[9];
 #pragma unroll
@@ -1260,19 +1295,27 @@ __global__ void __launch_bounds__(128) k_step_h2(const __grid_constant__ StepArg
       if (PH != PH_AB && cl[j][i] == CLS_BULK_REC) {
         const uint32_t sbi = a.aux[node0 + i];
 #pragma unroll
-        for (int k = 0; k < 9; k++)
-          a.sb_dst[(size_t)sbi * 9 + k] = (double)(i ? M[k].y : M[k].x) + wgt<double>(k) * a.rho0;
+        for (int k = 0; k < 9; k++) {
+          const float dv = (i ? M[k].y : M[k].x) * (MODEL == 3 ? a.inv_scale[k] : 1.f);
+          a.sb_dst[(size_t)sbi * 9 + k] = (double)dv + wgt<double>(k) * a.rho0;
+        }
       }
 #pragma unroll
     for (int k = 0; k < 9; k++) {
       if (PH == PH_AA_A) {
         // neighbour write x + e_k, element-wise for fluid nodes
-        if (cl[j][0] != CLS_SOLID) st_dev<ST>(d + (long long)k * a.plane + node0 + nb(k, a.pitch), k, M[k].x, a);
-        if (cl[j][1] != CLS_SOLID)
-          st_dev<ST>(d + (long long)k * a.plane + node0 + 1 + nb(k, a.pitch), k, M[k].y, a);
+        T *q = d + (long long)k * a.plane + node0 + nb(k, a.pitch);
+        if constexpr (MODEL == 3) {
+          if (cl[j][0] != CLS_SOLID) q[0] = to_raw<ST>(M[k].x);
+          if (cl[j][1] != CLS_SOLID) q[1] = to_raw<ST>(M[k].y);
+        } else {
+          if (cl[j][0] != CLS_SOLID) st_dev<ST>(q, k, M[k].x, a);
+          if (cl[j][1] != CLS_SOLID) st_dev<ST>(q + 1, k, M[k].y, a);
+        }
       } else {
         const int plane = (PH == PH_AB) ? k : OPP[k];
-        __stcs((unsigned *)(d + (long long)plane * a.plane + node0), pack2v<ST>(M[k], k, a));
+        const uint32_t wd = MODEL == 3 ? pack_raw2<ST>(M[k]) : pack2v<ST>(M[k], k, a);
+        __stcs((unsigned *)(d + (long long)plane * a.plane + node0), wd);
       }
     }
   }

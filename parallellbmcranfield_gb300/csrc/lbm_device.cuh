@@ -886,6 +886,14 @@ __device__ __forceinline__ void step_one(const StepArgs &a, long long node, uint
   collide_store<ST, MODEL, PH>(a, node, c, F, rho, u, v);
 }
 
+// The per-node path as a called function, for the paired kernels whose warps
+// take it only where a boundary runs through them: keeping it out of line
+// keeps its registers out of the bulk path's allocation.
+template <class ST, int MODEL, int PH>
+__device__ __noinline__ void step_one_cold(const StepArgs &a, long long node, uint8_t c) {
+  step_one<ST, MODEL, PH>(a, node, c);
+}
+
 // Fused step: METAF_t (layout PH) -> METAF_{t+1}.  A block is BX threads
 // along x; each thread updates NPT consecutive rows of its column.  When all
 // NPT nodes are free of boundary work their 9*NPT loads are issued before any
@@ -1189,7 +1197,7 @@ __device__ __forceinline__ constexpr int edge_slot(int k) {
 }
 
 template <class ST, int MODEL, int PH, int NPT>
-__global__ void __launch_bounds__(128) k_step_h2(const __grid_constant__ StepArgs a) {
+__global__ void __launch_bounds__(128, NPT == 2 ? 8 : 1) k_step_h2(const __grid_constant__ StepArgs a) {
   using T = typename ST::T;
   static_assert(sizeof(T) == 2, "paired-node kernel is for 16-bit storage");
   const unsigned FULL = 0xffffffffu;
@@ -1214,7 +1222,7 @@ __global__ void __launch_bounds__(128) k_step_h2(const __grid_constant__ StepArg
 #pragma unroll
       for (int i = 0; i < 2; i++)
         if (x0 + i < a.n && y0 + j < a.m)
-          step_one<ST, MODEL, PH>(a, (long long)(y0 + j) * a.pitch + x0 + i, cl[j][i]);
+          step_one_cold<ST, MODEL, PH>(a, (long long)(y0 + j) * a.pitch + x0 + i, cl[j][i]);
     return;
   }
   if (!__any_sync(FULL, fluid)) return;

@@ -233,6 +233,7 @@ typedef struct lbm_sg_config {
   float lr, beta1, beta2, eps;  /* Adam */
   uint64_t seed;           /* weight initialisation */
   int32_t device;
+  float weight_decay;      /* decoupled (AdamW) decay per unit learning rate; 0 = Adam */
 } lbm_sg_config;
 lbm_status lbm_sg_create(const lbm_sg_config *cfg, lbm_sg **out);
 void lbm_sg_destroy(lbm_sg *s);

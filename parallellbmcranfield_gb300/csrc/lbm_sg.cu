@@ -512,16 +512,16 @@ __global__ void k_mse(const bf16 *Y, const float *T, const float *mask, bf16 *dY
   if ((threadIdx.x & 31) == 0) atomicAdd(loss, s * inv_count);
 }
 
-// Adam on FP32 master weights.
+// Adam on FP32 master weights, with decoupled weight decay wd (AdamW).
 __global__ void k_adam(float *w, const float *g, float *m, float *v, size_t n, float lr, float b1,
-                       float b2, float eps, float c1, float c2) {
+                       float b2, float eps, float c1, float c2, float wd) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const float gi = g[i];
     const float mi = b1 * m[i] + (1.f - b1) * gi;
     const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
     m[i] = mi;
     v[i] = vi;
-    w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    w[i] -= lr * ((mi / c1) / (sqrtf(vi / c2) + eps) + wd * w[i]);
   }
 }
 
@@ -820,7 +820,7 @@ void adam(lbm_sg *s) {
   const lbm_sg_config &c = s->cfg;
   const float c1 = 1.f - std::pow(c.beta1, (float)s->step), c2 = 1.f - std::pow(c.beta2, (float)s->step);
   k_adam<<<grid_for(s->nparam), 256, 0, s->stream>>>(s->w, s->g, s->m, s->v, s->nparam, c.lr, c.beta1,
-                                                     c.beta2, c.eps, c1, c2);
+                                                     c.beta2, c.eps, c1, c2, c.weight_decay);
   refresh_weights(s);
 }
 

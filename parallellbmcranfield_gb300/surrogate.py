@@ -16,9 +16,11 @@ three give every cell its position, which 3x3 convolutions with zero padding do
 not see beyond their receptive field) and a gap-flow estimate g / U (channels:
 the inlet flow rate split over the fluid gaps of each column in proportion to
 gap width cubed, each gap carrying a parabolic profile; cavities: 0).  Output
-(3 maps): clip((rho - 1) / U^2, -8, 8) / 4, (u - g) / U, v / U on fluid cells
-(the clip keeps the pressure peaks at the lid corners from dominating the loss;
-the network corrects the gap-flow estimate rather than rebuilding it).
+(3 maps): clip((rho - 1) / U^2, -8, 8) / 10, (u - g) / U, v / U on fluid cells
+(the clip keeps the pressure peaks at the lid corners from dominating the loss
+and the factor 1/10 weights the squared error towards the velocity, which sets
+the warm start's slow modes; the network corrects the gap-flow estimate rather
+than rebuilding it).
 
 The training targets are run to a tighter tolerance (gen_tol) than the
 comparison (tol) and serve as the converged reference against which both the
@@ -40,7 +42,7 @@ import parallellbmcranfield_gb300 as G
 GRID = 256
 SIDE = GRID - 2
 IN_CH = 8
-RHO_CLIP, RHO_SCALE = 8.0, 0.25
+RHO_CLIP, RHO_SCALE = 8.0, 0.1
 
 
 def make_cases(n_cav, n_ch, seed, cavity_re=(100.0, 5000.0)):
@@ -209,13 +211,13 @@ def cosine_lr(lr, lr_min, epoch, epochs):
     return lr_min + 0.5 * (lr - lr_min) * (1.0 + math.cos(math.pi * epoch / max(1, epochs)))
 
 
-def train(X, Y, M, train_idx, epochs, batch, lr, seed, lr_min=None):
+def train(X, Y, M, train_idx, epochs, batch, lr, seed, lr_min=None, weight_decay=0.0):
     """Adam with a cosine learning-rate schedule over the samples train_idx of
     (X, Y, M); returns the network, the mean loss of every epoch and the time."""
     if len(train_idx) == 0:
         raise ValueError("no training samples (no case reached the generation tolerance)")
     net = G.Surrogate(height=GRID, width=GRID, in_channels=X.shape[-1], out_channels=3, base=32,
-                      max_batch=batch, lr=lr, seed=seed)
+                      max_batch=batch, lr=lr, seed=seed, weight_decay=weight_decay)
     net.set_dataset(X, Y, M)
     rng = np.random.default_rng(seed)
     lr_min = lr * 0.02 if lr_min is None else lr_min
@@ -306,6 +308,7 @@ def main(argv=None):
     p.add_argument("--epochs", type=int, default=100)
     p.add_argument("--batch", type=int, default=8)
     p.add_argument("--lr", type=float, default=1e-3)
+    p.add_argument("--weight-decay", type=float, default=0.0, help="AdamW decay")
     p.add_argument("--eval", type=int, default=400, help="test cases in the warm/cold comparison")
     p.add_argument("--no-augment", action="store_true", help="no mirrored channels in training")
     p.add_argument("--seed", type=int, default=20240601)
@@ -321,7 +324,8 @@ def main(argv=None):
     tr, te = tr[steady[tr]], te[steady[te]]
     Xt, Yt, Mt = training_set(cases, X, Y, M, tr, augment=not a.no_augment)
     n_samples = len(Xt)
-    net, hist, train_s = train(Xt, Yt, Mt, np.arange(len(Xt)), a.epochs, a.batch, a.lr, a.seed)
+    net, hist, train_s = train(Xt, Yt, Mt, np.arange(len(Xt)), a.epochs, a.batch, a.lr, a.seed,
+                               weight_decay=a.weight_decay)
     del Xt, Yt, Mt
     test_mse = masked_mse(net, X, Y, M, te)[0] if len(te) else None
     ev = evaluate(net, cases, meshes, X, Y, M, te[: a.eval], a.max_steps, a.check_every, a.tol)
@@ -331,6 +335,7 @@ def main(argv=None):
                         steps_mean=float(gen["steps"].mean()), max_steps=a.max_steps,
                         check_every=a.check_every, tol=a.gen_tol),
         training=dict(cases=len(tr), samples=n_samples, epochs=a.epochs, batch=a.batch,
+                      lr=a.lr, weight_decay=a.weight_decay,
                       seconds=train_s, loss_first=hist[0], loss_last=hist[-1],
                       params=net.num_params, history=hist),
         test_mse=test_mse, tol=a.tol, warm_vs_cold=ev)

@@ -82,7 +82,8 @@ __device__ __forceinline__ void ldsm_x4_t(uint32_t r[4], const void *row) {
 // warp 32 x BN/2; K in tiles of 32 through a GSTAGES-deep cp.async ring.  With
 // GATHER the A operand is the im2col of X, formed while loading: row p is a
 // pixel, column k = r*C + c is channel c of the pixel at tap offset r (3x3,
-// pad 1, or 1x1); C is a multiple of GBK, so one K tile lies within one tap.
+// pad 1, or 1x1), zero for k >= taps*C; C is a multiple of 8, so every
+// 16-byte chunk of a row lies within one tap.
 template <int EPI, bool GATHER, int BN>
 __global__ void __launch_bounds__(256) k_gemm(const GemmArgs g) {
   constexpr int NJ = BN / 16;  // n8 tiles per warp
@@ -116,11 +117,12 @@ __global__ void __launch_bounds__(256) k_gemm(const GemmArgs g) {
       const bf16 *src = g.Bt;  // any valid address when nothing is read
       bool ok = aok[it];
       if (GATHER) {
-        const int r = k0 / g.C, c0 = k0 - r * g.C;
+        const int kk = k0 + ac8[it];
+        const int r = kk / g.C, c = kk - r * g.C;
         const int dy = g.taps == 9 ? r / 3 - 1 : 0, dx = g.taps == 9 ? r % 3 - 1 : 0;
         const int yy = ay[it] + dy, xx = ax[it] + dx;
-        ok = ok && yy >= 0 && yy < g.H && xx >= 0 && xx < g.W;
-        if (ok) src = g.X + (size_t)(p + dy * g.W + dx) * g.C + c0 + ac8[it];
+        ok = ok && r < g.taps && yy >= 0 && yy < g.H && xx >= 0 && xx < g.W;
+        if (ok) src = g.X + (size_t)(p + dy * g.W + dx) * g.C + c;
       } else if (ok) {
         src = g.A + (size_t)p * g.K + k0 + ac8[it];
       }
@@ -662,8 +664,8 @@ void refresh_weights(lbm_sg *s) {
     k_weights<<<64, 256, 0, s->stream>>>(s->w + c.woff, c.Wt, c.Wd, c.cout, c.cin, c.taps, c.Kp, c.Kpd);
 }
 
-// The implicit im2col needs whole K tiles inside one tap.
-bool gather_ok(int C) { return C % GBK == 0; }
+// The implicit im2col needs every 16-byte chunk inside one tap.
+bool gather_ok(int C) { return C % 8 == 0; }
 
 lbm_status conv_fwd(lbm_sg *s, int li, int xi, int yi, int B) {
   const Conv &c = s->conv[li];
@@ -700,7 +702,7 @@ lbm_status conv_bwd(lbm_sg *s, int li, int xi, int yi, int B, bool need_dx) {
     k_bias_grad<<<grid_for((size_t)M), 256, 0, s->stream>>>(Y.dx, s->g + c.boff, (size_t)M, c.cout);
   }
   lbm_status st = LBM_OK;
-  if (X.c % 8 == 0 && c.cout % 8 == 0 && c.Kp == c.taps * X.c) {
+  if (X.c % 8 == 0 && c.cout % 8 == 0) {
     const int bm = (c.cout + DWM - 1) / DWM, bn = (c.Kp + DWN - 1) / DWN;
     const int splits = std::max(1, std::min(M / (DWK * 8), (152 * 6) / (bm * bn) + 1));
     const int pchunk = rup((M + splits - 1) / splits, DWK);

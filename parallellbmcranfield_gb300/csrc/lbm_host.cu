@@ -131,13 +131,16 @@ bool step_config(lbm_ctx *c, int var, dim3 *grid, dim3 *block, size_t *smem) {
     *grid = dim3((unsigned)((span + V.bx * V.v - 1) / (V.bx * V.v)),
                  (unsigned)((c->P.m + V.npt - 1) / V.npt));
     *block = dim3(V.bx);
-    if (V.kind == 3 && c->pf_blocks[var] == 0) {  // one wave of resident blocks, looked up once
+    // L2 prefetch distance of the paired kernel: a quarter of a wave of resident
+    // blocks (measured at 16384^2: 1/4-1/3 wave 1.79 ms/step, 1 wave 1.82, 2 waves 2.08,
+    // none 2.02), looked up once per variant
+    if (V.kind == 3 && c->pf_blocks[var] == 0) {
       const void *fn = c->ks->step[c->p.collision_model][layout_of(c)][var];
       int per_sm = 0, sms = 0;
       if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, V.bx, 0) != cudaSuccess)
         per_sm = 0;
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->p.device);
-      c->pf_blocks[var] = per_sm > 0 ? per_sm * sms : -1;
+      c->pf_blocks[var] = per_sm > 0 ? std::max(1, per_sm * sms / 4) : -1;
     }
     return true;
   }

@@ -84,7 +84,7 @@ struct StepArgs {
   int tma_stages;           // ring depth of the TMA step (from the shared-memory budget)
   int tma_tiles_x, tma_tiles_y;
   int pf_blocks;            // paired 16-bit step: L2 prefetch for the block this many launch
-                            // positions ahead (about one wave of resident blocks); 0 = off
+                            // positions ahead (a fraction of a wave of resident blocks); 0 = off
 };
 
 // Outputs of the read-only finish kernel (any pointer may be null).

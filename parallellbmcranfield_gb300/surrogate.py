@@ -324,10 +324,10 @@ def main(argv=None):
     p.add_argument("--check-every", type=int, default=100)
     p.add_argument("--tol", type=float, default=1e-6, help="du_rel of the warm/cold comparison")
     p.add_argument("--gen-tol", type=float, default=1e-7, help="du_rel of the training targets")
-    p.add_argument("--epochs", type=int, default=100)
+    p.add_argument("--epochs", type=int, default=200)
     p.add_argument("--batch", type=int, default=8)
     p.add_argument("--lr", type=float, default=1e-3)
-    p.add_argument("--weight-decay", type=float, default=0.0, help="AdamW decay")
+    p.add_argument("--weight-decay", type=float, default=0.01, help="AdamW decay")
     p.add_argument("--eval", type=int, default=400, help="test cases in the warm/cold comparison")
     p.add_argument("--no-augment", action="store_true", help="no mirrored channels in training")
     p.add_argument("--seed", type=int, default=20240601)

@@ -34,24 +34,7 @@ template <class ST, int MODEL, int BX, int NPT>
 __global__ void __launch_bounds__(BX) k_batch_step(const BatchCase *cases, const int4 *tiles,
                                                    int ntiles, const int *active,
                                                    const int *gpar) {
-  using T = typename ST::T;
-  constexpr unsigned ROW_BYTES = BX * sizeof(T);  // one plane row of a tile, 16-byte multiple
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    // L2 prefetch of this block's next tile (9 planes x NPT rows, one bulk
-    // prefetch each) while this one is computed.  A hint only; every address
-    // lies inside that case's state array.
-    const int tn = t + gridDim.x;
-    if (tn < ntiles && threadIdx.x < 9 * NPT) {
-      const int4 nx = tiles[tn];
-      if (active[nx.x]) {
-        const StepArgs &na = cases[nx.x].args[gpar[nx.x] & 1];
-        const int k = threadIdx.x / NPT, y = nx.z * NPT + threadIdx.x % NPT, x = nx.y * BX;
-        if (y < na.m && x + BX <= na.pitch) {
-          const T *p = (const T *)na.src + (long long)k * na.plane + (long long)y * na.pitch + x;
-          asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(ROW_BYTES) : "memory");
-        }
-      }
-    }
     const int4 tl = tiles[t];
     if (!active[tl.x]) continue;
     const StepArgs &a = cases[tl.x].args[gpar[tl.x] & 1];

@@ -30,10 +30,23 @@ struct BatchState {
   long long *conv_at; // per case: iteration at which du_rel <= tol was first seen (-1)
 };
 
+// Work-list compaction: the entries (x = case) of cases still stepping, in
+// any order, and their count (zeroed before the launch).  Run at the start of
+// every run segment, so that the step kernels walk only live work once cases
+// have converged.
+template <class E>
+__global__ void k_batch_compact(const E *in, int n, const int *active, E *out, int *count) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const E e = in[i];
+    if (active[e.x]) out[atomicAdd(count, 1)] = e;
+  }
+}
+
 template <class ST, int MODEL, int BX, int NPT>
 __global__ void __launch_bounds__(BX) k_batch_step(const BatchCase *cases, const int4 *tiles,
-                                                   int ntiles, const int *active,
+                                                   const int *ntiles_live, const int *active,
                                                    const int *gpar) {
+  const int ntiles = *ntiles_live;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int4 tl = tiles[t];
     if (!active[tl.x]) continue;
@@ -46,8 +59,9 @@ __global__ void __launch_bounds__(BX) k_batch_step(const BatchCase *cases, const
 // y: linear node index), after or alongside k_batch_step in the same step.
 template <class ST, int MODEL>
 __global__ void __launch_bounds__(128) k_batch_special(const BatchCase *cases, const int2 *list,
-                                                       int nlist, const int *active,
+                                                       const int *nlist_live, const int *active,
                                                        const int *gpar) {
+  const int nlist = *nlist_live;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nlist; i += gridDim.x * blockDim.x) {
     const int2 e = list[i];
     if (!active[e.x]) continue;
@@ -148,6 +162,8 @@ struct BatchKernels {
   const void *du;
   const void *advance;
   const void *converge;
+  const void *compact_tiles;    // k_batch_compact<int4>
+  const void *compact_special;  // k_batch_compact<int2>
 };
 
 }  // namespace lbm

@@ -60,6 +60,9 @@ struct lbm_batch {
   int nrows = 0;
   int2 *d_special = nullptr;  // (case, node) of every node with boundary work
   int nspecial = 0;
+  int4 *d_live_tiles = nullptr;   // compacted work lists of the cases still stepping
+  int2 *d_live_special = nullptr;
+  int *d_live_n = nullptr;        // [0]: live tiles, [1]: live special nodes
   int variant = 1;
   cudaStream_t stream = nullptr;
   const lbm::KernelSet *ks = nullptr;
@@ -145,17 +148,37 @@ lbm_status set_rest(lbm_batch *b) {
   return LBM_OK;
 }
 
+// The work lists of the cases still stepping (start of every run segment).
+lbm_status launch_compact(lbm_batch *b) {
+  LBM_BCK(cudaMemsetAsync(b->d_live_n, 0, 2 * sizeof(int), b->stream));
+  int *cnt_t = b->d_live_n, *cnt_s = b->d_live_n + 1;
+  int nt = b->ntiles[b->variant];
+  void *targs[] = {&b->d_tiles[b->variant], &nt, &b->s.active, &b->d_live_tiles, &cnt_t};
+  cudaError_t e = cudaLaunchKernel(b->bk->compact_tiles, dim3(std::min((nt + 255) / 256, 152 * 8)),
+                                   dim3(256), targs, 0, b->stream);
+  if (e == cudaSuccess && b->nspecial > 0) {
+    void *sargs[] = {&b->d_special, &b->nspecial, &b->s.active, &b->d_live_special, &cnt_s};
+    e = cudaLaunchKernel(b->bk->compact_special,
+                         dim3(std::min((b->nspecial + 255) / 256, 152 * 8)), dim3(256), sargs, 0,
+                         b->stream);
+  }
+  if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch compact: ") + cudaGetErrorString(e));
+  return LBM_OK;
+}
+
 lbm_status launch_steps(lbm_batch *b, int k) {
   const void *fn = b->bk->step[b->model][b->variant];
   const int bx = lbm::BVAR_BX[b->variant];
   const int grid = std::min(b->ntiles[b->variant], persistent_blocks(fn, bx, b->device));
+  lbm_status st = launch_compact(b);
+  if (st != LBM_OK) return st;
+  int *cnt_t = b->d_live_n, *cnt_s = b->d_live_n + 1;
   for (int i = 0; i < k; i++) {
-    void *args[] = {&b->d_cases, &b->d_tiles[b->variant], &b->ntiles[b->variant], &b->s.active,
-                    &b->s.gpar};
+    void *args[] = {&b->d_cases, &b->d_live_tiles, &cnt_t, &b->s.active, &b->s.gpar};
     cudaError_t e = cudaLaunchKernel(fn, dim3(grid), dim3(bx), args, 0, b->stream);
     if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
     if (b->nspecial > 0) {
-      void *sargs[] = {&b->d_cases, &b->d_special, &b->nspecial, &b->s.active, &b->s.gpar};
+      void *sargs[] = {&b->d_cases, &b->d_live_special, &cnt_s, &b->s.active, &b->s.gpar};
       const int sg = std::min((b->nspecial + 127) / 128, 152 * 16);
       e = cudaLaunchKernel(b->bk->special[b->model], dim3(sg), dim3(128), sargs, 0, b->stream);
       if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch special: ") + cudaGetErrorString(e));
@@ -322,6 +345,12 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
     if ((st = balloc(b, &b->d_tiles[v], tiles[v].size())) != LBM_OK) return bail(st);
     cudaMemcpy(b->d_tiles[v], tiles[v].data(), tiles[v].size() * sizeof(int4), cudaMemcpyHostToDevice);
   }
+  size_t max_tiles = 0;
+  for (int v = 0; v < lbm::BVAR; v++) max_tiles = std::max(max_tiles, tiles[v].size());
+  if ((st = balloc(b, &b->d_live_tiles, max_tiles)) != LBM_OK ||
+      (st = balloc(b, &b->d_live_special, specials.size())) != LBM_OK ||
+      (st = balloc(b, &b->d_live_n, 2)) != LBM_OK)
+    return bail(st);
   b->nspecial = (int)specials.size();
   if ((st = balloc(b, &b->d_special, specials.size())) != LBM_OK) return bail(st);
   if (!specials.empty())

@@ -39,6 +39,8 @@ const BatchKernels &LBM_BATCH_FN(LBM_PREC)() {
     k.du = (const void *)k_batch_du<LBM_ST>;
     k.advance = (const void *)k_batch_advance;
     k.converge = (const void *)k_batch_converge;
+    k.compact_tiles = (const void *)k_batch_compact<int4>;
+    k.compact_special = (const void *)k_batch_compact<int2>;
     return k;
   }();
   return bk;

@@ -3,6 +3,7 @@
     python -m parallellbmcranfield_gb300.workloads cylinder   [--out r.json]
     python -m parallellbmcranfield_gb300.workloads steady     [--out r.json]
     python -m parallellbmcranfield_gb300.workloads cavities   [--out r.json]
+    python -m parallellbmcranfield_gb300.workloads batch      [--cases N --steps K]
 
 cylinder: channel of 2048 x 512 nodes, MRT, parabolic inlet (u_max 0.04),
   constant-pressure outlet, a cylinder of diameter 64 centred at (400, 257)
@@ -16,6 +17,8 @@ cavities: 256 lid-driven cavities in one batch, sides log-uniform in
   [64, 1024], Re uniform in [100, 3200], lid 0.05, TRT (magic parameter 3/16),
   FP32, autotuned tile, run until every case reaches du_rel <= 1e-6 or stops
   on NaN.
+batch: throughput of the batched step alone: N lid-driven cavities of 256^2
+  nodes, MRT, Re 1000, FP32, K steps with no case converging (tol < 0).
 """
 import argparse
 import json
@@ -150,12 +153,34 @@ def cavities(n=256, max_steps=2000000, seed=20240603):
                 min_cell_re_diverged=float((0.05 / nu[conv == -1]).min()) if (conv == -1).any() else None)
 
 
+def batch(n=256, steps=2000, side=254):
+    cs = [(G.Mesh.cavity(side), dict(uavg=0.05, vavg=0.0, rho_ini=1.0, viscosity=0.05 * side / 1000,
+                                      inlet_profile=2, collision_model=G.MRT, curved_boundaries=1,
+                                      outlet_profile=2)) for _ in range(n)]
+    b = G.Batch(cs, precision="fp32")
+    tune = b.autotune(5)
+    b.set_rest()
+    b.run(200, check_every=100, tol=-1.0)  # warm-up
+    r = b.run(steps, check_every=100, tol=-1.0)
+    info = b.info()
+    b.close()
+    node_steps = float(info["nodes"]) * steps
+    return dict(cases=n, nodes=info["nodes"], steps=steps, seconds=r["seconds"], tune=tune,
+                glups=node_steps / r["seconds"] / 1e9,
+                hbm_gbs=node_steps * 72 / r["seconds"] / 1e9)
+
+
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("workload", choices=["cylinder", "steady", "cavities"])
+    p.add_argument("workload", choices=["cylinder", "steady", "cavities", "batch"])
+    p.add_argument("--cases", type=int, default=256)
+    p.add_argument("--steps", type=int, default=2000)
     p.add_argument("--out", default=None)
     a = p.parse_args(argv)
-    r = {"cylinder": cylinder, "steady": steady, "cavities": cavities}[a.workload]()
+    if a.workload == "batch":
+        r = batch(a.cases, a.steps)
+    else:
+        r = {"cylinder": cylinder, "steady": steady, "cavities": cavities}[a.workload]()
     print(json.dumps(r))
     if a.out:
         with open(a.out, "w") as f:

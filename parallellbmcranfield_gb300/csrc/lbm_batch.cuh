@@ -46,12 +46,20 @@ template <class ST, int MODEL, int BX, int NPT>
 __global__ void __launch_bounds__(BX) k_batch_step(const BatchCase *cases, const int4 *tiles,
                                                    const int *ntiles_live, const int *active,
                                                    const int *gpar) {
+  // The tile's case arguments are copied to shared memory once per tile: read
+  // through a pointer to global memory they could alias the population
+  // stores, and every node would reload them.
+  __shared__ __align__(16) StepArgs sa;
+  static_assert(sizeof(StepArgs) % 4 == 0, "word copy");
   const int ntiles = *ntiles_live;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int4 tl = tiles[t];
-    if (!active[tl.x]) continue;
-    const StepArgs &a = cases[tl.x].args[gpar[tl.x] & 1];
-    step_column<ST, MODEL, PH_AB, NPT, true>(a, tl.y * BX + threadIdx.x, tl.z * NPT);
+    if (!active[tl.x]) continue;  // uniform over the block
+    const int *from = (const int *)&cases[tl.x].args[gpar[tl.x] & 1];
+    __syncthreads();  // the previous tile is done with sa
+    for (int i = threadIdx.x; i < (int)(sizeof(StepArgs) / 4); i += BX) ((int *)&sa)[i] = from[i];
+    __syncthreads();
+    step_column<ST, MODEL, PH_AB, NPT, true>(sa, tl.y * BX + threadIdx.x, tl.z * NPT);
   }
 }
 

@@ -65,6 +65,8 @@ struct lbm_batch {
   int *d_live_n = nullptr;        // [0]: live tiles, [1]: live special nodes
   int variant = 1;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;  // boundary-node pass, concurrent with the bulk pass
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   const lbm::KernelSet *ks = nullptr;
   const lbm::BatchKernels *bk = nullptr;
   int *d_err = nullptr;
@@ -95,6 +97,9 @@ void bfree(lbm_batch *b) {
   if (b->graph) cudaGraphExecDestroy(b->graph);
   for (void *p : b->allocs) cudaFree(p);
   b->allocs.clear();
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->ev_join) cudaEventDestroy(b->ev_join);
+  if (b->side) cudaStreamDestroy(b->side);
   if (b->stream) cudaStreamDestroy(b->stream);
 }
 
@@ -174,14 +179,23 @@ lbm_status launch_steps(lbm_batch *b, int k) {
   if (st != LBM_OK) return st;
   int *cnt_t = b->d_live_n, *cnt_s = b->d_live_n + 1;
   for (int i = 0; i < k; i++) {
+    // the boundary-node pass writes other nodes than the bulk pass and both
+    // only read the source state, so it runs on a second stream alongside
+    // (fork and join by events: two parallel branches when captured)
+    if (b->nspecial > 0) {
+      LBM_BCK(cudaEventRecord(b->ev_fork, b->stream));
+      LBM_BCK(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
+    }
     void *args[] = {&b->d_cases, &b->d_live_tiles, &cnt_t, &b->s.active, &b->s.gpar};
     cudaError_t e = cudaLaunchKernel(fn, dim3(grid), dim3(bx), args, 0, b->stream);
     if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
     if (b->nspecial > 0) {
       void *sargs[] = {&b->d_cases, &b->d_live_special, &cnt_s, &b->s.active, &b->s.gpar};
       const int sg = std::min((b->nspecial + 127) / 128, 152 * 16);
-      e = cudaLaunchKernel(b->bk->special[b->model], dim3(sg), dim3(128), sargs, 0, b->stream);
+      e = cudaLaunchKernel(b->bk->special[b->model], dim3(sg), dim3(128), sargs, 0, b->side);
       if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch special: ") + cudaGetErrorString(e));
+      LBM_BCK(cudaEventRecord(b->ev_join, b->side));
+      LBM_BCK(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
     }
     void *aargs[] = {&b->nc, &b->s};
     e = cudaLaunchKernel(b->bk->advance, dim3((b->nc + 255) / 256), dim3(256), aargs, 0, b->stream);
@@ -260,7 +274,10 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
     default: b->ks = &lbm::kernels_f16(); b->bk = &lbm::batch_kernels_2(); break;
   }
   if (cudaSetDevice(p0.device) != cudaSuccess) return bail(fail(LBM_CUDA, "cudaSetDevice failed"));
-  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess)
     return bail(fail(LBM_CUDA, "cudaStreamCreate failed"));
   lbm_status st;
   if ((st = balloc(b, &b->d_err, 1)) != LBM_OK) return bail(st);

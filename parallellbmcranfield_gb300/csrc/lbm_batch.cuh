@@ -65,10 +65,15 @@ __global__ void __launch_bounds__(BX) k_batch_step(const BatchCase *cases, const
 
 // The nodes with boundary work of every case, one thread each (x: case,
 // y: linear node index), after or alongside k_batch_step in the same step.
+// The case arguments are read through restrict pointers: they do not alias
+// the population stores, so the compiler may keep them in registers across
+// the node's stores instead of reloading them.
 template <class ST, int MODEL>
-__global__ void __launch_bounds__(128) k_batch_special(const BatchCase *cases, const int2 *list,
-                                                       const int *nlist_live, const int *active,
-                                                       const int *gpar) {
+__global__ void __launch_bounds__(128) k_batch_special(const BatchCase *__restrict__ cases,
+                                                       const int2 *__restrict__ list,
+                                                       const int *__restrict__ nlist_live,
+                                                       const int *__restrict__ active,
+                                                       const int *__restrict__ gpar) {
   const int nlist = *nlist_live;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nlist; i += gridDim.x * blockDim.x) {
     const int2 e = list[i];

@@ -76,6 +76,12 @@ def barrier(ws):
         dist.barrier()
 
 
+def job_mlups(ws, nodes, steps, ms_max):
+    """Whole-job throughput of ws replicas of `nodes` nodes each, `steps`
+    steps, timed by the slowest rank (ms_max)."""
+    return ws * nodes * steps / (ms_max / 1e3) / 1e6
+
+
 def max_over_ranks(ws, x, device):
     if ws == 1:
         return x
@@ -274,7 +280,7 @@ def run_gpu(args):
     ms_max = max_over_ranks(ws, ms, dev)
     clocks = clk.summary()
     launches = args.steps  # one fused step kernel per step, nothing else in the timed region
-    mlups = ws * N * args.steps / (ms_max / 1e3) / 1e6
+    mlups = job_mlups(ws, N, args.steps, ms_max)
     per_launch_s = ms / 1e3 / args.steps
     bpn = BYTES[prec]
     achieved = bpn * N / per_launch_s / 1e9

@@ -234,6 +234,9 @@ typedef struct lbm_sg_config {
   uint64_t seed;           /* weight initialisation */
   int32_t device;
   float weight_decay;      /* decoupled (AdamW) decay per unit learning rate; 0 = Adam */
+  float coarse_weight;     /* weight of the block-mean loss term (0 = off): the masked means of
+                              output and target over coarse_block^2 cells are compared too */
+  int32_t coarse_block;    /* divides height and width */
 } lbm_sg_config;
 lbm_status lbm_sg_create(const lbm_sg_config *cfg, lbm_sg **out);
 void lbm_sg_destroy(lbm_sg *s);
@@ -243,7 +246,9 @@ lbm_status lbm_sg_set_params(lbm_sg *s, const float *in);
 /* y[batch][H][W][out] = net(x[batch][H][W][in]) */
 lbm_status lbm_sg_forward(lbm_sg *s, int32_t batch, const float *x, float *y);
 /* Masked mean-squared-error loss and its gradient (no update): loss = sum over
- * cells and outputs of mask * (y - target)^2 / (sum mask * out_channels);
+ * cells and outputs of mask * (y - target)^2 / (sum mask * out_channels), plus
+ * coarse_weight * the mean over blocks with mask and outputs of (block mean of y -
+ * block mean of target)^2 when coarse_weight > 0;
  * mask NULL = all ones; grads (NULL = not copied) receives num_params floats. */
 lbm_status lbm_sg_loss_grads(lbm_sg *s, int32_t batch, const float *x, const float *target,
                              const float *mask, double *loss, float *grads);

@@ -136,7 +136,9 @@ class Net:
             gX = self.rb(col2im(np.einsum("bhwo,orc->bhwrc", G, self.rb(W), optimize=True), taps, X.shape))
         return gX, (gW, gb)
 
-    def loss_grads(self, x, t, m=None):
+    def loss_grads(self, x, t, m=None, coarse=None):
+        """Loss, output and flat gradients; coarse = (weight, block) adds the
+        block-mean term of lbm_sg_loss_grads."""
         rb = self.rb
         y = self.forward(x)
         B, H, W, C = y.shape
@@ -145,6 +147,18 @@ class Net:
         d = y - t
         loss = float((m[..., None] * d * d).sum() * inv)
         G = rb(2 * inv * m[..., None] * d)
+        if coarse is not None and coarse[0] > 0:
+            lam, s = coarse
+            blk = lambda a: a.reshape(B, H // s, s, W // s, s, *a.shape[3:]).sum(axis=(2, 4))
+            w = blk(m)
+            ok = w > 0
+            D = np.where(ok[..., None], (blk(m[..., None] * y) - blk(m[..., None] * t)) /
+                         np.where(ok, w, 1)[..., None], 0.0)
+            nb = ok.sum()
+            loss += float(lam * (D[ok] ** 2).sum() / (nb * C))
+            up = lambda a: np.repeat(np.repeat(a, s, axis=1), s, axis=2)
+            g = lam * 2 * up(D) * m[..., None] / up(np.where(ok, w, 1))[..., None] / (nb * C)
+            G = rb(G + np.where(up(ok)[..., None], g, 0.0))
         grads = [None] * 15
         b = self.base
         G, grads[14] = self.conv_back(14, G)

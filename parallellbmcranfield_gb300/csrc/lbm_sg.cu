@@ -514,6 +514,58 @@ __global__ void k_mse(const bf16 *Y, const float *T, const float *mask, bf16 *dY
   if ((threadIdx.x & 31) == 0) atomicAdd(loss, s * inv_count);
 }
 
+// Block-mean term of the loss: the masked means of output and target over
+// s x s blocks (per sample and channel) are compared as well, so that errors
+// of the large scales weigh more than their share of single cells.
+// Pass 1, one thread per (block, channel): D = mean_m(y) - mean_m(t), the
+// block's mask weight, and the count of blocks with any weight (channel 0).
+__global__ void k_coarse_stats(const bf16 *Y, const float *T, const float *mask, int B, int H, int W,
+                               int C, int s, float *D, float *wsum, double *nblk) {
+  const int nbx = W / s, nby = H / s, nb = B * nby * nbx;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nb * C; i += gridDim.x * blockDim.x) {
+    const int c = i % C, blk = i / C;
+    const int bx = blk % nbx, by = (blk / nbx) % nby, b = blk / (nbx * nby);
+    float sy = 0.f, st = 0.f, sw = 0.f;
+    for (int yy = 0; yy < s; yy++)
+      for (int xx = 0; xx < s; xx++) {
+        const size_t p = ((size_t)b * H + by * s + yy) * W + bx * s + xx;
+        const float m = mask[p];
+        sy += m * bf(Y[p * C + c]);
+        st += m * T[p * C + c];
+        sw += m;
+      }
+    D[i] = sw > 0.f ? (sy - st) / sw : 0.f;
+    if (c == 0) {
+      wsum[blk] = sw;
+      if (sw > 0.f) atomicAdd(nblk, 1.0);
+    }
+  }
+}
+// Pass 2: loss += lambda * sum D^2 / (nblk * C) over blocks with weight, and
+// dY[p][c] += lambda * 2 D m_p / (w nblk C) (dY in BF16).
+__global__ void k_coarse_apply(bf16 *dY, const float *mask, int B, int H, int W, int C, int s,
+                               const float *D, const float *wsum, const double *nblk, float lambda,
+                               double *loss) {
+  const double inv = *nblk > 0 ? 1.0 / (*nblk * C) : 0.0;
+  const int nbx = W / s, nby = H / s;
+  const size_t P = (size_t)B * H * W, nbc = (size_t)B * nby * nbx * C;
+  double acc = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < P * C; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    const size_t p = i / C;
+    const int x = (int)(p % W), y = (int)((p / W) % H), b = (int)(p / ((size_t)W * H));
+    const int blk = (b * nby + y / s) * nbx + x / s;
+    const float w = wsum[blk];
+    if (w > 0.f) {
+      const float g = lambda * 2.f * D[(size_t)blk * C + c] * mask[p] / w * (float)inv;
+      dY[i] = __float2bfloat16_rn(bf(dY[i]) + g);
+    }
+    if (i < nbc && wsum[i / C] > 0.f) acc += (double)D[i] * D[i];
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, lambda * acc * inv);
+}
+
 // Adam on FP32 master weights, with decoupled weight decay wd (AdamW).
 __global__ void k_adam(float *w, const float *g, float *m, float *v, size_t n, float lr, float b1,
                        float b2, float eps, float c1, float c2, float wd) {
@@ -584,6 +636,7 @@ struct lbm_sg {
   float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
   bf16 *col = nullptr, *colT = nullptr, *dzT = nullptr;
   float *tgt = nullptr, *msk = nullptr, *xin = nullptr, *yout = nullptr;
+  float *coarse_d = nullptr, *coarse_w = nullptr;  // block-mean loss term scratch
   double *loss = nullptr;
   int64_t step = 0;
   cudaStream_t stream = nullptr;
@@ -804,10 +857,19 @@ lbm_status loss_grads(lbm_sg *s, int B, double *loss_out) {
   lbm_status st = forward(s, B);
   if (st != LBM_OK) return st;
   cudaMemsetAsync(s->g, 0, s->nparam * sizeof(float), s->stream);
-  cudaMemsetAsync(s->loss, 0, 2 * sizeof(double), s->stream);  // loss, mask sum
+  cudaMemsetAsync(s->loss, 0, 3 * sizeof(double), s->stream);  // loss, mask sum, block count
   k_mask_sum<<<grid_for(P), 256, 0, s->stream>>>(s->msk, P, s->loss + 1);
   k_mse<<<grid_for(P * c.out_channels), 256, 0, s->stream>>>(s->act[A_OUT].x, s->tgt, s->msk, s->act[A_OUT].dx, P,
                                                            c.out_channels, s->loss + 1, s->loss);
+  if (c.coarse_weight > 0.f) {
+    const int sb = c.coarse_block, nbc = B * (c.height / sb) * (c.width / sb) * c.out_channels;
+    k_coarse_stats<<<grid_for((size_t)nbc), 256, 0, s->stream>>>(
+        s->act[A_OUT].x, s->tgt, s->msk, B, c.height, c.width, c.out_channels, sb, s->coarse_d,
+        s->coarse_w, s->loss + 2);
+    k_coarse_apply<<<grid_for(P * c.out_channels), 256, 0, s->stream>>>(
+        s->act[A_OUT].dx, s->msk, B, c.height, c.width, c.out_channels, sb, s->coarse_d,
+        s->coarse_w, s->loss + 2, c.coarse_weight, s->loss);
+  }
   if ((st = backward(s, B)) != LBM_OK) return st;
   double h = 0;
   cudaMemcpyAsync(&h, s->loss, sizeof h, cudaMemcpyDeviceToHost, s->stream);
@@ -839,6 +901,9 @@ lbm_status lbm_sg_create(const lbm_sg_config *cfg, lbm_sg **out) {
       cfg->max_batch < 1)
     return fail(LBM_INVALID,
                 "surrogate: H, W multiples of 8 (>= 16), base multiple of 8, outputs <= 8 or a multiple of 8");
+  if (cfg->coarse_weight < 0.f ||
+      (cfg->coarse_weight > 0.f && (cfg->coarse_block < 1 || H % cfg->coarse_block || W % cfg->coarse_block)))
+    return fail(LBM_INVALID, "surrogate: coarse_block must divide height and width");
   lbm_sg *s = new lbm_sg();
   s->cfg = *cfg;
   auto bail = [&](lbm_status st) {
@@ -919,8 +984,12 @@ lbm_status lbm_sg_create(const lbm_sg_config *cfg, lbm_sg **out) {
   if ((st = salloc(s, &s->col, max_col)) || (st = salloc(s, &s->colT, max_colT)) ||
       (st = salloc(s, &s->dzT, max_dz)) || (st = salloc(s, &s->tgt, P * co)) ||
       (st = salloc(s, &s->msk, P)) || (st = salloc(s, &s->xin, P * ci)) ||
-      (st = salloc(s, &s->yout, P * co)) || (st = salloc(s, &s->loss, 2)))
+      (st = salloc(s, &s->yout, P * co)) || (st = salloc(s, &s->loss, 3)))
     return bail(st);
+  if (cfg->coarse_weight > 0.f) {
+    const size_t nb = (size_t)B * (H / cfg->coarse_block) * (W / cfg->coarse_block);
+    if ((st = salloc(s, &s->coarse_d, nb * co)) || (st = salloc(s, &s->coarse_w, nb))) return bail(st);
+  }
   refresh_weights(s);
   if (cudaStreamSynchronize(s->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess)
     return bail(fail(LBM_CUDA, "surrogate set-up failed"));

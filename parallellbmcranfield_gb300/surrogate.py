@@ -211,13 +211,15 @@ def cosine_lr(lr, lr_min, epoch, epochs):
     return lr_min + 0.5 * (lr - lr_min) * (1.0 + math.cos(math.pi * epoch / max(1, epochs)))
 
 
-def train(X, Y, M, train_idx, epochs, batch, lr, seed, lr_min=None, weight_decay=0.0):
+def train(X, Y, M, train_idx, epochs, batch, lr, seed, lr_min=None, weight_decay=0.0,
+          coarse_weight=0.0, coarse_block=32):
     """Adam with a cosine learning-rate schedule over the samples train_idx of
     (X, Y, M); returns the network, the mean loss of every epoch and the time."""
     if len(train_idx) == 0:
         raise ValueError("no training samples (no case reached the generation tolerance)")
     net = G.Surrogate(height=GRID, width=GRID, in_channels=X.shape[-1], out_channels=3, base=32,
-                      max_batch=batch, lr=lr, seed=seed, weight_decay=weight_decay)
+                      max_batch=batch, lr=lr, seed=seed, weight_decay=weight_decay,
+                      coarse_weight=coarse_weight, coarse_block=coarse_block)
     net.set_dataset(X, Y, M)
     rng = np.random.default_rng(seed)
     lr_min = lr * 0.02 if lr_min is None else lr_min
@@ -330,6 +332,9 @@ def main(argv=None):
     p.add_argument("--batch", type=int, default=8)
     p.add_argument("--lr", type=float, default=1e-3)
     p.add_argument("--weight-decay", type=float, default=0.01, help="AdamW decay")
+    p.add_argument("--coarse-weight", type=float, default=0.0,
+                   help="weight of the block-mean loss term (large-scale error)")
+    p.add_argument("--coarse-block", type=int, default=32)
     p.add_argument("--eval", type=int, default=400, help="test cases in the warm/cold comparison")
     p.add_argument("--no-augment", action="store_true", help="no mirrored channels in training")
     p.add_argument("--seed", type=int, default=20240601)
@@ -363,7 +368,8 @@ def main(argv=None):
     Xt, Yt, Mt = training_set(cases, X, Y, M, tr, augment=not a.no_augment)
     n_samples = len(Xt)
     net, hist, train_s = train(Xt, Yt, Mt, np.arange(len(Xt)), a.epochs, a.batch, a.lr, a.seed,
-                               weight_decay=a.weight_decay)
+                               weight_decay=a.weight_decay, coarse_weight=a.coarse_weight,
+                               coarse_block=a.coarse_block)
     del Xt, Yt, Mt
     test_mse = masked_mse(net, X, Y, M, te)[0] if len(te) else None
     ev = evaluate(net, cases, meshes, X, Y, M, te[: a.eval], a.max_steps, a.check_every, a.tol)
@@ -373,7 +379,8 @@ def main(argv=None):
                         steps_mean=float(gen["steps"].mean()), max_steps=a.max_steps,
                         check_every=a.check_every, tol=a.gen_tol),
         training=dict(cases=len(tr), samples=n_samples, epochs=a.epochs, batch=a.batch,
-                      lr=a.lr, weight_decay=a.weight_decay,
+                      lr=a.lr, weight_decay=a.weight_decay, coarse_weight=a.coarse_weight,
+                      coarse_block=a.coarse_block,
                       seconds=train_s, loss_first=hist[0], loss_last=hist[-1],
                       params=net.num_params, history=hist),
         test_mse=test_mse, tol=a.tol, warm_vs_cold=ev)

@@ -16,7 +16,7 @@ def sample(seed=1, B=2, h=H, cin=CIN):
     return x, t, m
 
 
-def torch_grads(params, x, t, m):
+def torch_grads(params, x, t, m, coarse=None):
     torch = pytest.importorskip("torch")
     F = torch.nn.functional
     P = torch.tensor(params, dtype=torch.float64, requires_grad=True)
@@ -48,7 +48,16 @@ def torch_grads(params, x, t, m):
     d0 = conv(13, conv(12, torch.cat([up(d1), e0], 1)))
     y = conv(14, d0).permute(0, 2, 3, 1)
     M = torch.tensor(m)[..., None]
-    loss = (M * (y - torch.tensor(t)) ** 2).sum() / (M.sum() * COUT)
+    T = torch.tensor(t)
+    loss = (M * (y - T) ** 2).sum() / (M.sum() * COUT)
+    if coarse is not None:
+        lam, s = coarse
+        B, Hh, Ww, C = y.shape
+        blk = lambda a: a.reshape(B, Hh // s, s, Ww // s, s, -1).sum(dim=(2, 4))
+        w = blk(M)
+        ok = (w > 0).squeeze(-1)
+        D = (blk(M * y) - blk(M * T)) / torch.where(w > 0, w, torch.ones_like(w))
+        loss = loss + lam * (D[ok] ** 2).sum() / (ok.sum() * C)
     loss.backward()
     return loss.item(), y.detach().numpy(), P.grad.numpy()
 
@@ -63,6 +72,17 @@ def test_oracle_matches_torch_autograd():
     assert np.abs(g - tg).max() <= 1e-10 * np.abs(tg).max()
 
 
+def test_oracle_coarse_term_matches_torch_autograd():
+    """The block-mean loss term of the oracle (mirrored by the GPU kernels)."""
+    params = SO.init_params(CIN, COUT, BASE, seed=4)
+    x, t, m = sample(seed=5)
+    m[0, :4, :4] = 0.0  # one block without fluid
+    loss, y, g = SO.Net(params, CIN, COUT, BASE).loss_grads(x, t, m, coarse=(2.0, 4))
+    tl, ty, tg = torch_grads(params, x, t, m, coarse=(2.0, 4))
+    assert abs(loss - tl) <= 1e-12 * abs(tl)
+    assert np.abs(g - tg).max() <= 1e-10 * np.abs(tg).max()
+
+
 def test_bf16_rounding_helper():
     v = np.array([1.0, 1.00390625, 1.005859375, -3.14159, 0.0])
     r = SO.to_bf16(v)
@@ -72,8 +92,9 @@ def test_bf16_rounding_helper():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("cin,base,h", [(CIN, BASE, H), (7, 32, 32), (8, 32, 32)])
-def test_gpu_gradients_match_oracle(cin, base, h):
+@pytest.mark.parametrize("cin,base,h,coarse", [(CIN, BASE, H, 0.0), (7, 32, 32, 0.0),
+                                               (8, 32, 32, 0.0), (CIN, BASE, H, 2.0)])
+def test_gpu_gradients_match_oracle(cin, base, h, coarse):
     """4 or 7 input channels: the first layer's products use an explicit im2col
     in memory; every layer with a multiple of 8 channels (all of them at 8
     inputs) uses the implicit-im2col forward/input-gradient products and the
@@ -81,11 +102,12 @@ def test_gpu_gradients_match_oracle(cin, base, h):
     import parallellbmcranfield_gb300 as G
 
     s = G.Surrogate(height=h, width=h, in_channels=cin, out_channels=COUT, base=base, max_batch=2,
-                    seed=5)
+                    seed=5, coarse_weight=coarse, coarse_block=4)
     params = s.params().astype(np.float64)
     x, t, m = sample(seed=2, h=h, cin=cin)
     loss, g = s.loss_grads(x, t, m)
-    oloss, oy, og = SO.Net(params, cin, COUT, base, bf16=True).loss_grads(x, t, m)
+    oloss, oy, og = SO.Net(params, cin, COUT, base, bf16=True).loss_grads(
+        x, t, m, coarse=(coarse, 4) if coarse else None)
     y = s.forward(x)
     assert np.abs(y - oy).max() <= 2e-2 * np.abs(oy).max()
     assert abs(loss - oloss) <= 2e-2 * oloss

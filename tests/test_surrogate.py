@@ -240,3 +240,17 @@ def test_pipeline_host_logic():
     assert (x2 == x).all() and (y2 == y).all() and (m2 == m).all()
     assert S.cosine_lr(1e-3, 2e-5, 0, 10) == 1e-3
     assert abs(S.cosine_lr(1e-3, 2e-5, 10, 10) - 2e-5) < 1e-12
+
+
+def test_config_validation_on_the_host():
+    """Bad network shapes are refused before any device work (CPU)."""
+    import parallellbmcranfield_gb300 as G
+
+    bad = [dict(height=30, width=32), dict(base=12), dict(out_channels=9),
+           dict(coarse_weight=1.0, coarse_block=5), dict(coarse_weight=-1.0)]
+    for kw in bad:
+        args = dict(height=32, width=32, in_channels=4, out_channels=3, base=8, max_batch=2)
+        args.update(kw)
+        with pytest.raises(G.LbmError) as e:
+            G.Surrogate(**args)
+        assert e.value.status == G.LBM_INVALID, kw

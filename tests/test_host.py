@@ -135,3 +135,17 @@ def test_generator_reproduces_shipped_cavity(case, side):
     assert np.array_equal(a["cls"], b["cls"])
     assert np.array_equal(a["flags"], b["flags"])
     assert np.abs(a["q"] - b["q"]).max() < 1e-4
+
+
+def test_batch_arguments_are_checked_on_the_host():
+    """A batch shares precision, model and pattern; the library refuses mixtures
+    before any device work (CPU)."""
+    base = dict(uavg=0.05, vavg=0.0, rho_ini=1.0, viscosity=0.05, inlet_profile=2,
+                curved_boundaries=1, outlet_profile=2)
+    mesh = G.Mesh.cavity(20)
+    with pytest.raises(G.LbmError) as e:
+        G.Batch([(mesh, dict(base, collision_model=1)), (mesh, dict(base, collision_model=3))])
+    assert e.value.status == G.LBM_INVALID
+    with pytest.raises(G.LbmError) as e:
+        G.Batch([(mesh, dict(base, collision_model=2))], precision="bf16dev")
+    assert e.value.status == G.LBM_INVALID

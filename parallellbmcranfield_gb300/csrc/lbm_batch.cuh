@@ -1,8 +1,9 @@
-// Batched stepping of many independent domains (cavities, channels) with one
-// launch per step: a device-side work list of (case, tile) is walked by a
-// persistent grid; per-case parity, step counters and convergence flags live
-// on the device so that a whole run segment (steps + check) can be captured
-// in one CUDA graph.
+// Batched stepping of many independent domains (cavities, channels): per step
+// one persistent bulk launch walks a device-side work list of (case, tile),
+// and a second launch, alongside it, the list of (case, node) with boundary
+// work; per-case parity, step counters and convergence flags live on the
+// device so that a whole run segment (steps + check) can be captured in one
+// CUDA graph.
 #pragma once
 #include "lbm_device.cuh"
 

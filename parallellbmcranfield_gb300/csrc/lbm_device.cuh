@@ -1,6 +1,6 @@
 // Device code of the fused D2Q9 step: storage policies, collision models,
-// boundary handling, and the kernel templates instantiated per precision in
-// lbm_kernels_<precision>.cu.
+// boundary handling, and the kernel templates instantiated per precision and
+// collision model by lbm_kernels_inst.cu (compiled once per combination).
 //
 // State convention.  The population state between launches is the
 // post-collision field METAF_t of the reference cells (serial/CellFunctions.c

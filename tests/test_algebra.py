@@ -1,0 +1,91 @@
+"""CPU: the folded-constant MRT operator of the two-node 16-bit kernel
+(collide_mrt_pair_raw: raw stored values in, raw values out) is the same map
+as the deviation-form MRT of the scalar kernels (collide_bulk_dev, model 3).
+Both are restated here in float64 from the device code."""
+import numpy as np
+
+C36W = np.array([16, 4, 4, 4, 4, 1, 1, 1, 1], float)  # 36 w_k
+
+
+def mrt_dev(F, rho0, om):
+    """collide_bulk_dev<3>: deviations d_k = f_k - w_k rho0 in and out."""
+    a13, a24 = F[1] + F[3], F[2] + F[4]
+    a14 = a13 + a24
+    p57, p68 = F[5] + F[7], F[6] + F[8]
+    a58 = p57 + p68
+    rt = (F[0] + a14) + a58
+    rho = rho0 + rt
+    m1 = 2 * a58 - a14 - 4 * F[0]
+    m2 = (4 * F[0] + a58) - 2 * a14
+    d13, d24 = F[1] - F[3], F[2] - F[4]
+    e57, e86 = F[5] - F[7], F[8] - F[6]
+    x58, y58 = e57 + e86, e57 - e86
+    jx, jy = d13 + x58, d24 + y58
+    m4, m6 = x58 - 2 * d13, y58 - 2 * d24
+    m7, m8 = a13 - a24, p57 - p68
+    inv = 1 / rho
+    jj = jx * jx + jy * jy
+    d1 = 1.4 * (m1 + 2 * rt - 3 * jj)
+    d2 = 1.4 * (m2 - rt + 3 * jj)
+    d4 = 1.2 * (m4 + jx)
+    d6 = 1.2 * (m6 + jy)
+    d7 = om * (m7 - (jx * jx - jy * jy) * inv)
+    d8 = om * (m8 - jx * jy * inv)
+    c = 1 / 36
+    ax, dg = -d1 - 2 * d2, 2 * d1 + d2
+    X, Y, P = -6 * d4, -6 * d6, 9 * d7
+    Xd, Yd, Q = 3 * d4, 3 * d6, 9 * d8
+    return np.array([
+        F[0] - c * (4 * (d2 - d1)),
+        F[1] - c * (ax + X + P), F[2] - c * (ax + Y - P),
+        F[3] - c * (ax - X + P), F[4] - c * (ax - Y - P),
+        F[5] - c * (dg + Xd + Yd + Q), F[6] - c * (dg - Xd + Yd - Q),
+        F[7] - c * (dg - Xd - Yd + Q), F[8] - c * (dg + Xd - Yd - Q)])
+
+
+def mrt_raw(S, rho0, om, u0):
+    """collide_mrt_pair_raw: stored values s_k = d_k / (36 w_k u0) in and out."""
+    t13, t24 = S[1] + S[3], S[2] + S[4]
+    t14 = t13 + t24
+    p57, p68 = S[5] + S[7], S[6] + S[8]
+    a58 = p57 + p68
+    rt = 16 * S[0] + (4 * t14 + a58)
+    rho = u0 * rt + rho0
+    u13, u24 = S[1] - S[3], S[2] - S[4]
+    e57, e86 = S[5] - S[7], S[8] - S[6]
+    x58, y58 = e57 + e86, e57 - e86
+    jx, jy = 4 * u13 + x58, 4 * u24 + y58
+    E4, E6 = -2 * u13 + x58, -2 * u24 + y58
+    w7, m8 = t13 - t24, p57 - p68
+    jj = jx * jx + jy * jy
+    ninv = -u0 / rho
+    g1 = -3 * u0 * jj + (-32 * S[0] + 4 * (a58 + t14))
+    g2 = 3 * u0 * jj + (48 * S[0] - 12 * t14)
+    h7 = (jx - jy) * (jx + jy) * ninv + 4 * w7
+    h8 = jx * jy * ninv + m8
+    P4, Q = om / 16 * h7, 0.25 * om * h8
+    A4 = -1.4 / 144 * (2 * g2 + g1)
+    D = 1.4 / 36 * (2 * g1 + g2)
+    ApP, AmP, DpQ, DmQ = A4 + P4, A4 - P4, D + Q, D - Q
+    S46, T46 = E4 + E6, E4 - E6
+    return np.array([
+        -5.6 / 576 * (g2 - g1) + S[0],
+        0.1 * E4 + (S[1] - ApP), 0.1 * E6 + (S[2] - AmP),
+        -0.1 * E4 + (S[3] - ApP), -0.1 * E6 + (S[4] - AmP),
+        -0.2 * S46 + (S[5] - DpQ), 0.2 * T46 + (S[6] - DmQ),
+        0.2 * S46 + (S[7] - DpQ), -0.2 * T46 + (S[8] - DmQ)])
+
+
+def test_folded_raw_operator_equals_deviation_operator():
+    rng = np.random.default_rng(7)
+    for rho0 in (1.0, 2.5):
+        for S_scale in (4096.0, 1.0):  # FP16 and BF16 scales
+            u0 = rho0 / (36 * S_scale)
+            for om in (1.9, 1.2):
+                w = C36W / 36
+                # deviations of a flow with |u| ~ 0.1 and small non-equilibrium parts
+                d = w[:, None] * rho0 * rng.normal(0, 0.3, (9, 500))
+                ref = mrt_dev(d, rho0, om)
+                s = d / (C36W[:, None] * u0)
+                got = mrt_raw(s, rho0, om, u0) * (C36W[:, None] * u0)
+                assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()

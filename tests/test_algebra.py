@@ -1,7 +1,15 @@
-"""CPU: the folded-constant MRT operator of the two-node 16-bit kernel
-(collide_mrt_pair_raw: raw stored values in, raw values out) is the same map
-as the deviation-form MRT of the scalar kernels (collide_bulk_dev, model 3).
-Both are restated here in float64 from the device code."""
+"""CPU: the reduced-precision MRT operators are the reference's MRT.
+
+* The deviation-form MRT of the FP32/16-bit kernels (collide_bulk_dev, model
+  3) equals the reference's moment-space MRT (serial/CellFunctions.c:401-438
+  with MRTInitializer's relaxation rates, serial/CellFunctions.c:60-90) applied
+  to f = d + w rho0; likewise BGK and TRT (serial/CellFunctions.c:352-395; the
+  reference's float rounding of the TRT split terms is kept by the FP64 path
+  only, so the comparison here is in exact arithmetic).
+* The folded-constant operator of the two-node 16-bit kernel
+  (collide_mrt_pair_raw: raw stored values in and out) equals the
+  deviation-form one.
+Each is restated here in float64 from its source."""
 import numpy as np
 
 C36W = np.array([16, 4, 4, 4, 4, 1, 1, 1, 1], float)  # 36 w_k
@@ -74,6 +82,81 @@ def mrt_raw(S, rho0, om, u0):
         -0.1 * E4 + (S[3] - ApP), -0.1 * E6 + (S[4] - AmP),
         -0.2 * S46 + (S[5] - DpQ), 0.2 * T46 + (S[6] - DmQ),
         0.2 * S46 + (S[7] - DpQ), -0.2 * T46 + (S[8] - DmQ)])
+
+
+# the reference's MRT transform and its inverse (x 36), serial/CellFunctions.c:24-47
+TM = np.array([[1, 1, 1, 1, 1, 1, 1, 1, 1], [-4, -1, -1, -1, -1, 2, 2, 2, 2],
+               [4, -2, -2, -2, -2, 1, 1, 1, 1], [0, 1, 0, -1, 0, 1, -1, -1, 1],
+               [0, -2, 0, 2, 0, 1, -1, -1, 1], [0, 0, 1, 0, -1, 1, 1, -1, -1],
+               [0, 0, -2, 0, 2, 1, 1, -1, -1], [0, 1, -1, 1, -1, 0, 0, 0, 0],
+               [0, 0, 0, 0, 0, 1, -1, 1, -1]], float)
+CX = np.array([0, 1, 0, -1, 0, 1, -1, -1, 1], float)
+CY = np.array([0, 0, 1, 0, -1, 1, 1, -1, -1], float)
+
+
+def mrt_reference(f, om):
+    """Moment-space MRT on absolute populations: f - Minv S (M f - m_eq)."""
+    R = f.sum(0)
+    U, V = (CX[:, None] * f).sum(0) / R, (CY[:, None] * f).sum(0) / R
+    meq = np.array([R, R * (-2 + 3 * R * (U * U + V * V)), R * (1 - 3 * R * (U * U + V * V)),
+                    R * U, -R * U, R * V, -R * V, R * (U * U - V * V), R * U * V])
+    S = np.diag([1.0, 1.4, 1.4, 1.0, 1.2, 1.0, 1.2, om, om])
+    return f - np.linalg.inv(TM) @ S @ (TM @ f - meq)
+
+
+def test_deviation_operator_equals_reference_mrt():
+    rng = np.random.default_rng(3)
+    w = C36W / 36
+    for rho0 in (1.0, 5.0):
+        for om in (1.9, 1.1):
+            d = w[:, None] * rho0 * rng.normal(0, 0.3, (9, 400))
+            f = d + w[:, None] * rho0
+            ref = mrt_reference(f, om) - w[:, None] * rho0
+            got = mrt_dev(d, rho0, om)
+            assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+OPP = [0, 3, 4, 1, 2, 7, 8, 5, 6]
+
+
+def feq_abs(f):
+    R = f.sum(0)
+    U, V = (CX[:, None] * f).sum(0) / R, (CY[:, None] * f).sum(0) / R
+    w = C36W / 36
+    cu = CX[:, None] * U + CY[:, None] * V
+    return R * w[:, None] * (1 + 3 * cu + 4.5 * cu ** 2 - 1.5 * (U * U + V * V))
+
+
+def bgk_trt_dev(F, rho0, om, omA, model):
+    """collide_bulk_dev, models 1 (BGK) and 2 (TRT), on deviations."""
+    rt = F.sum(0)
+    jx, jy = (CX[:, None] * F).sum(0), (CY[:, None] * F).sum(0)
+    rho = rho0 + rt
+    u, v = jx / rho, jy / rho
+    w = C36W / 36
+    T2 = CX[:, None] * u + CY[:, None] * v
+    feq = w[:, None] * (rt + rho * (3 * T2 + 4.5 * T2 * T2 - 1.5 * (u * u + v * v)))
+    if model == 1:
+        return om * (feq - F) + F
+    sp = 0.5 * ((F + F[OPP]) - (feq + feq[OPP]))
+    sm = 0.5 * ((F - F[OPP]) - (feq - feq[OPP]))
+    return F - om * sp - omA * sm
+
+
+def test_deviation_bgk_trt_equal_reference():
+    rng = np.random.default_rng(11)
+    w = C36W / 36
+    for rho0 in (1.0, 5.0):
+        om = 1.7
+        omA = 8 * (2 - om) / (8 - om)  # serial/Iterate.c:180
+        d = w[:, None] * rho0 * rng.normal(0, 0.3, (9, 400))
+        f = d + w[:, None] * rho0
+        fe = feq_abs(f)
+        bgk = om * fe + (1 - om) * f
+        trt = f - 0.5 * ((f + f[OPP]) - (fe + fe[OPP])) * om - 0.5 * ((f - f[OPP]) - (fe - fe[OPP])) * omA
+        for model, ref in ((1, bgk), (2, trt)):
+            got = bgk_trt_dev(d, rho0, om, omA, model) + w[:, None] * rho0
+            assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max(), model
 
 
 def test_folded_raw_operator_equals_deviation_operator():

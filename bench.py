@@ -206,13 +206,18 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+ELEM_BYTES = {"fp64": 8, "fp32": 4, "fp16dev": 2, "bf16dev": 2}
+
+
 def workload_config(args, side):
     n, m = side + 2, side + 3
+    pop_gb = n * m * 9 * ELEM_BYTES[args.precision] * (2 if args.pattern == "ab" else 1) / 1e9
     return {"workload": f"lid-driven cavity {n}x{m} nodes ({side}^2 fluid), lid u=0.05, Re=10000, "
                         f"D2Q9 MRT, {args.precision} {args.pattern.upper()}",
             "nodes": n * m, "fluid_nodes": side * side, "precision": args.precision,
             "pattern": args.pattern, "collision_model": args.model,
-            "l2_flush": "inputs larger than L2 (populations 19.3 GB at fp32 A-B)"}
+            "l2_flush": f"inputs larger than L2 (populations {pop_gb:.2f} GB, L2 0.13 GB)"
+                        if pop_gb > 0.129 else "inputs fit in L2: no flush (small case)"}
 
 
 def load_traffic(precision, pattern, model):

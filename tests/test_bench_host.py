@@ -1,0 +1,31 @@
+"""bench.py host helpers on CPU: the clock record, the workload description,
+the committed traffic figures."""
+import os
+import sys
+import types
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+import bench  # noqa: E402
+
+
+def test_clock_summary_flags_throttle_reasons(tmp_path):
+    c = bench.ClockSampler(0)
+    c.f.write("0, 2070, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active\n"
+              "0, 2055, 2070, 1400.0, 0x4, Not Active, Not Active, Not Active, Active\n"
+              "0, 2070, 2070, 1390.0, 0x4, Not Active, Not Active, Not Active, Active\n")
+    r = c.summary()
+    assert r["sm_mhz"] == 2070.0 and r["sm_max_mhz"] == 2070.0 and r["samples"] == 3
+    assert r["reasons"] == ["sw_power_cap"]
+
+
+def test_workload_config_and_traffic():
+    a = types.SimpleNamespace(precision="fp32", pattern="ab", model=3)
+    cfg = bench.workload_config(a, 16382)
+    assert cfg["nodes"] == 16384 * 16385 and cfg["fluid_nodes"] == 16382 ** 2
+    assert "19.33 GB" in cfg["l2_flush"]
+    a.precision = "fp16dev"
+    assert "9.66 GB" in bench.workload_config(a, 16382)["l2_flush"]
+    t = bench.load_traffic("fp32", "ab", 3)
+    assert 0.95 < t / (72 * 16384 * 16385) < 1.0  # measured bytes per launch vs algorithmic
+    assert bench.load_traffic("fp64", "aa", 1) is None

@@ -176,8 +176,10 @@ lbm_status lbm_inspect_mesh(const lbm_mesh *mesh, const lbm_params *params, int3
 /* ---------------------------------------------------------------------------
  * Batches.  No counterpart in the reference, which runs one case per process:
  * many independent domains (cavities, channels of different sizes and
- * parameters) advanced together by one persistent launch per step over a
- * device-side list of (case, tile).  Per-case convergence flags live on the
+ * parameters) advanced together: per step one persistent launch over a
+ * device-side list of (case, tile), and alongside it one over the (case, node)
+ * list of boundary nodes; both lists are compacted to the cases still stepping
+ * at the start of every run segment.  Per-case convergence flags live on the
  * device; each run segment (check_every steps and one check) is one CUDA graph
  * replay.  All cases share precision (FP64, FP32 or FP16-dev), the A-B pattern,
  * the collision model and the device; everything else is per case.

@@ -254,3 +254,21 @@ def test_config_validation_on_the_host():
         with pytest.raises(G.LbmError) as e:
             G.Surrogate(**args)
         assert e.value.status == G.LBM_INVALID, kw
+
+
+def test_gap_flow_of_an_empty_channel_is_the_inlet_parabola():
+    """Without cylinders every column is one gap of the full width: the
+    estimate is the parabolic profile with peak 1.5 x the mean speed (CPU)."""
+    from parallellbmcranfield_gb300 import surrogate as S
+
+    umax = 0.08
+    case = dict(kind="channel", U=umax, params=dict(uavg=umax / 1.5))
+    fl = np.zeros((S.GRID, S.GRID), np.float32)
+    fl[1:-1, 1:-1] = 1.0
+    g = S.gap_flow(case, fl)
+    h = S.GRID - 2
+    s = (np.arange(h) + 0.5) / h
+    want = 6.0 * (umax / 1.5) * s * (1 - s) / umax
+    assert np.allclose(g[1:-1, 128], want, rtol=1e-6)
+    assert abs(g[1:-1, 128].max() - 1.0) < 1e-3  # peak = umax
+    assert (g[0] == 0).all() and (g[:, 0] == 0).all()

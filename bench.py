@@ -3,7 +3,9 @@
 Workload (the large single cavity): a lid-driven cavity of 16382^2 fluid
 cells in a 16384 x 16385 node array (268.4 M nodes), lid u = 0.05,
 Re = 10000 (nu = u L / Re), MRT collision, FP32 populations, A-B pattern,
-started from f = f_eq at rest.  A step is one time step over the whole array.
+started from f = f_eq at rest.  A step is one iteration of the reference's
+loop body over the whole array: the fused step kernel plus the reference's
+residual line (serial/Iterate.c:263-307).
 
   value   MLUPS = nodes x steps / device time of the timed steps (CUDA events
           on the solver's stream; state resident in HBM; 19.3 GB of
@@ -11,8 +13,11 @@ started from f = f_eq at rest.  A step is one time step over the whole array.
   e2e     the same job through the C ABI with host buffers: lbm_set_state
           from pinned host rho/u/v, K x lbm_step(1) with the reference's
           per-step residual line copied back, lbm_get_fields to host
-  roofline  algorithmic bytes 72 B/node/step (9 FP32 loads + 9 stores) per
-          launch / average launch time, against the measured HBM copy peak
+  roofline  algorithmic bytes per node and step (FP32: 9 loads + 9 stores of
+          4 bytes = 72 B) x nodes / average duration of the step kernel alone
+          (a second timed run without residual lines), against the measured
+          HBM copy peak
+  variants  the other storages and patterns of the same cavity (AA, 16-bit)
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
   torchrun --nproc-per-node N bench.py --gpus N ...   (N replicas, one per GPU)
@@ -36,6 +41,8 @@ PREC_NAME = {0: "fp64", 1: "fp32", 2: "fp16dev", 3: "bf16dev"}
 DTYPE = {0: "f64", 1: "f32", 2: "f16 storage, f32 compute", 3: "bf16 storage, f32 compute"}
 BYTES = {0: 144, 1: 72, 2: 36, 3: 36}
 CPU_SAMPLE_SIDE = 1022  # 1024 x 1025 node cavity for the CPU legs
+VARIANTS = (("fp32", "aa"), ("fp16dev", "ab"), ("fp16dev", "aa"), ("bf16dev", "ab"),
+            ("bf16dev", "aa"))
 
 
 def parse():
@@ -49,12 +56,39 @@ def parse():
     p.add_argument("--pattern", default="ab", choices=["ab", "aa"])
     p.add_argument("--model", type=int, default=3)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--cpu-side", type=int, default=CPU_SAMPLE_SIDE,
+                   help="fluid cells per side of the CPU sample cavity")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--tile", type=int, default=0,
-                   help="fused-step tile variant 1..4; 0 = autotune")
-    p.add_argument("--variants", action="store_true",
-                   help="also time AA and 16-bit storage (fewer steps)")
+                   help="fused-step tile variant 1..6; 0 = autotune")
+    p.add_argument("--no-variants", action="store_true",
+                   help="skip the AA and 16-bit storage variants of the cavity")
     return p.parse_args()
+
+
+def host_info():
+    """CPU model string and logical core count of this host."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() in ("Model name", "Model"):
+                val = line.split(":", 1)[1].strip()
+                if val and not val.isdigit():
+                    model = val
+                    break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if model is None:
+        try:
+            with open("/proc/cpuinfo") as fh:
+                for line in fh:
+                    if line.lower().startswith(("model name", "cpu part")):
+                        model = line.split(":", 1)[1].strip()
+                        break
+        except OSError:
+            pass
+    return {"cpu_model": model or "unknown", "nproc": os.cpu_count()}
 
 
 def dist_setup():
@@ -144,20 +178,29 @@ def feq_rest(rho0, N):
     return np.tile(rho0 * W9, (N, 1))
 
 
-def cpu_port_mlups(side, model, seconds, steps=None):
-    """The oracle (C restatement of the serial reference, 1 thread) on a cavity sample."""
-    import parallellbmcranfield_gb300 as G
+def _port_sample(side, model):
+    """The oracle port on a side^2 cavity at rest, after its first collision.
+    The mesh comes from numpy (oracle.meshgen): no GPU library is loaded."""
+    from oracle import meshgen
     from oracle import oracle as O
 
-    O.build(ref=False)
-    mesh = G.Mesh.cavity(side)
+    nodes, conns, (n, m) = meshgen.cavity(side)
     nu = 0.05 * side / 10000.0
-    port = O.Port(mesh.nodes, mesh.conns, uavg=0.05, vavg=0.0, rho_ini=1.0, viscosity=nu,
+    port = O.Port(nodes, conns, uavg=0.05, vavg=0.0, rho_ini=1.0, viscosity=nu,
                   inlet_profile=2, model=model, curved=1, outlet=2)
-    n, m = mesh.shape
     N = n * m
     port.set_state(feq_rest(1.0, N), np.ones(N), np.zeros(N), np.zeros(N))
     port.run(1, want_resid=False)
+    return port, N
+
+
+def cpu_port_mlups(side, model, seconds, steps=None):
+    """The oracle (C restatement of the serial reference, 1 thread) on a cavity
+    sample, one step and the reference's residual line at a time."""
+    from oracle import oracle as O
+
+    O.build(ref=False)
+    port, N = _port_sample(side, model)
     done, t0 = 0, time.perf_counter()
     while True:
         port.run(1, want_resid=True)
@@ -169,37 +212,60 @@ def cpu_port_mlups(side, model, seconds, steps=None):
     return N * done / el / 1e6, N, done, el
 
 
+def _replica(job):
+    """One CPU core's share of the reference arm: warm-up, then the timed steps."""
+    side, model, warmup, steps = job
+    port, N = _port_sample(side, model)
+    port.run(warmup, want_resid=True)
+    t0 = time.perf_counter()
+    port.run(steps, want_resid=True)
+    el = time.perf_counter() - t0
+    port.close()
+    return N, el
+
+
 def reference_arm(args):
+    """The reference's own CPU arithmetic (the oracle port, bit-identical to the
+    serial code) on every host core: one independent cavity per core, as the
+    serial program is single-threaded.  It loads nothing of the GPU library."""
+    import multiprocessing as mp
+
     ws, rank, _ = dist_setup()
     if rank != 0:
         return
-    import parallellbmcranfield_gb300 as G  # noqa: F401  (mesh generator)
     from oracle import oracle as O
 
     O.build(ref=False)
-    side = CPU_SAMPLE_SIDE
-    mesh = G.Mesh.cavity(side)
-    nu = 0.05 * side / 10000.0
-    port = O.Port(mesh.nodes, mesh.conns, uavg=0.05, vavg=0.0, rho_ini=1.0, viscosity=nu,
-                  inlet_profile=2, model=args.model, curved=1, outlet=2)
-    n, m = mesh.shape
-    N = n * m
-    port.set_state(feq_rest(1.0, N), np.ones(N), np.zeros(N), np.zeros(N))
-    port.run(args.warmup, want_resid=True)
-    t0 = time.perf_counter()
-    port.run(args.steps, want_resid=True)
-    el = time.perf_counter() - t0
-    mlups = N * args.steps / el / 1e6
-    sample = (f"cavity {n}x{m} nodes (fluid {side}^2), MRT, FP64, lid 0.05, Re 10000, "
-              f"{args.steps} steps after {args.warmup} warm-up; per-step residual as the serial loop")
+    host = host_info()
+    cores = host["nproc"] or 1
+    side = args.cpu_side
+    with mp.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(_replica, [(side, args.model, args.warmup, args.steps)] * cores)
+    N = res[0][0]
+    el_max = max(el for _, el in res)
+    mlups = cores * N * args.steps / el_max / 1e6
+    n, m = side + 2, side + 3
+    sample = (f"oracle port (the serial reference's arithmetic, bit-identical; 528-byte cells, five "
+              f"sweeps) on {cores} independent {n}x{m}-node cavities, one per host core "
+              f"({host['cpu_model']}, nproc {host['nproc']}), {args.steps} steps each after "
+              f"{args.warmup} warm-up, per-step residual line as the serial loop; whole-host MLUPS "
+              f"timed by the slowest core")
     line = {
         "impl": "reference", "metric": "MLUPS", "value": round(mlups, 3), "unit": "MLUPS",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(el / args.steps * 1e3, 3), "higher_is_better": True,
+        "ms_per_step": round(el_max / args.steps * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": workload_config(args, args.side),
-        "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": 1, "kind": "port",
-                         "sample": sample},
+        "config": {"workload": f"lid-driven cavity {n}x{m} nodes ({side}^2 fluid), lid u=0.05, "
+                               f"Re=10000, D2Q9 MRT, FP64 as the serial reference, x{cores} "
+                               f"(one per host core); CPU sample of the GPU arm's "
+                               f"{args.side + 2}x{args.side + 3} cavity, which does not fit "
+                               f"the reference's 528-byte cells in host memory",
+                   "nodes": n * m * cores, "fluid_nodes": side * side * cores,
+                   "precision": "fp64", "collision_model": args.model, "replicas": cores,
+                   "l2_flush": f"CPU run: each cavity holds {n * m * 528 / 1e9:.3f} GB of "
+                               f"528-byte cells"},
+        "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": cores,
+                         "kind": "port", "sample": sample, "host": host},
         "e2e": {"value": round(mlups, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -239,6 +305,35 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+def cavity_solver(G, side, prec_name, pat_name, model, local, stream, tile=0):
+    mesh = G.Mesh.cavity(side)
+    s = G.Solver(mesh, uavg=0.05, vavg=0.0, rho_ini=1.0, viscosity=0.05 * side / 10000.0,
+                 inlet_profile=2, collision_model=model, curved_boundaries=1, outlet_profile=2,
+                 precision=G.PRECISIONS[prec_name], pattern=G.PATTERNS[pat_name], device=local,
+                 stream=stream.cuda_stream, tile_variant=tile)
+    del mesh
+    return s
+
+
+def timed_steps(torch, dev, stream, solver, steps, check_every, local=0, clocks=False):
+    """Device time (ms) of `steps` lbm_step iterations on the solver's stream,
+    with nvidia-smi sampling the clocks meanwhile when asked."""
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clk = ClockSampler(local) if clocks else None
+    if clk:
+        clk.__enter__()
+    try:
+        torch.cuda.synchronize(dev)
+        ev0.record(stream)
+        solver.step(steps, check_every)
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+    finally:
+        if clk:
+            clk.__exit__()
+    return ev0.elapsed_time(ev1), (clk.summary() if clk else None)
+
+
 def run_gpu(args):
     import torch
 
@@ -248,20 +343,13 @@ def run_gpu(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     prec = G.PRECISIONS[args.precision]
-    pat = G.PATTERNS[args.pattern]
     side = args.side
-    nu = 0.05 * side / 10000.0
     t_setup = time.perf_counter()
-    mesh = G.Mesh.cavity(side)
-    n, m = mesh.shape
-    N = n * m
     stream = torch.cuda.Stream(device=dev)
-    solver = G.Solver(mesh, uavg=0.05, vavg=0.0, rho_ini=1.0, viscosity=nu, inlet_profile=2,
-                      collision_model=args.model, curved_boundaries=1, outlet_profile=2,
-                      precision=prec, pattern=pat, device=local, stream=stream.cuda_stream,
-                      tile_variant=args.tile)
-    del mesh
-    tune = solver.autotune(5) if args.tile == 0 else {"variant": args.tile - 1, "fixed": True}
+    solver = cavity_solver(G, side, args.precision, args.pattern, args.model, local, stream,
+                           args.tile)
+    N = solver.N
+    tune = solver.autotune(10) if args.tile == 0 else {"variant": args.tile - 1, "fixed": True}
     # pinned host state: f = f_eq at rest is formed on the device from rho/u/v
     rho_h = torch.ones(N, dtype=torch.float64, pin_memory=True)
     u_h = torch.zeros(N, dtype=torch.float64, pin_memory=True)
@@ -269,24 +357,19 @@ def run_gpu(args):
     solver.set_state(None, rho_h.numpy(), u_h.numpy(), v_h.numpy())
     setup_s = time.perf_counter() - t_setup
 
-    # ---- device-resident throughput
-    solver.step(args.warmup, 0)
+    # ---- device-resident throughput: the loop body of the reference (fused
+    # step + residual line every step)
+    solver.step(args.warmup, 1)
     torch.cuda.synchronize(dev)
     barrier(ws)
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        torch.cuda.synchronize(dev)
-        ev0.record(stream)
-        solver.step(args.steps, 0)
-        ev1.record(stream)
-        torch.cuda.synchronize(dev)
-    ms = ev0.elapsed_time(ev1)
+    ms, clocks = timed_steps(torch, dev, stream, solver, args.steps, 1, local, clocks=True)
     barrier(ws)
     ms_max = max_over_ranks(ws, ms, dev)
-    clocks = clk.summary()
-    launches = args.steps  # one fused step kernel per step, nothing else in the timed region
+    launches = 2 * args.steps  # per step: the fused step kernel and the residual kernel
     mlups = job_mlups(ws, N, args.steps, ms_max)
-    per_launch_s = ms / 1e3 / args.steps
+    # ---- the step kernel alone (roofline)
+    ms_k, _ = timed_steps(torch, dev, stream, solver, args.steps, 0)
+    per_launch_s = ms_k / 1e3 / args.steps
     bpn = BYTES[prec]
     achieved = bpn * N / per_launch_s / 1e9
     peak, peak_kind = measured_peak()
@@ -317,34 +400,48 @@ def run_gpu(args):
                "d2h_bytes_per_step": int(32 + 3 * 8 * N / args.steps),
                "what": "lbm_set_state(host rho,u,v) + steps x lbm_step(1, residual line) + "
                        "lbm_get_fields(host rho,u,v), wall clock"}
+    solver.close()
 
     variants = {}
-    if args.variants:
-        solver.close()
-        for vp, vpat in (("fp32", "aa"), ("fp16dev", "ab"), ("fp16dev", "aa"), ("bf16dev", "aa")):
-            variants[f"{vp}_{vpat}"] = time_variant(args, G, torch, dev, stream, local, vp, vpat)
-    else:
-        solver.close()
+    if not args.no_variants:
+        for vp, vpat in VARIANTS:
+            if (vp, vpat) != (args.precision, args.pattern):
+                variants[f"{vp}_{vpat}"] = time_variant(args, G, torch, dev, stream, local, vp,
+                                                        vpat)
+        base = variants.get("fp32_ab") if args.precision != "fp32" else None
+        ref_ms = base["ms_per_step"] if base else (ms_k / args.steps
+                                                   if args.precision == "fp32" and
+                                                   args.pattern == "ab" else None)
+        if ref_ms:
+            for v in variants.values():
+                v["speedup_vs_fp32_ab"] = round(ref_ms / v["ms_per_step"], 3)
 
     if rank != 0:
         return
-    cpu_mlups, cpu_N, cpu_steps, cpu_s = cpu_port_mlups(CPU_SAMPLE_SIDE, args.model,
+    cpu_mlups, cpu_N, cpu_steps, cpu_s = cpu_port_mlups(args.cpu_side, args.model,
                                                         args.cpu_seconds)
+    host = host_info()
     line = {
         "metric": "MLUPS", "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": DTYPE[prec], "data": "synthetic",
         "config": workload_config(args, side),
+        "what": "value: per step the fused step kernel and the reference's residual line "
+                "(serial/Iterate.c:263-307), state resident on the device; roofline: the step "
+                "kernel alone",
         "fluid_mlups": round(ws * args.side ** 2 * args.steps / (ms_max / 1e3) / 1e6, 1),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "peak_kind": peak_kind, "bytes_per_node_step": bpn,
+                     "kernel_ms": round(ms_k / args.steps, 4),
                      "kernel": "lbm::k_step (fused pull-stream + BC + moments + collision)"},
         "cpu_baseline": {"value": round(cpu_mlups, 3), "unit": "MLUPS", "cores": 1, "kind": "port",
                          "sample": f"oracle port (serial reference restated, bit-identical), cavity "
-                                   f"{CPU_SAMPLE_SIDE + 2}x{CPU_SAMPLE_SIDE + 3} MRT FP64, "
-                                   f"{cpu_steps} steps in {cpu_s:.1f} s, 1 thread"},
+                                   f"{args.cpu_side + 2}x{args.cpu_side + 3} MRT FP64, "
+                                   f"{cpu_steps} steps in {cpu_s:.1f} s, 1 thread of "
+                                   f"{host['nproc']} ({host['cpu_model']})",
+                         "host": host},
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clocks,
@@ -357,35 +454,25 @@ def run_gpu(args):
     print(json.dumps(line), flush=True)
 
 
-def time_variant(args, G, torch, dev, stream, local, prec_name, pat_name, steps=None):
-    """MLUPS of another storage/pattern on the same cavity (autotuned tile)."""
-    side = args.side
-    steps = steps or max(10, args.steps // 2)
-    mesh = G.Mesh.cavity(side)
-    n, m = mesh.shape
-    N = n * m
-    s = G.Solver(mesh, uavg=0.05, vavg=0.0, rho_ini=1.0, viscosity=0.05 * side / 10000.0,
-                 collision_model=args.model, curved_boundaries=1, outlet_profile=2,
-                 precision=G.PRECISIONS[prec_name], pattern=G.PATTERNS[pat_name], device=local,
-                 stream=stream.cuda_stream)
-    del mesh
-    tune = s.autotune(5)
+def time_variant(args, G, torch, dev, stream, local, prec_name, pat_name):
+    """MLUPS, HBM fraction and clocks of another storage / pattern on the same
+    cavity (autotuned tile), the step kernel alone."""
+    steps = max(10, args.steps // 2)
+    s = cavity_solver(G, args.side, prec_name, pat_name, args.model, local, stream)
+    N = s.N
+    tune = s.autotune(10)
     s.set_state(None, np.ones(N), np.zeros(N), np.zeros(N))
-    s.step(4, 0)
-    torch.cuda.synchronize(dev)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    s.step(steps, 0)
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    ms = e0.elapsed_time(e1)
+    s.step(max(3, args.warmup), 0)
+    ms, clocks = timed_steps(torch, dev, stream, s, steps, 0, local, clocks=True)
     s.close()
     prec = G.PRECISIONS[prec_name]
     per = ms / 1e3 / steps
     peak, _ = measured_peak()
     return {"mlups": round(N / per / 1e6, 1),
             "ms_per_step": round(ms / steps, 4), "steps": steps,
-            "hbm_frac": round(BYTES[prec] * N / per / 1e9 / peak, 4), "tile": tune}
+            "bytes_per_node_step": BYTES[prec],
+            "hbm_frac": round(BYTES[prec] * N / per / 1e9 / peak, 4), "tile": tune,
+            "clocks": clocks}
 
 
 def main():

@@ -82,7 +82,7 @@ typedef struct lbm_params {
   int32_t device;            /* CUDA device ordinal */
   double rho_out;            /* outlet density for outlet_profile 4 */
   void *stream;              /* cudaStream_t to run on; NULL = a stream owned by the context */
-  int32_t tile_variant;      /* fused-step tile: 0 = default or lbm_autotune's choice, 1..4 fixed */
+  int32_t tile_variant;      /* fused-step tile: 0 = default or lbm_autotune's choice, 1..6 fixed */
 } lbm_params;
 
 typedef struct lbm_ctx lbm_ctx;
@@ -122,7 +122,11 @@ lbm_status lbm_set_state(lbm_ctx *ctx, const double *f, const double *rho, const
  * residuals (may be NULL): the reference's L2_norm, L2_norm_weighted, Drag,
  * Lift (serial/ComputeResiduals.c:6-51, including its index quirk).  The
  * buffer must hold 4 * (nsteps / check_every) doubles.  Returns LBM_DIVERGED
- * if any reported residual is NaN. */
+ * if any reported residual is NaN (serial/ComputeResiduals.c:47-51) and, for
+ * FP32 and 16-bit storage, also when any node's collision met a NaN or an
+ * infinity during these steps, whatever check_every is (the reference's
+ * residual cannot see most nodes; FP64 keeps its report).  The state is then
+ * lost: lbm_set_state starts again. */
 lbm_status lbm_step(lbm_ctx *ctx, int32_t nsteps, int32_t check_every, double *residuals);
 
 /* Fields after the last completed iteration; any pointer may be NULL.
@@ -139,18 +143,21 @@ lbm_status lbm_check(lbm_ctx *ctx, lbm_diagnostics *out);
  * memory to its own pool, a loop that must not allocate between steps).
  * No counterpart in the reference, whose residual needs no device memory.
  * Same sums as lbm_check except du_rel (returned as NaN: it needs per-cell
- * reference fields).  Uses one fixed 5 MiB device array inside the library,
- * held on every GPU that loads it until exit, so domains whose diagnostics
- * grid needs more than 65536 blocks of 128 positions (about 8.4 M grid
- * positions) get LBM_INVALID.  Calls share that array: calls whose kernels
- * overlap on the GPU (other streams or host threads) race; serialise them.
+ * reference fields).  Uses one fixed 5 MiB device array inside the library
+ * (65536 reduction blocks), held on every GPU that loads it until exit.  It
+ * reduces on lbm_check's grid (one block column per 128 grid columns, at most
+ * 8192 blocks where the width allows), so only domains wider than 65536 x 128
+ * (about 8.4 M) grid columns get LBM_INVALID.  Calls share that array:
+ * calls whose kernels overlap on the GPU (other streams or host threads)
+ * race; serialise them.
  * The first call on a device looks up the array's address; make it before
  * any stream capture. */
 lbm_status lbm_check_noalloc(lbm_ctx *ctx, lbm_diagnostics *out);
 
 /* Autotuner (no counterpart in the reference): times every tile variant of
  * the fused step (threads along x, rows per thread) on this context's domain
- * and keeps the fastest.  Must run before lbm_set_state: it steps a scratch
+ * (the median of three runs of steps_per_trial steps each, after two
+ * untimed steps) and keeps the fastest.  Must run before lbm_set_state: it steps a scratch
  * state at rest and discards it.  cache_path (NULL = none) is a file of JSON
  * lines keyed by GPU, storage, pattern, model and grid size: a hit skips the
  * timing, a miss appends the result.  report (NULL = none) receives the
@@ -199,7 +206,9 @@ lbm_status lbm_batch_set_tile(lbm_batch *b, int32_t tile_variant);
 /* Times the batched step's tile shapes and keeps the fastest (before stepping). */
 lbm_status lbm_batch_autotune(lbm_batch *b, int32_t steps_per_trial, char *report,
                               size_t report_cap);
-/* Steps every unconverged case until all have converged or max_steps have run.
+/* Steps every unconverged case until all have converged or max_steps have run
+ * (max_steps is rounded up to a multiple of check_every: the run advances in
+ * whole segments of check_every steps and one check).
  * Every check_every steps each active case gets the relative change per step
  * du_rel = ||(u,v) - (u,v)_prev|| / (check_every ||(u,v)||) against the previous
  * check (FP64 sums), so tol does not depend on check_every; a case with du_rel <= tol

@@ -19,7 +19,12 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "liblbm_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libserialref.so")
-REF_SRC = "/root/reference/serial"
+# The reference checkout (mate-szoke/ParallelLbmCranfield) is named by the
+# LBM_REFERENCE_DIR environment variable; where it is unset or absent, the
+# reference harness is not built and the tests that need it skip.
+REF_ROOT = os.environ.get("LBM_REFERENCE_DIR", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "serial")
+REF_CASES = os.path.join(REF_ROOT, "cases")
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")

@@ -427,6 +427,14 @@ __device__ __forceinline__ void collide(const R F[9], R rho, R u, R v, const Ste
   else collide_mrt<R>(F, rho, u, v, a, M);
 }
 
+// Divergence flag of the reduced-precision steps.  A NaN or infinity in any
+// population a node pulls reaches its M[0] (every collision operator forms
+// M[0] from rho and j, which sum all nine), so one compare per node finds it
+// and one plain store records it; nothing else is read or written.
+__device__ __forceinline__ void flag_nonfinite(const StepArgs &a, float m0) {
+  if (!(fabsf(m0) <= 3.0e38f) && a.nanflag) *a.nanflag = 1;
+}
+
 // Moments plus collision of a node without boundary work.  In FP32 the MRT
 // operator takes rho, j from its own moment transform (rho = m0, j = m3, m5)
 // so the conserved moments relax by exactly zero and need no work; rho^2 q is
@@ -528,6 +536,7 @@ __device__ __forceinline__ void collide_bulk_dev(const typename ST::R F[9], cons
     M[6] = F[6] - c * (dg - Xd + Yd - Q);
     M[7] = F[7] - c * (dg - Xd - Yd + Q);
     M[8] = F[8] - c * (dg + Xd - Yd - Q);
+    flag_nonfinite(a, M[0]);
   } else {
     R rt = ((F[0] + F[1]) + (F[2] + F[3])) + ((F[4] + F[5]) + (F[6] + F[7])) + F[8];
     R jx = (F[1] - F[3]) + (F[5] - F[6]) + (F[8] - F[7]);
@@ -556,6 +565,7 @@ __device__ __forceinline__ void collide_bulk_dev(const typename ST::R F[9], cons
         M[k] = F[k] - om * sp - omA * sm;
       }
     }
+    flag_nonfinite(a, M[0]);
   }
 }
 
@@ -768,6 +778,7 @@ __device__ __forceinline__ void collide_dev(const float F[9], float rho, float u
       }
     }
   }
+  flag_nonfinite(a, M[0]);
 }
 
 // ------------------------------------------------------------------- kernels
@@ -1313,6 +1324,7 @@ __global__ void __launch_bounds__(128, NPT == 2 ? 8 : 1) k_step_h2(const __grid_
     if (cl[j][1] == CLS_SOLID)
 #pragma unroll
       for (int k = 0; k < 9; k++) M[k].y = 0.f;
+    if constexpr (MODEL == 3) flag_nonfinite(a, M[0].x + M[0].y);
     const long long node0 = (long long)y * a.pitch + x0;
 #pragma unroll
     for (int i = 0; i < 2; i++)

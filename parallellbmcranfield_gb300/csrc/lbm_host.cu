@@ -2,6 +2,7 @@
 // state upload, the stepping loop and field / diagnostic read-back.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -56,7 +57,7 @@ struct lbm_ctx {
   int variant = 0;           // tile variant of the fused step
   int pf_blocks[lbm::NVAR] = {};  // per variant: resident blocks of one wave (-1: not known yet)
   void *pop_raw[2] = {nullptr, nullptr};  // allocations behind pop[] (guard elements in front)
-  int *d_err = nullptr;      // device error word of bounded waits
+  int *d_err = nullptr;      // [0] error word of bounded waits, [1] NaN flag of the step
   lbm::StepArgs base{};
 };
 
@@ -196,15 +197,18 @@ lbm_status launch_step(lbm_ctx *c) {
   return LBM_OK;
 }
 
-// A bounded device wait that gave up sets the error word; report and clear it.
+// A bounded device wait that gave up sets the error word; report and clear
+// it.  A reduced-precision step that produced a NaN or infinity sets the NaN
+// flag, which stays set until the next lbm_set_state (the state is lost).
 lbm_status check_device_error(lbm_ctx *c) {
-  int h = 0;
-  LBM_CK(cudaMemcpyAsync(&h, c->d_err, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+  int h[2] = {0, 0};
+  LBM_CK(cudaMemcpyAsync(h, c->d_err, sizeof h, cudaMemcpyDeviceToHost, c->stream));
   LBM_CK(cudaStreamSynchronize(c->stream));
-  if (h != 0) {
+  if (h[0] != 0) {
     cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
     return fail(LBM_TIMEOUT, "a bounded device wait (TMA stage barrier) gave up");
   }
+  if (h[1] != 0) return fail(LBM_DIVERGED, "DIVERGENCE! (NaN or infinity in the populations)");
   return LBM_OK;
 }
 
@@ -282,6 +286,7 @@ lbm_status set_state_impl(lbm_ctx *c, const double *f, const double *rho, const 
   if (s != LBM_OK) return s;
   LBM_CK(cudaStreamSynchronize(c->stream));
   LBM_CK(cudaGetLastError());
+  LBM_CK(cudaMemsetAsync(c->d_err + 1, 0, sizeof(int), c->stream));
   c->iter = 0;
   c->have_state = true;
   c->have_prev = false;
@@ -365,8 +370,8 @@ lbm_status lbm_create(const lbm_mesh *mesh, const lbm_params *params, lbm_ctx **
       return bail(fail(LBM_CUDA, "cudaMemset failed"));
     c->pop[i] = (char *)c->pop_raw[i] + guard * c->ks->elem_size;
   }
-  if ((s = dalloc(c, &c->d_err, 1)) != LBM_OK) return bail(s);
-  if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess)
+  if ((s = dalloc(c, &c->d_err, 2)) != LBM_OK) return bail(s);
+  if (cudaMemset(c->d_err, 0, 2 * sizeof(int)) != cudaSuccess)
     return bail(fail(LBM_CUDA, "cudaMemset failed"));
   if (params->pattern == LBM_AA)
     for (int i = 0; i < 2; i++)
@@ -412,6 +417,9 @@ lbm_status lbm_create(const lbm_mesh *mesh, const lbm_params *params, lbm_ctx **
   }
   std::memcpy(a.stmiv, P.stmiv, sizeof a.stmiv);
   a.err = c->d_err;
+  // FP64 is the parity mode: its divergence report stays the reference's
+  // (a NaN residual line); the other storages flag any NaN in the step
+  a.nanflag = params->precision == LBM_FP64 ? nullptr : c->d_err + 1;
   *out = c;
   return LBM_OK;
 }
@@ -576,7 +584,9 @@ extern "C" lbm_status lbm_check_noalloc(lbm_ctx *ctx, lbm_diagnostics *out) {
     return fail(LBM_INVALID, "no completed iteration to check");
   LBM_CK(cudaSetDevice(ctx->p.device));
   double h[lbm::NSUM];
-  lbm_status s = lbm::check_noalloc(ctx->ks, args_now(ctx), layout_of(ctx), node_grid(ctx),
+  // the launch shape of lbm_check (block rows capped at kFinishBlocks
+  // partial rows), so both reduce the same partial sums in the same order
+  lbm_status s = lbm::check_noalloc(ctx->ks, args_now(ctx), layout_of(ctx), finish_grid(ctx),
                                     ctx->stream, h);
   if (s != LBM_OK) return s;
   out->iteration = ctx->iter;
@@ -660,13 +670,20 @@ extern "C" lbm_status lbm_autotune(lbm_ctx *ctx, int32_t steps_per_trial, const 
       }
       ctx->variant = v;
       for (int i = 0; i < 2 && s == LBM_OK; i++) s = launch_step(ctx);
-      cudaEventRecord(e0, ctx->stream);
-      for (int i = 0; i < steps_per_trial && s == LBM_OK; i++) s = launch_step(ctx);
-      cudaEventRecord(e1, ctx->stream);
-      cudaEventSynchronize(e1);
-      float t = 0.f;
-      cudaEventElapsedTime(&t, e0, e1);
-      ms[v] = (double)t / steps_per_trial;
+      // median of three timed runs: one slow run (a clock change, another
+      // process) must not decide the pick
+      double rep[3];
+      for (int r = 0; r < 3; r++) {
+        cudaEventRecord(e0, ctx->stream);
+        for (int i = 0; i < steps_per_trial && s == LBM_OK; i++) s = launch_step(ctx);
+        cudaEventRecord(e1, ctx->stream);
+        cudaEventSynchronize(e1);
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        rep[r] = (double)t / steps_per_trial;
+      }
+      std::sort(rep, rep + 3);
+      ms[v] = rep[1];
       if (ms[v] < ms[best]) best = v;
     }
     cudaEventDestroy(e0);

@@ -11,9 +11,11 @@
 // in the library image instead.
 //
 // The array: kNoallocMaxBlocks blocks x NSUM doubles (5 MiB), held by every
-// GPU that loads the library until the process exits.  A domain whose
-// diagnostics grid needs more blocks (more than 65536 x 128 = 8.4 M grid
-// positions) is rejected with LBM_INVALID.
+// GPU that loads the library until the process exits.  The reduction grid is
+// lbm_check's: one block column per 128 grid columns, block rows striding
+// over the grid rows so that at most 8192 blocks result when the columns
+// allow.  Only a domain wider than 65536 x 128 = 8.4 M grid columns needs
+// more blocks than the array holds; it is rejected with LBM_INVALID.
 //
 // Sharing: every call uses the same array, which keeps the last call's
 // contents.  Each call writes every slot it later reads (one slot row per
@@ -71,9 +73,9 @@ lbm_status check_noalloc(const KernelSet *ks, const StepArgs &a, int layout, dim
   if (nblk > kNoallocMaxBlocks)
     return fail(LBM_INVALID, "lbm_check_noalloc: the domain needs " + std::to_string(nblk) +
                                  " reduction blocks; the fixed scratch holds " +
-                                 std::to_string(kNoallocMaxBlocks) + " (about " +
+                                 std::to_string(kNoallocMaxBlocks) + " (domains up to " +
                                  std::to_string((long long)kNoallocMaxBlocks * 128) +
-                                 " grid positions)");
+                                 " grid columns)");
   double *scratch = nullptr;
   lbm_status s = scratch_for_current_device(&scratch);
   if (s != LBM_OK) return s;

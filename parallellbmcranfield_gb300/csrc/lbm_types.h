@@ -81,6 +81,8 @@ struct StepArgs {
   float scale[9], inv_scale[9];
   double stmiv[81];         // Minv * diag(s) of MRTInitializer, row-major
   int *err;                 // device error word: set when a bounded wait gives up
+  int *nanflag;             // set to 1 by a reduced-precision step that produced a NaN or
+                            // infinity (null: no check, the FP64 parity mode and batches)
   int tma_stages;           // ring depth of the TMA step (from the shared-memory budget)
   int tma_tiles_x, tma_tiles_y;
   int pf_blocks;            // paired 16-bit step: L2 prefetch for the block this many launch

@@ -29,3 +29,32 @@ def test_workload_config_and_traffic():
     t = bench.load_traffic("fp32", "ab", 3)
     assert 0.95 < t / (72 * 16384 * 16385) < 1.0  # measured bytes per launch vs algorithmic
     assert bench.load_traffic("fp64", "aa", 1) is None
+
+
+def test_reference_arm_loads_no_gpu_library():
+    """The reference arm times the oracle port on every host core and states
+    the workload it timed; neither it nor its workers load liblbm_gb300.so."""
+    import json
+    import subprocess
+
+    code = ("import sys, runpy; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '2', "
+            "'--warmup', '1', '--cpu-side', '30']; runpy.run_path('bench.py', run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('LOADED' if 'liblbm_gb300' in maps or 'parallellbmcranfield_gb300' in sys.modules "
+            "else 'CLEAN')")
+    out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True,
+                         timeout=600)
+    assert out.returncode == 0, out.stderr
+    lines = out.stdout.strip().splitlines()
+    assert lines[-1] == "CLEAN"
+    line = json.loads(lines[-2])
+    assert line["impl"] == "reference" and line["unit"] == "MLUPS" and line["value"] > 0
+    assert "32x33 nodes" in line["config"]["workload"] and "FP64" in line["config"]["workload"]
+    cb = line["cpu_baseline"]
+    assert cb["cores"] == os.cpu_count() and cb["kind"] == "port"
+    assert cb["host"]["nproc"] == os.cpu_count() and cb["host"]["cpu_model"]
+
+
+def test_host_info():
+    h = bench.host_info()
+    assert h["nproc"] == os.cpu_count() and isinstance(h["cpu_model"], str)

@@ -120,12 +120,12 @@ def test_missing_mesh_file_is_io_error(tmp_path):
     assert e.value.status == G.LBM_IO
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/cases/coarse"),
+@pytest.mark.skipif(not os.path.isdir(os.path.join(O.REF_CASES, "coarse")),
                     reason="shipped meshes not present")
 @pytest.mark.parametrize("case,side", [("coarse", 125), ("medium", 253)])
 def test_generator_reproduces_shipped_cavity(case, side):
     """The generated cavity takes every CellIni decision the shipped mesh does."""
-    d = f"/root/reference/cases/{case}/Mesh"
+    d = os.path.join(O.REF_CASES, case, "Mesh")
     shipped = G.Mesh.read(f"{d}/D2node.dat", f"{d}/BCconnectors.dat")
     gen = G.Mesh.cavity(side)
     assert shipped.shape == gen.shape
@@ -149,3 +149,16 @@ def test_batch_arguments_are_checked_on_the_host():
     with pytest.raises(G.LbmError) as e:
         G.Batch([(mesh, dict(base, collision_model=2))], precision="bf16dev")
     assert e.value.status == G.LBM_INVALID
+
+
+@pytest.mark.parametrize("side", [2, 3, 30, 125])
+def test_numpy_cavity_equals_library_cavity(side):
+    """oracle.meshgen (numpy, for the CPU legs of bench.py) writes the same
+    node and link lines as lbm_mesh_cavity."""
+    from oracle import meshgen
+
+    lib = G.Mesh.cavity(side)
+    nodes, conns, shape = meshgen.cavity(side)
+    assert lib.shape == shape
+    assert np.array_equal(lib.nodes, nodes)
+    assert np.array_equal(lib.conns, conns)

@@ -10,7 +10,7 @@ import cases
 from oracle import oracle as O
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
-REF_CASES = "/root/reference/cases"
+REF_CASES = O.REF_CASES
 
 
 def load_golden(name):

@@ -37,12 +37,13 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 W9 = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4)
-PREC_NAME = {0: "fp64", 1: "fp32", 2: "fp16dev", 3: "bf16dev"}
-DTYPE = {0: "f64", 1: "f32", 2: "f16 storage, f32 compute", 3: "bf16 storage, f32 compute"}
-BYTES = {0: 144, 1: 72, 2: 36, 3: 36}
+PREC_NAME = {0: "fp64", 1: "fp32", 2: "fp16dev", 3: "bf16dev", 4: "fp16neq"}
+DTYPE = {0: "f64", 1: "f32", 2: "f16 storage, f32 compute", 3: "bf16 storage, f32 compute",
+         4: "24-bit fixed rho/j + f16 non-equilibrium moments, f32 compute"}
+BYTES = {0: 144, 1: 72, 2: 36, 3: 36, 4: 42}
 CPU_SAMPLE_SIDE = 1022  # 1024 x 1025 node cavity for the CPU legs
-VARIANTS = (("fp32", "aa"), ("fp16dev", "ab"), ("fp16dev", "aa"), ("bf16dev", "ab"),
-            ("bf16dev", "aa"))
+VARIANTS = (("fp32", "aa"), ("fp16neq", "ab"), ("fp16dev", "ab"), ("fp16dev", "aa"),
+            ("bf16dev", "ab"), ("bf16dev", "aa"))
 
 
 def parse():
@@ -272,7 +273,7 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
-ELEM_BYTES = {"fp64": 8, "fp32": 4, "fp16dev": 2, "bf16dev": 2}
+ELEM_BYTES = {"fp64": 8, "fp32": 4, "fp16dev": 2, "bf16dev": 2, "fp16neq": 21 / 9}
 
 
 def workload_config(args, side):

@@ -48,7 +48,11 @@ typedef enum lbm_precision {
   LBM_FP64 = 0,    /* FP64 storage and arithmetic in the reference's order (parity mode) */
   LBM_FP32 = 1,    /* FP32 storage and arithmetic */
   LBM_FP16DEV = 2, /* FP16 storage of scaled (f_k - w_k rho0), FP32 arithmetic */
-  LBM_BF16DEV = 3  /* BF16 storage of scaled (f_k - w_k rho0), FP32 arithmetic */
+  LBM_BF16DEV = 3, /* BF16 storage of scaled (f_k - w_k rho0), FP32 arithmetic */
+  LBM_FP16NEQ = 4  /* moment storage, A-B pattern only: rho - rho0 and j in 24-bit fixed
+                      point (|rho - rho0| < 0.5 rho0, |j| < 0.25 rho0, else LBM_DIVERGED), the six
+                      non-equilibrium moments in FP16, nodes with boundary work in FP32;
+                      21 bytes per node, FP32 arithmetic */
 } lbm_precision;
 
 typedef enum lbm_pattern {
@@ -183,8 +187,8 @@ lbm_status lbm_inspect_mesh(const lbm_mesh *mesh, const lbm_params *params, int3
 /* ---------------------------------------------------------------------------
  * Batches.  No counterpart in the reference, which runs one case per process:
  * many independent domains (cavities, channels of different sizes and
- * parameters) advanced together: per step one persistent launch over a
- * device-side list of (case, tile), and alongside it one over the (case, node)
+ * parameters) advanced together: per step one launch over a device-side
+ * list of (case, tile), and alongside it one over the (case, node)
  * list of boundary nodes; both lists are compacted to the cases still stepping
  * at the start of every run segment.  Per-case convergence flags live on the
  * device; each run segment (check_every steps and one check) is one CUDA graph

@@ -17,10 +17,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liblbm_gb300.so")
 
 LBM_OK, LBM_DIVERGED, LBM_IO, LBM_CUDA, LBM_TIMEOUT, LBM_INVALID, LBM_NOMEM = range(7)
-FP64, FP32, FP16DEV, BF16DEV = range(4)
+FP64, FP32, FP16DEV, BF16DEV, FP16NEQ = range(5)
 AB, AA = range(2)
 BGKW, TRT, MRT = 1, 2, 3
-PRECISIONS = {"fp64": FP64, "fp32": FP32, "fp16dev": FP16DEV, "bf16dev": BF16DEV}
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "fp16dev": FP16DEV, "bf16dev": BF16DEV,
+              "fp16neq": FP16NEQ}
 PATTERNS = {"ab": AB, "aa": AA}
 
 

@@ -1,7 +1,7 @@
 // Batched stepping of many independent domains (cavities, channels): per step
-// one persistent bulk launch walks a device-side work list of (case, tile),
-// and a second launch, alongside it, the list of (case, node) with boundary
-// work; per-case parity, step counters and convergence flags live on the
+// one bulk launch covers a device-side work list of (case, tile) (one block
+// per tile; FP64 walks it with a persistent grid), and a second launch,
+// alongside it, the list of (case, node) with boundary work; per-case parity, step counters and convergence flags live on the
 // device so that a whole run segment (steps + check) can be captured in one
 // CUDA graph.
 #pragma once
@@ -82,6 +82,83 @@ __global__ void __launch_bounds__(128) k_batch_special(const BatchCase *__restri
     const StepArgs &a = cases[e.x].args[gpar[e.x] & 1];
     step_one<ST, MODEL, PH_AB>(a, (long long)e.y, (uint8_t)CLS_SPECIAL);
   }
+}
+
+// The fields of one case's StepArgs that the bulk update reads, per A-B
+// parity (k_batch_bulk): 128 bytes instead of the full argument record.
+struct BulkArgs {
+  const void *src;
+  void *dst;
+  const uint8_t *cls;
+  long long plane;
+  int pitch, n, m;
+  float omega, omegaA, rho0;
+  float scale[9], inv_scale[9];
+};
+static_assert(sizeof(BulkArgs) == 128, "BulkArgs layout");
+
+// Bulk nodes (class 1) of one column of NPT rows; every other class is left
+// to the boundary-node pass.  The loads of all NPT nodes go out first.
+template <class ST, int MODEL, int NPT>
+__device__ __forceinline__ void bulk_column(const StepArgs &a, int x, int y0) {
+  using R = typename ST::R;
+  using T = typename ST::T;
+  if (x >= a.n) return;
+  uint8_t c[NPT];
+#pragma unroll
+  for (int j = 0; j < NPT; j++)
+    c[j] = (y0 + j < a.m) ? a.cls[(long long)(y0 + j) * a.pitch + x] : (uint8_t)CLS_SOLID;
+  const T *s = (const T *)a.src;
+  R F[NPT][9];
+#pragma unroll
+  for (int j = 0; j < NPT; j++) {
+    const long long node = (long long)(y0 + j) * a.pitch + x;
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+      F[j][k] = (c[j] == CLS_BULK) ? ld_dev<ST>(s + pull_index<PH_AB>(k, node, a), k, a) : R(0);
+  }
+#pragma unroll
+  for (int j = 0; j < NPT; j++)
+    if (c[j] == CLS_BULK)
+      bulk_store<ST, MODEL, PH_AB>(a, (long long)(y0 + j) * a.pitch + x, c[j], F[j]);
+}
+
+// Batched bulk pass with one block per live (case, tile): no persistent loop
+// and no shared-memory copy of the case arguments, so a block's loads go out
+// as soon as it starts and the hardware keeps every SM filled with blocks.
+// Blocks past the live count (the grid is sized for all tiles when the
+// graph is captured) return at once.
+template <class ST, int MODEL, int BX, int NPT>
+__global__ void __launch_bounds__(BX) k_batch_bulk(const BulkArgs *__restrict__ args,
+                                                   const int4 *__restrict__ tiles,
+                                                   const int *__restrict__ ntiles_live,
+                                                   const int *__restrict__ active,
+                                                   const int *__restrict__ gpar) {
+  const int t = blockIdx.x;
+  if (t >= __ldg(ntiles_live)) return;
+  const int4 tl = __ldg(&tiles[t]);
+  if (!__ldg(&active[tl.x])) return;
+  const BulkArgs &b = args[2 * tl.x + (__ldg(&gpar[tl.x]) & 1)];
+  StepArgs a;
+  a.src = const_cast<void *>(b.src);
+  a.dst = b.dst;
+  a.cls = b.cls;
+  a.plane = b.plane;
+  a.pitch = b.pitch;
+  a.n = b.n;
+  a.m = b.m;
+  a.omega = b.omega;
+  a.omegaA = b.omegaA;
+  a.rho0 = b.rho0;
+  a.nanflag = nullptr;
+  if constexpr (sizeof(typename ST::T) == 2) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      a.scale[k] = b.scale[k];
+      a.inv_scale[k] = b.inv_scale[k];
+    }
+  }
+  bulk_column<ST, MODEL, NPT>(a, tl.y * BX + threadIdx.x, tl.z * NPT);
 }
 
 // After a step: active cases advance their parity and counters.
@@ -172,6 +249,8 @@ static __global__ void k_batch_converge(int ncases, BatchState s, double tol, do
 
 struct BatchKernels {
   const void *step[4][BVAR];  // [model 1..3][tile shape]
+  int per_tile;               // 1: step kernels take BulkArgs and one block per tile
+                              // (k_batch_bulk); 0: BatchCase and a persistent grid
   const void *special[4];     // [model 1..3]
   const void *du;
   const void *advance;

@@ -53,6 +53,7 @@ struct lbm_batch {
   std::vector<CaseDev> cases;
   std::vector<lbm::BatchCase> hcases;
   lbm::BatchCase *d_cases = nullptr;
+  lbm::BulkArgs *d_bulk = nullptr;  // per case and parity: the bulk pass's arguments
   lbm::BatchState s{};
   int4 *d_tiles[lbm::BVAR] = {};
   int ntiles[lbm::BVAR] = {};
@@ -174,7 +175,11 @@ lbm_status launch_compact(lbm_batch *b) {
 lbm_status launch_steps(lbm_batch *b, int k) {
   const void *fn = b->bk->step[b->model][b->variant];
   const int bx = lbm::BVAR_BX[b->variant];
-  const int grid = std::min(b->ntiles[b->variant], persistent_blocks(fn, bx, b->device));
+  // per-tile kernels: one block per tile of the full list (blocks past the
+  // live count return); persistent kernels: one wave of resident blocks
+  const int grid = b->bk->per_tile ? b->ntiles[b->variant]
+                                   : std::min(b->ntiles[b->variant], persistent_blocks(fn, bx, b->device));
+  void *step_args0 = b->bk->per_tile ? (void *)b->d_bulk : (void *)b->d_cases;
   lbm_status st = launch_compact(b);
   if (st != LBM_OK) return st;
   int *cnt_t = b->d_live_n, *cnt_s = b->d_live_n + 1;
@@ -186,7 +191,7 @@ lbm_status launch_steps(lbm_batch *b, int k) {
       LBM_BCK(cudaEventRecord(b->ev_fork, b->stream));
       LBM_BCK(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
     }
-    void *args[] = {&b->d_cases, &b->d_live_tiles, &cnt_t, &b->s.active, &b->s.gpar};
+    void *args[] = {&step_args0, &b->d_live_tiles, &cnt_t, &b->s.active, &b->s.gpar};
     cudaError_t e = cudaLaunchKernel(fn, dim3(grid), dim3(bx), args, 0, b->stream);
     if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
     if (b->nspecial > 0) {
@@ -357,6 +362,31 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
   }
   if ((st = balloc(b, &b->d_cases, (size_t)ncases)) != LBM_OK) return bail(st);
   cudaMemcpy(b->d_cases, b->hcases.data(), ncases * sizeof(lbm::BatchCase), cudaMemcpyHostToDevice);
+  {
+    std::vector<lbm::BulkArgs> bulk(2 * (size_t)ncases);
+    for (int c = 0; c < ncases; c++)
+      for (int par = 0; par < 2; par++) {
+        const lbm::StepArgs &a = b->hcases[c].args[par];
+        lbm::BulkArgs &q = bulk[2 * c + par];
+        std::memset(&q, 0, sizeof q);
+        q.src = a.src;
+        q.dst = a.dst;
+        q.cls = a.cls;
+        q.plane = a.plane;
+        q.pitch = a.pitch;
+        q.n = a.n;
+        q.m = a.m;
+        q.omega = (float)a.omega;
+        q.omegaA = (float)a.omegaA;
+        q.rho0 = (float)a.rho0;
+        for (int k = 0; k < 9; k++) {
+          q.scale[k] = a.scale[k];
+          q.inv_scale[k] = a.inv_scale[k];
+        }
+      }
+    if ((st = balloc(b, &b->d_bulk, bulk.size())) != LBM_OK) return bail(st);
+    cudaMemcpy(b->d_bulk, bulk.data(), bulk.size() * sizeof(lbm::BulkArgs), cudaMemcpyHostToDevice);
+  }
   for (int v = 0; v < lbm::BVAR; v++) {
     b->ntiles[v] = (int)tiles[v].size();
     if ((st = balloc(b, &b->d_tiles[v], tiles[v].size())) != LBM_OK) return bail(st);

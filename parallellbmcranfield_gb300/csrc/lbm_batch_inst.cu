@@ -18,18 +18,30 @@
 
 namespace lbm {
 
+// FP64 (the parity mode, whose MRT reads the full stmiv table) keeps the
+// persistent kernel over full case arguments; FP32 and FP16-dev take the
+// per-tile bulk kernel over compact arguments.
+template <class ST, int MODEL, int V>
+const void *batch_step_fn() {
+  if constexpr (std::is_same<ST, StF64>::value)
+    return (const void *)k_batch_step<ST, MODEL, BVAR_BX[V], BVAR_NPT[V]>;
+  else
+    return (const void *)k_batch_bulk<ST, MODEL, BVAR_BX[V], BVAR_NPT[V]>;
+}
+
 template <class ST, int MODEL>
 void fill_batch_steps(const void *out[BVAR]) {
-  out[0] = (const void *)k_batch_step<ST, MODEL, BVAR_BX[0], BVAR_NPT[0]>;
-  out[1] = (const void *)k_batch_step<ST, MODEL, BVAR_BX[1], BVAR_NPT[1]>;
-  out[2] = (const void *)k_batch_step<ST, MODEL, BVAR_BX[2], BVAR_NPT[2]>;
-  out[3] = (const void *)k_batch_step<ST, MODEL, BVAR_BX[3], BVAR_NPT[3]>;
+  out[0] = batch_step_fn<ST, MODEL, 0>();
+  out[1] = batch_step_fn<ST, MODEL, 1>();
+  out[2] = batch_step_fn<ST, MODEL, 2>();
+  out[3] = batch_step_fn<ST, MODEL, 3>();
   static_assert(BVAR == 4, "batch tile table");
 }
 
 const BatchKernels &LBM_BATCH_FN(LBM_PREC)() {
   static const BatchKernels bk = [] {
     BatchKernels k{};
+    k.per_tile = std::is_same<LBM_ST, StF64>::value ? 0 : 1;
     fill_batch_steps<LBM_ST, 1>(k.step[1]);
     fill_batch_steps<LBM_ST, 2>(k.step[2]);
     fill_batch_steps<LBM_ST, 3>(k.step[3]);

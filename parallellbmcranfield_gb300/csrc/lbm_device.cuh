@@ -1727,11 +1727,10 @@ static __global__ void k_reduce_partials(const double *partial, int nblocks, dou
 // The serial residual (serial/ComputeResiduals.c:6-51) with its index quirk:
 // only cells 0..m-1 (reference numbering j*n+i) are visited, each n times.
 // One block; writes L2, L2_weighted, Drag, Lift to out[0..3].
-template <class ST, int L>
-__global__ void __launch_bounds__(256) k_resid_ref(const __grid_constant__ StepArgs a, double *out) {
-  using R = typename ST::R;
+template <class ACC>
+__device__ __forceinline__ void resid_body(const StepArgs &a, const ACC &acc_m, double *out) {
+  using R = typename ACC::R;
   __shared__ double sh[3][256];
-  AccMain<ST, L> acc_m(a, a.src);
   double s2 = 0.0, sd = 0.0, sl = 0.0;
   for (int c = threadIdx.x; c < a.m; c += blockDim.x) {
     const int x = c % a.n, y = c / a.n;
@@ -1775,6 +1774,11 @@ __global__ void __launch_bounds__(256) k_resid_ref(const __grid_constant__ StepA
     out[2] = td * nn;
     out[3] = tl * nn;
   }
+}
+
+template <class ST, int L>
+__global__ void __launch_bounds__(256) k_resid_ref(const __grid_constant__ StepArgs a, double *out) {
+  resid_body<AccMain<ST, L>>(a, AccMain<ST, L>(a, a.src), out);
 }
 
 }  // namespace lbm

@@ -58,6 +58,12 @@ struct lbm_ctx {
   int pf_blocks[lbm::NVAR] = {};  // per variant: resident blocks of one wave (-1: not known yet)
   void *pop_raw[2] = {nullptr, nullptr};  // allocations behind pop[] (guard elements in front)
   int *d_err = nullptr;      // [0] error word of bounded waits, [1] NaN flag of the step
+  // moment storage (LBM_FP16NEQ)
+  const lbm::MomKernels *mk = nullptr;
+  float *ss[2] = {nullptr, nullptr};  // FP32 side arrays of the class-3 nodes (A-B parities)
+  uint32_t *d_mlist = nullptr;        // class-3 and class-2 nodes
+  int mlist_n = 0;
+  std::vector<uint32_t> mlist_host;
   lbm::StepArgs base{};
 };
 
@@ -81,7 +87,8 @@ lbm_status dalloc(lbm_ctx *c, T **p, size_t count) {
 void release(lbm_ctx *c) {
   void *ptrs[] = {c->pop_raw[0], c->pop_raw[1], c->sb[0], c->sb[1], c->d_cls, c->d_err,
                   c->d_aux,  c->d_rec,  c->d_rho0,   c->d_u0,       c->d_v0,
-                  c->d_uprev, c->d_vprev, c->d_partial, c->d_sums, c->d_hist};
+                  c->d_uprev, c->d_vprev, c->d_partial, c->d_sums, c->d_hist,
+                  c->ss[0], c->ss[1], c->d_mlist};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -99,9 +106,12 @@ int layout_of(const lbm_ctx *c) {
 // Arguments for a launch that reads generation g (and writes g+1).
 lbm::StepArgs args_now(const lbm_ctx *c) {
   lbm::StepArgs a = c->base;
+  a.gen = (unsigned)(c->g + 1);
   if (c->p.pattern == LBM_AB) {
     a.src = c->pop[c->g & 1];
     a.dst = c->pop[(c->g + 1) & 1];
+    a.ss_src = c->ss[c->g & 1];
+    a.ss_dst = c->ss[(c->g + 1) & 1];
   } else {
     a.src = a.dst = c->pop[0];
     a.sb_src = c->sb[c->g & 1];
@@ -181,7 +191,26 @@ bool step_config(lbm_ctx *c, int var, dim3 *grid, dim3 *block, size_t *smem) {
   return true;
 }
 
+// Moment storage: the bulk kernel over pairs of nodes (NPT rows per thread)
+// and the special-node kernel over the compact list, both reading the same
+// generation (they write disjoint nodes).
+lbm_status launch_step_mom(lbm_ctx *c) {
+  const int npt = lbm::MOM_NPT[c->variant];
+  lbm::StepArgs a = args_now(c);
+  void *args[] = {&a};
+  const dim3 grid((unsigned)((c->P.pitch + 255) / 256), (unsigned)((c->P.m + npt - 1) / npt));
+  cudaError_t e = cudaLaunchKernel(c->mk->step[c->p.collision_model][c->variant], grid, dim3(128),
+                                   args, 0, c->stream);
+  if (e == cudaSuccess && c->mlist_n > 0)
+    e = cudaLaunchKernel(c->mk->special[c->p.collision_model],
+                         dim3((unsigned)((c->mlist_n + 127) / 128)), dim3(128), args, 0, c->stream);
+  if (e != cudaSuccess) return fail(LBM_CUDA, std::string("step launch: ") + cudaGetErrorString(e));
+  c->g++;
+  return LBM_OK;
+}
+
 lbm_status launch_step(lbm_ctx *c) {
+  if (c->mk) return launch_step_mom(c);
   const int var = c->variant;
   dim3 grid, block;
   size_t smem;
@@ -208,6 +237,9 @@ lbm_status check_device_error(lbm_ctx *c) {
     cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
     return fail(LBM_TIMEOUT, "a bounded device wait (TMA stage barrier) gave up");
   }
+  if (h[1] == 2)
+    return fail(LBM_DIVERGED,
+                "moment storage out of range (|rho - rho0| >= 0.5 rho0 or |j| >= 0.25 rho0)");
   if (h[1] != 0) return fail(LBM_DIVERGED, "DIVERGENCE! (NaN or infinity in the populations)");
   return LBM_OK;
 }
@@ -215,8 +247,13 @@ lbm_status check_device_error(lbm_ctx *c) {
 lbm_status launch_resid(lbm_ctx *c, double *out) {
   lbm::StepArgs a = args_now(c);
   void *args[] = {&a, &out};
-  return launch(c->ks->resid[layout_of(c)], dim3(1), dim3(256), args, c->stream);
+  return launch(c->mk ? c->mk->resid : c->ks->resid[layout_of(c)], dim3(1), dim3(256), args,
+                c->stream);
 }
+
+// Finish and reduction kernels of the context's storage.
+const void *finish_fn(const lbm_ctx *c) { return c->mk ? c->mk->finish : c->ks->finish[layout_of(c)]; }
+const void *reduce_fn(const lbm_ctx *c) { return c->mk ? c->mk->reduce : c->ks->reduce; }
 
 // Grid of the finish kernel: one block column per 128 x positions, block rows
 // striding over the grid so that at most kFinishBlocks partial rows result.
@@ -234,11 +271,10 @@ lbm_status launch_finish(lbm_ctx *c, lbm::FinishOut &o) {
   void *args[] = {&a, &o};
   const dim3 g = finish_grid(c);
   int nb = (int)(g.x * g.y);
-  lbm_status s = launch(c->ks->finish[layout_of(c)], g, dim3(kBlock), args, c->stream);
+  lbm_status s = launch(finish_fn(c), g, dim3(kBlock), args, c->stream);
   if (s != LBM_OK) return s;
   void *rargs[] = {&c->d_partial, &nb, &c->d_sums};
-  return launch(c->ks->reduce, dim3(1), dim3(32 * lbm::NSUM), rargs,
-                c->stream);
+  return launch(reduce_fn(c), dim3(1), dim3(32 * lbm::NSUM), rargs, c->stream);
 }
 
 // Host copy of a per-cell default field.
@@ -274,19 +310,22 @@ lbm_status set_state_impl(lbm_ctx *c, const double *f, const double *rho, const 
     else
       LBM_CK(cudaMemsetAsync(d_f, 0, N * 9 * sizeof(double), c->stream));
   }
+  LBM_CK(cudaMemsetAsync(c->d_err + 1, 0, sizeof(int), c->stream));  // the first collision may set it
   c->g = 0;
   lbm::StepArgs a = args_now(c);
   a.dst = c->pop[0];
   a.sb_dst = c->sb[0];
+  a.ss_dst = c->ss[0];
+  a.gen = 0;
   void *args[] = {&a, &d_f, &c->d_rho0, &c->d_u0, &c->d_v0};
   int which = c->p.pattern == LBM_AB ? 0 : 1;
-  lbm_status s = launch(c->ks->init[c->p.collision_model][which], node_grid(c), dim3(kBlock),
-                        args, c->stream);
+  lbm_status s = launch(c->mk ? c->mk->init[c->p.collision_model]
+                              : c->ks->init[c->p.collision_model][which],
+                        node_grid(c), dim3(kBlock), args, c->stream);
   if (d_f) cudaFreeAsync(d_f, c->stream);
   if (s != LBM_OK) return s;
   LBM_CK(cudaStreamSynchronize(c->stream));
   LBM_CK(cudaGetLastError());
-  LBM_CK(cudaMemsetAsync(c->d_err + 1, 0, sizeof(int), c->stream));
   c->iter = 0;
   c->have_state = true;
   c->have_prev = false;
@@ -315,10 +354,16 @@ const char *lbm_last_error(void) { return lbm::g_err.c_str(); }
 lbm_status lbm_create(const lbm_mesh *mesh, const lbm_params *params, lbm_ctx **out) {
   if (!out || !params) return fail(LBM_INVALID, "null argument");
   *out = nullptr;
-  if (params->precision < LBM_FP64 || params->precision > LBM_BF16DEV)
+  if (params->precision < LBM_FP64 || params->precision > LBM_FP16NEQ)
     return fail(LBM_INVALID, "unknown precision");
   if (params->pattern != LBM_AB && params->pattern != LBM_AA)
     return fail(LBM_INVALID, "unknown pattern");
+  const bool mom = params->precision == LBM_FP16NEQ;
+  if (mom && params->pattern != LBM_AB)
+    return fail(LBM_INVALID, "moment storage (LBM_FP16NEQ) runs the A-B pattern only");
+  if (mom && params->tile_variant > lbm::MOM_NVAR)
+    return fail(LBM_INVALID, "tile_variant must be 0 (default/tuned) or 1.." +
+                                 std::to_string(lbm::MOM_NVAR) + " for moment storage");
   lbm_ctx *c = new lbm_ctx();
   c->p = *params;
   lbm_status s = lbm::preprocess(mesh, params, &c->P);
@@ -339,7 +384,25 @@ lbm_status lbm_create(const lbm_mesh *mesh, const lbm_params *params, lbm_ctx **
     case LBM_FP64: c->ks = &lbm::kernels_f64(); break;
     case LBM_FP32: c->ks = &lbm::kernels_f32(); break;
     case LBM_FP16DEV: c->ks = &lbm::kernels_f16(); break;
+    case LBM_FP16NEQ: c->mk = &lbm::kernels_mom(); break;
     default: c->ks = &lbm::kernels_b16(); break;
+  }
+  if (mom) {
+    // fluid nodes next to a class-3 node become class 2: the special-node
+    // kernel updates both, so the bulk kernel never reads the side array
+    lbm::Prep &Pm = c->P;
+    std::vector<uint32_t> list;
+    for (const lbm::BRec &r : Pm.rec) {
+      for (int dy = -1; dy <= 1; dy++)
+        for (int dx = -1; dx <= 1; dx++) {
+          const long long z = (long long)r.node + dx + (long long)dy * Pm.pitch;
+          if (z >= 0 && z < Pm.plane && Pm.cls[z] == lbm::CLS_BULK) Pm.cls[z] = lbm::CLS_BULK_REC;
+        }
+    }
+    for (long long z = 0; z < Pm.plane; z++)
+      if (Pm.cls[z] == lbm::CLS_BULK_REC || Pm.cls[z] == lbm::CLS_SPECIAL) list.push_back((uint32_t)z);
+    c->mlist_n = (int)list.size();
+    c->mlist_host.swap(list);
   }
   auto bail = [&](lbm_status st) {
     release(c);
@@ -361,14 +424,29 @@ lbm_status lbm_create(const lbm_mesh *mesh, const lbm_params *params, lbm_ctx **
   // halo granules of the TMA row copies and the edge reads of the vector
   // tiles reach up to 16 bytes (plus one row for the last tile) outside
   const size_t guard = 1024;
-  const size_t pop_elems = (size_t)P.plane * 9 + 2 * guard + (size_t)P.pitch;
+  // moment storage: 21 bytes per node (nine 16-bit planes, three byte planes)
+  const size_t es = mom ? 1 : (size_t)c->ks->elem_size;
+  const size_t pop_elems =
+      mom ? (size_t)P.plane * 21 + 2 * guard : (size_t)P.plane * 9 + 2 * guard + (size_t)P.pitch;
   const int npop = params->pattern == LBM_AB ? 2 : 1;
   for (int i = 0; i < npop; i++) {
-    if ((s = dalloc(c, (char **)&c->pop_raw[i], pop_elems * c->ks->elem_size)) != LBM_OK)
+    if ((s = dalloc(c, (char **)&c->pop_raw[i], pop_elems * es)) != LBM_OK)
       return bail(s);
-    if (cudaMemset(c->pop_raw[i], 0, pop_elems * c->ks->elem_size) != cudaSuccess)
+    if (cudaMemset(c->pop_raw[i], 0, pop_elems * es) != cudaSuccess)
       return bail(fail(LBM_CUDA, "cudaMemset failed"));
-    c->pop[i] = (char *)c->pop_raw[i] + guard * c->ks->elem_size;
+    c->pop[i] = (char *)c->pop_raw[i] + guard * es;
+  }
+  if (mom) {
+    for (int i = 0; i < 2; i++) {
+      if ((s = dalloc(c, &c->ss[i], P.rec.size() * 9)) != LBM_OK) return bail(s);
+      if (cudaMemset(c->ss[i], 0, std::max<size_t>(16, P.rec.size() * 9 * 4)) != cudaSuccess)
+        return bail(fail(LBM_CUDA, "cudaMemset failed"));
+    }
+    if ((s = dalloc(c, &c->d_mlist, c->mlist_host.size())) != LBM_OK) return bail(s);
+    if (!c->mlist_host.empty() &&
+        cudaMemcpy(c->d_mlist, c->mlist_host.data(), c->mlist_host.size() * 4,
+                   cudaMemcpyHostToDevice) != cudaSuccess)
+      return bail(fail(LBM_CUDA, "upload of the special-node list failed"));
   }
   if ((s = dalloc(c, &c->d_err, 2)) != LBM_OK) return bail(s);
   if (cudaMemset(c->d_err, 0, 2 * sizeof(int)) != cudaSuccess)
@@ -420,6 +498,20 @@ lbm_status lbm_create(const lbm_mesh *mesh, const lbm_params *params, lbm_ctx **
   // FP64 is the parity mode: its divergence report stays the reference's
   // (a NaN residual line); the other storages flag any NaN in the step
   a.nanflag = params->precision == LBM_FP64 ? nullptr : c->d_err + 1;
+  if (mom) {
+    // 24-bit fixed point: rho - rho0 within +-0.5 rho0, j within +-0.25 rho0
+    const double r0 = params->rho_ini > 0 ? params->rho_ini : 1.0;
+    const double qmax = (double)((1 << 23) - 1);
+    a.fx_rho = (float)(0.5 * r0 / qmax);
+    a.fx_irho = (float)(qmax / (0.5 * r0));
+    a.fx_j = (float)(0.25 * r0 / qmax);
+    a.fx_ij = (float)(qmax / (0.25 * r0));
+    a.fx_irho0 = (float)(1.0 / r0);
+    a.neq_s = 4096.f;
+    a.neq_is = 1.f / 4096.f;
+    a.mlist = c->d_mlist;
+    a.mlist_n = c->mlist_n;
+  }
   *out = c;
   return LBM_OK;
 }
@@ -443,7 +535,7 @@ lbm_status lbm_get_info(const lbm_ctx *ctx, int64_t *iteration, int64_t *device_
   if (!ctx) return fail(LBM_INVALID, "null argument");
   if (iteration) *iteration = ctx->iter;
   if (device_bytes) *device_bytes = ctx->dev_bytes;
-  if (bytes_per_node_step) *bytes_per_node_step = 18 * ctx->ks->elem_size;
+  if (bytes_per_node_step) *bytes_per_node_step = ctx->mk ? 42 : 18 * ctx->ks->elem_size;
   return LBM_OK;
 }
 
@@ -586,8 +678,8 @@ extern "C" lbm_status lbm_check_noalloc(lbm_ctx *ctx, lbm_diagnostics *out) {
   double h[lbm::NSUM];
   // the launch shape of lbm_check (block rows capped at kFinishBlocks
   // partial rows), so both reduce the same partial sums in the same order
-  lbm_status s = lbm::check_noalloc(ctx->ks, args_now(ctx), layout_of(ctx), finish_grid(ctx),
-                                    ctx->stream, h);
+  lbm_status s = lbm::check_noalloc(finish_fn(ctx), reduce_fn(ctx), args_now(ctx),
+                                    finish_grid(ctx), ctx->stream, h);
   if (s != LBM_OK) return s;
   out->iteration = ctx->iter;
   out->l2_full = std::sqrt(h[lbm::S_L2]);
@@ -611,14 +703,14 @@ std::string tune_key(const lbm_ctx *c) {
   cudaDeviceProp prop;
   std::string gpu = "gpu";
   if (cudaGetDeviceProperties(&prop, c->p.device) == cudaSuccess) gpu = prop.name;
-  const char *prec[] = {"fp64", "fp32", "fp16dev", "bf16dev"};
+  const char *prec[] = {"fp64", "fp32", "fp16dev", "bf16dev", "fp16neq"};
   return gpu + "|" + prec[c->p.precision] + "|" + (c->p.pattern == LBM_AB ? "ab" : "aa") + "|m" +
          std::to_string(c->p.collision_model) + "|" + std::to_string(c->P.n) + "x" +
          std::to_string(c->P.m);
 }
 
 // Cache lines: {"key": "<key>", "variant": <v>, "ms": [..]} -- last line for a key wins.
-int cache_lookup(const char *path, const std::string &key) {
+int cache_lookup(const char *path, const std::string &key, int nvar) {
   if (!path) return -1;
   FILE *f = std::fopen(path, "r");
   if (!f) return -1;
@@ -630,7 +722,7 @@ int cache_lookup(const char *path, const std::string &key) {
     const char *v = std::strstr(line, "\"variant\": ");
     if (k && v) {
       int var = std::atoi(v + 11);
-      if (var >= 0 && var < lbm::NVAR) found = var;
+      if (var >= 0 && var < nvar) found = var;
     }
   }
   std::fclose(f);
@@ -646,7 +738,8 @@ extern "C" lbm_status lbm_autotune(lbm_ctx *ctx, int32_t steps_per_trial, const 
   LBM_CK(cudaSetDevice(ctx->p.device));
   const std::string key = tune_key(ctx);
   std::string rep = "{\"key\": \"" + key + "\"";
-  int best = cache_lookup(cache_path, key);
+  const int nvar = ctx->mk ? lbm::MOM_NVAR : lbm::NVAR;
+  int best = cache_lookup(cache_path, key, nvar);
   if (best >= 0) {
     ctx->variant = best;
     rep += ", \"variant\": " + std::to_string(best) + ", \"cached\": true}";
@@ -661,10 +754,10 @@ extern "C" lbm_status lbm_autotune(lbm_ctx *ctx, int32_t steps_per_trial, const 
     LBM_CK(cudaEventCreate(&e1));
     double ms[lbm::NVAR];
     best = 0;
-    for (int v = 0; v < lbm::NVAR && s == LBM_OK; v++) {
+    for (int v = 0; v < nvar && s == LBM_OK; v++) {
       dim3 g_, b_;
       size_t sm_;
-      if (!step_config(ctx, v, &g_, &b_, &sm_)) {
+      if (!ctx->mk && !step_config(ctx, v, &g_, &b_, &sm_)) {
         ms[v] = INFINITY;
         continue;
       }
@@ -697,7 +790,7 @@ extern "C" lbm_status lbm_autotune(lbm_ctx *ctx, int32_t steps_per_trial, const 
     ctx->variant = best;
     std::string arr = "[";
     char buf[64];
-    for (int v = 0; v < lbm::NVAR; v++) {
+    for (int v = 0; v < nvar; v++) {
       if (std::isinf(ms[v])) std::snprintf(buf, sizeof buf, "%snull", v ? ", " : "");
       else std::snprintf(buf, sizeof buf, "%s%.5f", v ? ", " : "", ms[v]);
       arr += buf;

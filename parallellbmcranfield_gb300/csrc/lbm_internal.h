@@ -53,6 +53,17 @@ struct KernelSet {
   const void *reduce;        // k_reduce_partials
   int elem_size;
 };
+// Launch table of the moment storage (LBM_FP16NEQ, lbm_mom_inst.cu).
+struct MomKernels {
+  const void *step[4][3];  // [model 1..3][tile variant: 2, 4, 8 rows per thread]
+  const void *special[4];  // [model] class-3 / class-2 nodes from the compact list
+  const void *init[4];     // [model]
+  const void *finish;
+  const void *resid;
+  const void *reduce;
+};
+const MomKernels &kernels_mom();
+
 const KernelSet &kernels_f64();
 const KernelSet &kernels_f32();
 const KernelSet &kernels_f16();
@@ -63,6 +74,6 @@ const KernelSet &kernels_b16();
 namespace lbm {
 // Diagnostics reduction with the library's fixed device scratch array
 // (lbm_noalloc.cu); performs no device allocation.
-lbm_status check_noalloc(const KernelSet *ks, const StepArgs &a, int layout, dim3 grid,
+lbm_status check_noalloc(const void *finish, const void *reduce, const StepArgs &a, dim3 grid,
                          cudaStream_t stream, double sums[NSUM]);
 }  // namespace lbm

@@ -1,0 +1,562 @@
+// Moment storage (LBM_FP16NEQ): the state between launches is each node's
+// post-collision moments instead of its nine post-collision populations.
+//
+// Why.  With 16-bit populations the rounding of every store lands in the
+// conserved moments (mass and momentum), which no collision relaxes: the slow
+// viscous modes sum those errors up and the steady state ends 1e-3..1e-2 off
+// the FP64 one.  Stored as moments, the conserved ones keep 24 bits and only
+// the six non-conserved moments are 16-bit; a rounding error there is
+// relaxed by the next collision and reaches the momentum equation only as
+// the divergence of a stress error.
+//
+// Per node (A-B pattern, 21 bytes):
+//   planes 0..2   int16  high 16 bits of Q(rho - rho0), Q(j_x), Q(j_y)
+//   planes 3..8   FP16   n_i = (m*_i - b_i) * neq_scale, i = 1, 2, 4, 6, 7, 8
+//   bytes  0..2   uint8  low 8 bits of the three fixed-point values
+// Q(x) = floor(x / step + u) is a 24-bit signed fixed-point number with a
+// per-node, per-generation dither u in [0, 1) (unbiased rounding; steps from
+// the host: the density range +-0.5 rho0, the momentum range +-0.25 rho0); a value
+// beyond the range is not stored and sets the step's flag (value 2).  b_i is
+// a storage reference, a polynomial of the stored conserved moments
+// (b1 = -2 rho~ + 3 |j|^2, b2 = rho~ - 3 |j|^2, b4 = -j_x, b6 = -j_y,
+// b7 = (j_x^2 - j_y^2) / rho0, b8 = j_x j_y / rho0; rho~ = rho - rho0), so that
+// the stored n_i are the small non-equilibrium parts.  Moments are those of
+// the reference's MRT transform (serial/CellFunctions.c:37-47) applied to the
+// deviations d_k = f_k - w_k rho0.
+//
+// Nodes with boundary work (class 3) keep their post-collision populations
+// in FP32 in a side array indexed by their record instead (the boundary
+// treatment reads populations, and the corners' large non-equilibrium parts
+// lose most to 16 bits).  Fluid nodes next to them (class 2 in this mode)
+// are updated together with them by k_special_mom, so the bulk kernel never
+// reads a class-3 node.
+#pragma once
+#include "lbm_device.cuh"
+
+namespace lbm {
+
+constexpr int MOM_QMAX = (1 << 23) - 1;     // largest fixed-point magnitude
+
+// Byte offsets of the planes in one moment buffer of `plane` nodes per plane.
+__device__ __forceinline__ const int16_t *mom_hi(const void *b, const StepArgs &a, int p) {
+  return (const int16_t *)b + (long long)p * a.plane;
+}
+__device__ __forceinline__ const __half *mom_n(const void *b, const StepArgs &a, int i) {
+  return (const __half *)b + (long long)(3 + i) * a.plane;
+}
+__device__ __forceinline__ const uint8_t *mom_lo(const void *b, const StepArgs &a, int p) {
+  return (const uint8_t *)b + 18 * a.plane + (long long)p * a.plane;
+}
+
+// The stored moment set of one node in deviation form: r = rho - rho0,
+// x = j_x, y = j_y, n[6] = m*_i - b_i (i = 1, 2, 4, 6, 7, 8).
+struct MomSet {
+  float r, x, y, n[6];
+};
+
+// Post-collision deviations d*_k = (Minv m*)_k of a stored moment set
+// (Minv = (1/36) x integers, serial/CellFunctions.c:49-59).
+__device__ __forceinline__ void mom_to_pops(const MomSet &s, const StepArgs &a, float d[9]) {
+  const float jj = s.x * s.x + s.y * s.y, i0 = a.fx_irho0;
+  const float m1 = fmaf(3.f, jj, -2.f * s.r) + s.n[0];
+  const float m2 = fmaf(-3.f, jj, s.r) + s.n[1];
+  const float m4 = s.n[2] - s.x, m6 = s.n[3] - s.y;
+  const float m7 = (s.x * s.x - s.y * s.y) * i0 + s.n[4];
+  const float m8 = s.x * s.y * i0 + s.n[5];
+  const float c = 1.f / 36.f;
+  const float ax = 4.f * s.r - m1 - 2.f * m2, dg = 4.f * s.r + 2.f * m1 + m2;
+  const float P = 9.f * m7;
+  const float Xd = fmaf(3.f, m4, 6.f * s.x), Yd = fmaf(3.f, m6, 6.f * s.y), Q = 9.f * m8;
+  d[5] = c * (dg + Xd + Yd + Q);
+  d[6] = c * (dg - Xd + Yd - Q);
+  d[7] = c * (dg - Xd - Yd + Q);
+  d[8] = c * (dg + Xd - Yd - Q);
+  // c = 1/36 is not exact in FP32: Minv applied as above would scale mass and
+  // momentum by 36 c = 1 + 7.5e-9 every step, a bias the slow modes sum up.
+  // So only the non-conserved shape comes from Minv; the axis pairs take the
+  // momentum that the diagonals leave and the rest population the mass, which
+  // makes sum d = r and sum c d = j up to one rounding each.
+  const float s13 = c * (2.f * ax + 2.f * P), s24 = c * (2.f * ax - 2.f * P);
+  const float dx = s.x - ((d[5] - d[7]) + (d[8] - d[6]));
+  const float dy = s.y - ((d[5] - d[7]) + (d[6] - d[8]));
+  d[1] = 0.5f * (s13 + dx);
+  d[3] = 0.5f * (s13 - dx);
+  d[2] = 0.5f * (s24 + dy);
+  d[4] = 0.5f * (s24 - dy);
+  d[0] = s.r - (((d[1] + d[3]) + (d[2] + d[4])) + ((d[5] + d[7]) + (d[6] + d[8])));
+}
+
+// Fixed point <-> float of one conserved moment (p: 0 density, 1 and 2 momentum).
+__device__ __forceinline__ float fx_step(const StepArgs &a, int p) { return p == 0 ? a.fx_rho : a.fx_j; }
+__device__ __forceinline__ float fx_istep(const StepArgs &a, int p) { return p == 0 ? a.fx_irho : a.fx_ij; }
+
+// Stored moment set of node z (any class but special; solid and padding
+// nodes read as all zero, i.e. f = w rho0).
+__device__ __forceinline__ MomSet mom_load(const StepArgs &a, const void *b, long long z) {
+  MomSet s;
+  float q[3];
+#pragma unroll
+  for (int p = 0; p < 3; p++) {
+    const int hi = __ldg(mom_hi(b, a, p) + z);
+    const int lo = __ldg(mom_lo(b, a, p) + z);
+    q[p] = (float)(hi * 256 + lo) * fx_step(a, p);
+  }
+  s.r = q[0];
+  s.x = q[1];
+  s.y = q[2];
+#pragma unroll
+  for (int i = 0; i < 6; i++) s.n[i] = __half2float(__ldg(mom_n(b, a, i) + z)) * a.neq_is;
+  return s;
+}
+
+// Moments (deviation form) of deviation populations d: r, j and the six
+// non-conserved ones in the order 1, 2, 4, 6, 7, 8.
+__device__ __forceinline__ void pops_to_mom(const float d[9], float &r, float &jx, float &jy,
+                                            float m[6]) {
+  const float a13 = d[1] + d[3], a24 = d[2] + d[4], a14 = a13 + a24;
+  const float p57 = d[5] + d[7], p68 = d[6] + d[8], a58 = p57 + p68;
+  r = (d[0] + a14) + a58;
+  const float d13 = d[1] - d[3], d24 = d[2] - d[4];
+  const float e57 = d[5] - d[7], e86 = d[8] - d[6];
+  const float x58 = e57 + e86, y58 = e57 - e86;
+  jx = d13 + x58;
+  jy = d24 + y58;
+  m[0] = 2.f * a58 - a14 - 4.f * d[0];
+  m[1] = (4.f * d[0] + a58) - 2.f * a14;
+  m[2] = x58 - 2.f * d13;
+  m[3] = y58 - 2.f * d24;
+  m[4] = a13 - a24;
+  m[5] = p57 - p68;
+}
+
+// Collision in moment space (deviation form; rho = rho0 + r).  MRT is the
+// reference's operator (serial/CellFunctions.c:401-438: meq_1 = -2 rho +
+// 3 |j|^2, meq_2 = rho - 3 |j|^2, s = 1.4, 1.4, 1.2, 1.2, omega, omega);
+// BGK and TRT are the same relaxation of M f toward M f_eq with the
+// second-order f_eq (meq_1 = -2 rho + 3 |j|^2 / rho, meq_2 = rho -
+// 3 |j|^2 / rho), at rates omega (BGK) or omega for the even and omegaA for
+// the odd moments 4, 6 (TRT, serial/CellFunctions.c:372-395).  m[] becomes
+// the post-collision moments; r and j are conserved.
+template <int MODEL>
+__device__ __forceinline__ void collide_mom(float r, float jx, float jy, float m[6],
+                                           const StepArgs &a) {
+  const float rho = (float)a.rho0 + r;
+  const float inv = 1.f / rho;
+  const float jj = jx * jx + jy * jy;
+  const float q = MODEL == 3 ? jj : jj * inv;
+  const float e1 = fmaf(3.f, q, -2.f * r), e2 = fmaf(-3.f, q, r);
+  const float e7 = (jx * jx - jy * jy) * inv, e8 = jx * jy * inv;
+  const float om = (float)a.omega;
+  const float s12 = MODEL == 3 ? 1.4f : om;
+  const float s46 = MODEL == 3 ? 1.2f : (MODEL == 2 ? (float)a.omegaA : om);
+  m[0] -= s12 * (m[0] - e1);
+  m[1] -= s12 * (m[1] - e2);
+  m[2] -= s46 * (m[2] + jx);
+  m[3] -= s46 * (m[3] + jy);
+  m[4] -= om * (m[4] - e7);
+  m[5] -= om * (m[5] - e8);
+}
+
+// Fixed-point code of a conserved moment, rounded with a dither u in [0, 1):
+// floor(v / step + u).  Rounding to nearest would give a node at steady state
+// the same error every step, and the mass of the domain would drift by their
+// sum each step; with the dither the expected code is v / step and the errors
+// of successive steps are independent.  `ok` turns false out of range.
+__device__ __forceinline__ int fx_code(float v, float istep, float u, bool &ok) {
+  // x + u would round to the grid of x (1/8 at |x| ~ 2^20) and bias the
+  // dither; the integer part and the fraction of x are exact instead
+  const float x = v * istep;
+  const float xi = floorf(x);
+  const float t = xi + ((x - xi) > u ? 1.f : 0.f);
+  ok = ok && fabsf(t) <= (float)MOM_QMAX;
+  return (int)fminf(fmaxf(t, -(float)MOM_QMAX), (float)MOM_QMAX);
+}
+
+// 32-bit integer hash (the "lowbias32" finaliser of C. Wellons' hash-prospector
+// search: xor-shift / multiply rounds); three 10-bit dithers per node and
+// generation.
+__device__ __forceinline__ uint32_t mix32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+__device__ __forceinline__ void dithers(long long z, unsigned gen, float u[3]) {
+  const uint32_t h = mix32((uint32_t)z ^ mix32(gen * 0x9e3779b9u + 0x632be5abu));
+#pragma unroll
+  for (int p = 0; p < 3; p++) u[p] = (float)((h >> (10 * p)) & 1023u) * (1.f / 1024.f) + (1.f / 2048.f);
+}
+
+// Encoded moment set (codes and FP16 non-equilibrium parts) of post-collision
+// moments; the references b_i come from the stored (rounded) r and j.
+struct MomCode {
+  int q[3];
+  __half n[6];
+};
+__device__ __forceinline__ MomCode mom_encode(float r, float jx, float jy, const float m[6],
+                                              const StepArgs &a, long long z, bool &ok) {
+  MomCode c;
+  float u[3];
+  dithers(z, a.gen, u);
+  c.q[0] = fx_code(r, a.fx_irho, u[0], ok);
+  c.q[1] = fx_code(jx, a.fx_ij, u[1], ok);
+  c.q[2] = fx_code(jy, a.fx_ij, u[2], ok);
+  const float rs = (float)c.q[0] * a.fx_rho, xs = (float)c.q[1] * a.fx_j,
+              ys = (float)c.q[2] * a.fx_j;
+  const float jj = xs * xs + ys * ys, i0 = a.fx_irho0;
+  const float b[6] = {fmaf(3.f, jj, -2.f * rs), fmaf(-3.f, jj, rs), -xs, -ys,
+                      (xs * xs - ys * ys) * i0, xs * ys * i0};
+#pragma unroll
+  for (int i = 0; i < 6; i++) c.n[i] = __float2half_rn((m[i] - b[i]) * a.neq_s);
+  return c;
+}
+
+__device__ __forceinline__ void mom_store(const StepArgs &a, void *b, long long z,
+                                          const MomCode &c) {
+#pragma unroll
+  for (int p = 0; p < 3; p++) {
+    ((int16_t *)mom_hi(b, a, p))[z] = (int16_t)(c.q[p] >> 8);
+    ((uint8_t *)mom_lo(b, a, p))[z] = (uint8_t)(c.q[p] & 0xff);
+  }
+#pragma unroll
+  for (int i = 0; i < 6; i++) ((__half *)mom_n(b, a, i))[z] = c.n[i];
+}
+
+// Out-of-range or non-finite result: the step's flag (checked by the host).
+__device__ __forceinline__ void mom_flag(const StepArgs &a, bool ok, float probe) {
+  if (a.nanflag) {
+    if (!(fabsf(probe) <= 3.0e38f)) *a.nanflag = 1;
+    else if (!ok) *a.nanflag = 2;
+  }
+}
+
+// METAF of any node in deviation form (DEV) or absolute: class 3 from the
+// FP32 side array of the current parity, solid as zero, others decoded.
+template <bool DEV>
+struct AccMom {
+  using R = float;
+  static constexpr bool dev = DEV;
+  const StepArgs &a;
+  __device__ AccMom(const StepArgs &a_, const void *) : a(a_) {}
+  __device__ __forceinline__ float meta(long long z, int k) const {
+    const uint8_t c = a.cls[z];
+    const float w0 = wgt<float>(k) * (float)a.rho0;
+    float d;
+    if (c == CLS_SOLID) {
+      d = -w0;
+    } else if (c == CLS_SPECIAL) {
+      d = a.ss_src[(size_t)a.aux[z] * 9 + k];
+    } else {
+      float p[9];
+      mom_to_pops(mom_load(a, a.src, z), a, p);
+      d = p[k];
+    }
+    return DEV ? d : d + w0;
+  }
+  // All nine METAF of a non-solid node (deviation form).
+  __device__ __forceinline__ void all(long long z, float d[9]) const {
+    if (a.cls[z] == CLS_SPECIAL) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) d[k] = a.ss_src[(size_t)a.aux[z] * 9 + k];
+    } else {
+      mom_to_pops(mom_load(a, a.src, z), a, d);
+    }
+  }
+};
+
+// ------------------------------------------------------------------ bulk step
+
+// Decoded post-collision deviations of the two nodes (x0, x0+1) of row r.
+__device__ __forceinline__ void mom_pair(const StepArgs &a, const void *b, int r, int x0,
+                                         float2 d[9]) {
+  const long long z = (long long)r * a.pitch + x0;
+  MomSet s0, s1;
+  float q0[3], q1[3];
+#pragma unroll
+  for (int p = 0; p < 3; p++) {
+    const uint32_t hw = __ldg((const unsigned *)(mom_hi(b, a, p) + z));
+    const uint32_t lw = __ldg((const unsigned short *)(mom_lo(b, a, p) + z));
+    const int h0 = (int)(int16_t)(hw & 0xffffu), h1 = (int)(int16_t)(hw >> 16);
+    q0[p] = (float)(h0 * 256 + (int)(lw & 0xffu)) * fx_step(a, p);
+    q1[p] = (float)(h1 * 256 + (int)(lw >> 8)) * fx_step(a, p);
+  }
+  s0.r = q0[0]; s0.x = q0[1]; s0.y = q0[2];
+  s1.r = q1[0]; s1.x = q1[1]; s1.y = q1[2];
+#pragma unroll
+  for (int i = 0; i < 6; i++) {
+    const uint32_t w = __ldg((const unsigned *)(mom_n(b, a, i) + z));
+    __half2 h;
+    memcpy(&h, &w, 4);
+    const float2 f = __half22float2(h);
+    s0.n[i] = f.x * a.neq_is;
+    s1.n[i] = f.y * a.neq_is;
+  }
+  float p0[9], p1[9];
+  mom_to_pops(s0, a, p0);
+  mom_to_pops(s1, a, p1);
+#pragma unroll
+  for (int k = 0; k < 9; k++) d[k] = make_float2(p0[k], p1[k]);
+}
+
+// Bulk step of the moment storage (A-B): each thread owns the node pair
+// (x0, x0+1) of NPT consecutive rows.  It decodes the source rows y0-1 ..
+// y0+NPT in order; a decoded row r hands its populations with c_y = +1 to
+// destination row r+1, c_y = 0 to row r and c_y = -1 to row r-1, and the
+// +-1 x-shift comes from the neighbouring lane (warp shuffle; lanes 0 and 31
+// decode the node beyond the warp themselves).  When row r is decoded, row
+// r-1 has all nine pulled populations: it collides and stores.  Every lane
+// runs the same instructions; only class-1 nodes are stored (class 2/3 nodes
+// are k_special_mom's, solid nodes are never written).
+template <int MODEL, int NPT>
+__global__ void __launch_bounds__(128) k_step_mom(const __grid_constant__ StepArgs a) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int x0 = (blockIdx.x * 128 + threadIdx.x) * 2;
+  const int y0 = blockIdx.y * NPT;
+  if (x0 - lane * 2 >= a.pitch) return;  // the whole warp lies past the row
+  bool any = false;
+  uint8_t cl[NPT][2];
+#pragma unroll
+  for (int j = 0; j < NPT; j++) {
+    const int y = y0 + j;
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+      cl[j][i] = (y < a.m && x0 + i < a.n) ? a.cls[(long long)y * a.pitch + x0 + i] : (uint8_t)0;
+      any = any || cl[j][i] == CLS_BULK;
+    }
+  }
+  if (!__any_sync(FULL, any)) return;
+  float2 F[NPT][9];
+  bool ok = true;
+#pragma unroll
+  for (int j = -1; j <= NPT; j++) {
+    const int r = y0 + j;
+    float2 d[9];
+    const bool in = r >= 0 && r < a.m;  // warp-uniform
+    if (in) {
+      mom_pair(a, a.src, r, x0, d);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 9; k++) d[k] = make_float2(0.f, 0.f);
+    }
+    // the node beyond the warp's edge: x0-1 for lane 0, x0+2 for lane 31
+    float h[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) h[k] = 0.f;
+    if (in && (lane == 0 || lane == 31)) {
+      const int hx = lane == 0 ? x0 - 1 : x0 + 2;
+      if (hx >= 0 && hx < a.n) mom_to_pops(mom_load(a, a.src, (long long)r * a.pitch + hx), a, h);
+    }
+    // shifted pairs for the destinations of this source row
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      const int dj = j + CY[k];  // destination row index (y + c_y)
+      if (dj < 0 || dj >= NPT) continue;
+      float2 v = d[k];
+      if (CX[k] == 1) {
+        float left = __shfl_up_sync(FULL, d[k].y, 1);
+        if (lane == 0) left = h[k];
+        v = make_float2(left, d[k].x);
+      } else if (CX[k] == -1) {
+        float right = __shfl_down_sync(FULL, d[k].x, 1);
+        if (lane == 31) right = h[k];
+        v = make_float2(d[k].y, right);
+      }
+      F[dj][k] = v;
+    }
+    // destination row j-1 is complete
+    const int jd = j - 1;
+    if (jd >= 0 && jd < NPT) {
+      const int y = y0 + jd;
+#pragma unroll
+      for (int i = 0; i < 2; i++) {
+        if (cl[jd][i] != CLS_BULK) continue;
+        float f[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) f[k] = i ? F[jd][k].y : F[jd][k].x;
+        float rr, jx, jy, m[6];
+        pops_to_mom(f, rr, jx, jy, m);
+        collide_mom<MODEL>(rr, jx, jy, m, a);
+        const long long z = (long long)y * a.pitch + x0 + i;
+        const MomCode c = mom_encode(rr, jx, jy, m, a, z, ok);
+        mom_flag(a, ok, rr + m[4]);
+        mom_store(a, a.dst, z, c);
+      }
+    }
+  }
+}
+
+// Nodes with boundary work (class 3) and their fluid neighbours (class 2),
+// one thread each, from a compact list.  Class 3: the reference's boundary
+// treatment (special_node, on the populations the accessor reconstructs),
+// collision, FP32 side array.  Class 2: pull (from side array or decoded
+// moments), collision, moment store.
+template <int MODEL>
+__global__ void __launch_bounds__(128) k_special_mom(const __grid_constant__ StepArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.mlist_n) return;
+  const long long node = a.mlist[i];
+  const uint8_t c = a.cls[node];
+  AccMom<true> acc(a, nullptr);
+  float F[9], M[9];
+  if (c == CLS_SPECIAL) {
+    float mac[3];
+    special_node<float>(a, acc, node, F, mac);
+    collide_dev<MODEL>(F, mac[0], mac[1], mac[2], a, M);
+    float *o = a.ss_dst + (size_t)a.aux[node] * 9;
+#pragma unroll
+    for (int k = 0; k < 9; k++) o[k] = M[k];
+    return;
+  }
+#pragma unroll
+  for (int k = 0; k < 9; k++) F[k] = acc.meta(node - nb(k, a.pitch), k);
+  float rr, jx, jy, m[6];
+  pops_to_mom(F, rr, jx, jy, m);
+  collide_mom<MODEL>(rr, jx, jy, m, a);
+  bool ok = true;
+  const MomCode code = mom_encode(rr, jx, jy, m, a, node, ok);
+  mom_flag(a, ok, rr + m[4]);
+  mom_store(a, a.dst, node, code);
+}
+
+// First collision after lbm_set_state: f = f0 or f_eq(rho, u, v), collided,
+// stored in the moment form (class 3 in the side array).
+template <int MODEL>
+__global__ void __launch_bounds__(128) k_init_mom(const __grid_constant__ StepArgs a,
+                                                  const double *f0, const double *rho0,
+                                                  const double *u0, const double *v0) {
+  int x, y;
+  if (!node_xy(a, x, y)) return;
+  const long long node = (long long)y * a.pitch + x;
+  const long long cell = (long long)y * a.n + x;
+  const uint8_t c = a.cls[node];
+  if (c == CLS_SOLID) return;
+  const double rho = rho0[cell], u = u0[cell], v = v0[cell];
+  double fe[9];
+  if (f0) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) fe[k] = f0[cell * 9 + k];
+  } else {
+    equilibrium<double>(rho, u, v, fe);
+  }
+  float F[9], M[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) F[k] = (float)(fe[k] - wgt<double>(k) * a.rho0);
+  collide_dev<MODEL>(F, (float)rho, (float)u, (float)v, a, M);
+  if (c == CLS_SPECIAL) {
+    float *o = a.ss_dst + (size_t)a.aux[node] * 9;
+#pragma unroll
+    for (int k = 0; k < 9; k++) o[k] = M[k];
+    return;
+  }
+  float rr, jx, jy, m[6];
+  pops_to_mom(M, rr, jx, jy, m);
+  bool ok = true;
+  const MomCode code = mom_encode(rr, jx, jy, m, a, node, ok);
+  mom_flag(a, ok, rr + m[4]);
+  mom_store(a, a.dst, node, code);
+}
+
+// Read-only: F_{t+1}, macroscopic fields and FP64 diagnostics (the sums of
+// k_finish, same lanes and launch shape) through the moment accessor.
+__global__ void __launch_bounds__(128) k_finish_mom(const __grid_constant__ StepArgs a,
+                                                    const FinishOut o) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc[NSUM];
+  float part[NSUM];
+#pragma unroll
+  for (int i = 0; i < NSUM; i++) acc[i] = 0.0, part[i] = 0.f;
+  AccMom<true> am(a, nullptr);
+  int chunk = 0;
+  for (int y = blockIdx.y; y < a.m && x < a.n; y += gridDim.y) {
+    const long long node = (long long)y * a.pitch + x;
+    const long long cell = (long long)y * a.n + x;
+    const uint8_t c = a.cls[node];
+    if (c == CLS_SOLID) {
+      if (o.f)
+        for (int k = 0; k < 9; k++) o.f[cell * 9 + k] = 0.0;
+      if (o.metaf)
+        for (int k = 0; k < 9; k++) o.metaf[cell * 9 + k] = 0.0;
+      if (o.rho) o.rho[cell] = o.rho_solid[cell];
+      if (o.u) o.u[cell] = o.u_solid[cell];
+      if (o.v) o.v[cell] = o.v_solid[cell];
+      continue;
+    }
+    float F[9], M[9], rho, u, v;
+    if (c != CLS_SPECIAL) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) F[k] = am.meta(node - nb(k, a.pitch), k);
+      const float rt = ((F[0] + F[1]) + (F[2] + F[3])) + ((F[4] + F[5]) + (F[6] + F[7])) + F[8];
+      const float jx = (F[1] - F[3]) + (F[5] - F[6]) + (F[8] - F[7]);
+      const float jy = (F[2] - F[4]) + (F[5] - F[7]) + (F[6] - F[8]);
+      rho = (float)a.rho0 + rt;
+      u = jx / rho;
+      v = jy / rho;
+    } else {
+      float mac[3];
+      special_node<float>(a, am, node, F, mac);
+      rho = mac[0];
+      u = mac[1];
+      v = mac[2];
+    }
+    am.all(node, M);
+    float l2 = 0.f;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      const float dk = F[k] - M[k];
+      l2 += dk * dk;
+    }
+    if (o.f)
+      for (int k = 0; k < 9; k++) o.f[cell * 9 + k] = (double)F[k] + wgt<double>(k) * a.rho0;
+    if (o.metaf)
+      for (int k = 0; k < 9; k++) o.metaf[cell * 9 + k] = (double)M[k] + wgt<double>(k) * a.rho0;
+    if (o.rho) o.rho[cell] = (double)rho;
+    if (o.u) o.u[cell] = (double)u;
+    if (o.v) o.v[cell] = (double)v;
+    const float uu = u * u + v * v;
+    part[S_L2] += l2;
+    part[S_MASS] += rho;
+    part[S_MX] += rho * u;
+    part[S_MY] += rho * v;
+    part[S_UU] += uu;
+    part[S_VMAX] = fmaxf(part[S_VMAX], sqrtf(uu));
+    if (rho != rho || u != u || v != v) part[S_NAN] += 1.f;
+    if (o.uprev) {
+      const float pu = o.uprev[cell], pv = o.vprev[cell];
+      part[S_DU] += (u - pu) * (u - pu) + (v - pv) * (v - pv);
+      o.uprev[cell] = u;
+      o.vprev[cell] = v;
+    }
+    if (c == CLS_SPECIAL) {
+      const BRec &r = a.rec[a.aux[node]];
+      if (r.flags & FL_DRAG) {
+        const uint32_t wall = (r.flags >> FL_WALL_SHIFT) & 0x1FFu;
+        for (int k = 1; k < 9; k++)
+          if ((wall >> k) & 1u) {
+            const double g = (double)M[k] + (double)F[OPP[k]] + 2.0 * wgt<double>(k) * a.rho0;
+            acc[S_FX] += g * CX[k];
+            acc[S_FY] += g * CY[k];
+          }
+      }
+    }
+    if (++chunk == 8) {
+      chunk = 0;
+#pragma unroll
+      for (int i = 0; i < NSUM; i++) {
+        if (i == S_VMAX) acc[i] = fmax(acc[i], (double)part[i]);
+        else if (i != S_FX && i != S_FY) acc[i] += (double)part[i];
+        part[i] = 0.f;
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < NSUM; i++) {
+    if (i == S_VMAX) acc[i] = fmax(acc[i], (double)part[i]);
+    else if (i != S_FX && i != S_FY) acc[i] += (double)part[i];
+  }
+  block_reduce_store(acc, o.partial);
+}
+
+}  // namespace lbm

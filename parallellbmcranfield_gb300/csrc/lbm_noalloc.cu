@@ -67,7 +67,7 @@ lbm_status scratch_for_current_device(double **out) {
 
 namespace lbm {
 
-lbm_status check_noalloc(const KernelSet *ks, const StepArgs &a, int layout, dim3 grid,
+lbm_status check_noalloc(const void *finish, const void *reduce, const StepArgs &a, dim3 grid,
                          cudaStream_t stream, double sums[NSUM]) {
   const long long nblk = (long long)grid.x * grid.y;
   if (nblk > kNoallocMaxBlocks)
@@ -85,11 +85,11 @@ lbm_status check_noalloc(const KernelSet *ks, const StepArgs &a, int layout, dim
   o.partial = partial;
   StepArgs args = a;
   void *fargs[] = {&args, &o};
-  cudaError_t e = cudaLaunchKernel(ks->finish[layout], grid, dim3(128), fargs, 0, stream);
+  cudaError_t e = cudaLaunchKernel(finish, grid, dim3(128), fargs, 0, stream);
   if (e != cudaSuccess) return fail(LBM_CUDA, std::string("finish launch: ") + cudaGetErrorString(e));
   int nb = (int)nblk;
   void *rargs[] = {&partial, &nb, &total};
-  e = cudaLaunchKernel(ks->reduce, dim3(1), dim3(32 * NSUM), rargs, 0, stream);
+  e = cudaLaunchKernel(reduce, dim3(1), dim3(32 * NSUM), rargs, 0, stream);
   if (e != cudaSuccess) return fail(LBM_CUDA, std::string("reduce launch: ") + cudaGetErrorString(e));
   e = cudaMemcpyAsync(sums, total, NSUM * sizeof(double), cudaMemcpyDeviceToHost, stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(stream);

@@ -7,7 +7,7 @@
 // iteration, or one per --check-every), autosave_iterNNNNN.csv|dat,
 // SerialTimeMeasuerment.dat and FinalData.csv|dat.
 //
-//   lbm_solver [--dir CASE] [--precision fp64|fp32|fp16dev|bf16dev] [--pattern ab|aa]
+//   lbm_solver [--dir CASE] [--precision fp64|fp32|fp16dev|bf16dev|fp16neq] [--pattern ab|aa]
 //              [--tile N] [--check-every K] [--final-data compat|fields|both]
 //
 // FinalData keeps the reference's index quirk by default (serial/FileIO.c:368
@@ -148,7 +148,7 @@ double now_s() {
 
 int usage() {
   std::fprintf(stderr,
-               "usage: lbm_solver [--dir CASE] [--precision fp64|fp32|fp16dev|bf16dev] "
+               "usage: lbm_solver [--dir CASE] [--precision fp64|fp32|fp16dev|bf16dev|fp16neq] "
                "[--pattern ab|aa] [--tile N] [--check-every K] [--final-data compat|fields|both]\n");
   return 2;
 }
@@ -165,7 +165,7 @@ int main(int argc, char **argv) {
     else if (a == "--precision") {
       std::string p = val();
       precision = p == "fp64" ? LBM_FP64 : p == "fp32" ? LBM_FP32 : p == "fp16dev" ? LBM_FP16DEV
-                : p == "bf16dev" ? LBM_BF16DEV : -1;
+                : p == "bf16dev" ? LBM_BF16DEV : p == "fp16neq" ? LBM_FP16NEQ : -1;
       if (precision < 0) return usage();
     } else if (a == "--pattern") {
       std::string p = val();

@@ -57,6 +57,9 @@ constexpr int NVAR = 6;
 constexpr TileVariant VARS[NVAR] = {
     {0, 128, 1, 1, 0, 0, 0},   {0, 64, 1, 4, 0, 0, 0},   {1, 128, 4, 1, 0, 0, 0},
     {2, 0, 0, 0, 128, 4, 2},   {3, 128, 2, 2, 0, 0, 0},  {3, 128, 2, 4, 0, 0, 0}};
+// Bulk-step tiles of the moment storage: 128 threads x 2 nodes, these rows per thread.
+constexpr int MOM_NVAR = 3;
+constexpr int MOM_NPT[MOM_NVAR] = {2, 4, 8};
 constexpr int TMA_MAX_SMEM = 200 * 1024;  // dynamic shared memory budget of one TMA block
 constexpr int TMA_MAX_STAGES = 4;
 
@@ -87,6 +90,15 @@ struct StepArgs {
   int tma_tiles_x, tma_tiles_y;
   int pf_blocks;            // paired 16-bit step: L2 prefetch for the block this many launch
                             // positions ahead (a fraction of a wave of resident blocks); 0 = off
+  // moment storage (LBM_FP16NEQ)
+  float *ss_src, *ss_dst;   // FP32 post-collision deviations of class-3 nodes (9 per record)
+  const uint32_t *mlist;    // class-3 and class-2 nodes, updated by the special-node kernel
+  int mlist_n;
+  float fx_rho, fx_irho;    // fixed-point step of rho - rho0 and its inverse
+  float fx_j, fx_ij;        // fixed-point step of j and its inverse
+  float fx_irho0;           // 1 / rho0
+  float neq_s, neq_is;      // scale of the stored non-equilibrium moments and its inverse
+  unsigned gen;             // generation written by this launch (seed of the rounding dither)
 };
 
 // Outputs of the read-only finish kernel (any pointer may be null).

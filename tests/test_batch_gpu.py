@@ -83,3 +83,21 @@ def test_batch_convergence_freezes_cases():
     f1 = b.fields(0)
     b.close()
     assert np.isfinite(f1["u"]).all()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16dev"])
+def test_batch_matches_single_contexts_reduced(precision):
+    """FP32 / FP16-dev: the per-tile bulk kernel and the boundary-node pass do
+    the single-domain arithmetic per node (same operators, same storage)."""
+    cs = batch_cases(3)
+    b = G.Batch(cs, precision=precision)
+    b.set_rest()
+    b.run(60, check_every=20, tol=-1.0)
+    for c, (mesh, params) in enumerate(cs):
+        got = b.fields(c)
+        want = single(mesh, params, G.PRECISIONS[precision], 61)
+        speed = np.sqrt(want["u"] ** 2 + want["v"] ** 2).max()
+        err = np.sqrt((got["u"] - want["u"]) ** 2 + (got["v"] - want["v"]) ** 2).max() / speed
+        assert err <= 1e-5, (c, err)
+        assert np.abs(got["rho"] - want["rho"]).max() <= 1e-6
+    b.close()

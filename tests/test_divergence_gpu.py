@@ -35,7 +35,8 @@ def planted(s, where):
 @pytest.mark.parametrize("precision,pattern,model,tile", [
     (G.FP32, G.AB, G.MRT, 1), (G.FP32, G.AA, G.MRT, 2), (G.FP32, G.AB, G.BGKW, 3),
     (G.FP32, G.AB, G.TRT, 4), (G.FP16DEV, G.AB, G.MRT, 5), (G.FP16DEV, G.AA, G.MRT, 6),
-    (G.FP16DEV, G.AB, G.TRT, 5), (G.BF16DEV, G.AB, G.MRT, 1)])
+    (G.FP16DEV, G.AB, G.TRT, 5), (G.BF16DEV, G.AB, G.MRT, 1), (G.FP16NEQ, G.AB, G.MRT, 1),
+    (G.FP16NEQ, G.AB, G.BGKW, 3)])
 def test_nan_in_a_bulk_node_is_reported(precision, pattern, model, tile):
     s = solver(precision, pattern, model, tile)
     centre = (s.m // 2) * s.n + s.n // 2
@@ -50,8 +51,9 @@ def test_nan_in_a_bulk_node_is_reported(precision, pattern, model, tile):
     s.close()
 
 
-def test_nan_next_to_a_wall_is_reported():
-    s = solver(G.FP16DEV, G.AB, G.MRT, 5)
+@pytest.mark.parametrize("precision,tile", [(G.FP16DEV, 5), (G.FP16NEQ, 2)])
+def test_nan_next_to_a_wall_is_reported(precision, tile):
+    s = solver(precision, G.AB, G.MRT, tile)
     planted(s, 1 * s.n + 1)  # the bottom-left fluid corner: a boundary node
     with pytest.raises(G.DivergedError):
         s.step(2, 0)

@@ -1,0 +1,91 @@
+"""GPU: evidence behind two workload results.
+
+Batched cavities (256 lid-driven cavities, sides log-uniform in [64, 1024],
+Re uniform in [100, 3200], lid 0.05, TRT, seed 20240603): every case that
+stopped on NaN has a lattice cell Reynolds number U / nu of 6.4 or more.  The
+smallest of them (65 x 65 nodes of fluid and wall, Re 2038 and Re 738) are
+run here in FP64 on the GPU and on the CPU oracle (the reference's TRT,
+serial/CellFunctions.c:372-395): both diverge, at the same step, so the NaN
+is the reference arithmetic's instability at that viscosity, not the
+library's.  A cavity of the same size at cell Re 6 stays finite, and a batch
+of the three freezes the two diverging cases without stopping the third.
+"""
+import numpy as np
+import pytest
+
+import parallellbmcranfield_gb300 as G
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+SIDE = 63  # fluid cells per side: 65 x 66 nodes, the smallest diverging cases of the batch
+W9 = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4)
+DIVERGING = [2038.1622561908594, 737.6543366610242]  # Re of batch cases 58 and 213
+STABLE_RE = SIDE * 6.0                                # cell Re 6
+CHUNK = 10
+
+
+def params(re):
+    return dict(uavg=0.05, vavg=0.0, rho_ini=1.0, viscosity=0.05 * SIDE / re, inlet_profile=2,
+                collision_model=G.TRT, curved_boundaries=1, outlet_profile=2)
+
+
+def oracle_nan_step(re, cap=3000):
+    mesh = G.Mesh.cavity(SIDE)
+    p = params(re)
+    port = O.Port(mesh.nodes, mesh.conns, uavg=p["uavg"], vavg=0.0, rho_ini=1.0,
+                  viscosity=p["viscosity"], inlet_profile=2, model=2, curved=1, outlet=2)
+    n, m = mesh.shape
+    N = n * m
+    port.set_state(np.tile(W9, (N, 1)), np.ones(N), np.zeros(N), np.zeros(N))
+    for it in range(CHUNK, cap + 1, CHUNK):
+        port.run(CHUNK, want_resid=False)
+        if not np.isfinite(port.state()["rho"]).all():
+            port.close()
+            return it
+    port.close()
+    return None
+
+
+def gpu_nan_step(re, precision, cap=3000):
+    mesh = G.Mesh.cavity(SIDE)
+    s = G.Solver(mesh, precision=precision, **params(re))
+    s.set_state(None, np.ones(s.N), np.zeros(s.N), np.zeros(s.N))
+    it = 0  # lbm_step(k) after lbm_set_state is the oracle's run(k)
+    try:
+        while it < cap:
+            s.step(CHUNK)  # reduced precision: the step's NaN flag raises here
+            it += CHUNK
+            s.check()      # FP64: the full-field sums see the NaN
+    except G.DivergedError:
+        s.close()
+        return it
+    s.close()
+    return None
+
+
+@pytest.mark.parametrize("re", DIVERGING)
+def test_diverging_batch_cases_diverge_in_the_reference_arithmetic(re):
+    ref = oracle_nan_step(re)
+    gpu64 = gpu_nan_step(re, G.FP64)
+    gpu32 = gpu_nan_step(re, G.FP32)
+    print(f"Re {re:.1f} (cell Re {re / SIDE:.1f}): NaN by step oracle {ref}, FP64 {gpu64}, "
+          f"FP32 {gpu32}")
+    assert ref is not None and ref < 1000
+    assert abs(gpu64 - ref) <= CHUNK  # bit-identical FP64 arithmetic: the same chunk
+    assert gpu32 is not None and abs(gpu32 - ref) <= 0.2 * ref
+
+
+def test_cell_re_6_stays_finite():
+    assert oracle_nan_step(STABLE_RE, cap=2000) is None
+    assert gpu_nan_step(STABLE_RE, G.FP32, cap=20000) is None
+
+
+def test_batch_freezes_the_diverging_cases():
+    cs = [(G.Mesh.cavity(SIDE), params(re)) for re in DIVERGING + [STABLE_RE]]
+    b = G.Batch(cs, precision="fp32")
+    r = b.run(2000, check_every=100, tol=-1.0, raise_on_nan=False)
+    assert list(r["converged"]) == [-1, -1, 0]
+    assert r["steps"][2] == 2000 and r["steps"][0] < 1000 and r["steps"][1] < 1000
+    assert np.isfinite(b.fields(2)["u"]).all()
+    b.close()

@@ -16,8 +16,8 @@ import parallellbmcranfield_gb300 as G
 
 pytestmark = pytest.mark.gpu
 
-TOL_RHO = 1e-4  # max |rho - rho_FP64| / max rho
-TOL_U = 2e-3    # max |(u, v) - (u, v)_FP64| / max |(u, v)_FP64|
+TOL_RHO = 2e-5  # max |rho - rho_FP64| / max rho
+TOL_U = 2e-4    # max |(u, v) - (u, v)_FP64| / max |(u, v)_FP64|
 FEQ_CASES = sorted(k for k, v in cases.ALL.items() if v[2] == "feq")
 
 
@@ -47,16 +47,17 @@ def test_fp16neq_against_fp64(name):
     assert abs(dlow["mass"] - dref["mass"]) <= TOL_RHO * abs(dref["mass"])
 
 
-def test_tiles_agree():
+@pytest.mark.parametrize("tile", [1, 2, 3])
+def test_every_tile_against_fp64(tile):
     """The three bulk tiles (2, 4, 8 rows per thread) do the same arithmetic per
-    node up to the compiler's choice of fused multiply-adds, whose last-bit
-    differences can move a dithered fixed-point code by one step."""
-    outs = [run("cavity_mrt_curved", G.FP16NEQ, tile=t)[0] for t in (1, 2, 3)]
-    speed = np.sqrt(outs[0]["u"] ** 2 + outs[0]["v"] ** 2).max()
-    for o in outs[1:]:
-        assert np.abs(o["rho"] - outs[0]["rho"]).max() <= 1e-6 * np.abs(outs[0]["rho"]).max()
-        for k in ("u", "v"):
-            assert np.abs(o[k] - outs[0][k]).max() <= 1e-5 * speed, k
+    node, but the compiler may fuse multiply-adds differently in each; a
+    last-bit difference can move a dithered fixed-point code by one step, so
+    the tiles are not bitwise equal: each meets the FP64 tolerances."""
+    ref, _ = run("cavity_mrt_curved", G.FP64)
+    low, _ = run("cavity_mrt_curved", G.FP16NEQ, tile=tile)
+    speed = np.sqrt(ref["u"] ** 2 + ref["v"] ** 2).max()
+    assert np.abs(low["rho"] - ref["rho"]).max() <= TOL_RHO * np.abs(ref["rho"]).max()
+    assert np.sqrt((low["u"] - ref["u"]) ** 2 + (low["v"] - ref["v"]) ** 2).max() <= TOL_U * speed
 
 
 def test_autotune_and_bytes():

@@ -252,6 +252,8 @@ typedef struct lbm_sg_config {
   float coarse_weight;     /* weight of the block-mean loss term (0 = off): the masked means of
                               output and target over coarse_block^2 cells are compared too */
   int32_t coarse_block;    /* divides height and width */
+  int32_t products;        /* 0: convolution products on tcgen05 (tensor-memory accumulators)
+                              where the shapes allow, 1: every product on the mma.sync kernels */
 } lbm_sg_config;
 lbm_status lbm_sg_create(const lbm_sg_config *cfg, lbm_sg **out);
 void lbm_sg_destroy(lbm_sg *s);

@@ -377,7 +377,8 @@ class lbm_sg_config(C.Structure):
                 ("out_channels", C.c_int32), ("base", C.c_int32), ("max_batch", C.c_int32),
                 ("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
                 ("seed", C.c_uint64), ("device", C.c_int32), ("weight_decay", C.c_float),
-                ("coarse_weight", C.c_float), ("coarse_block", C.c_int32)]
+                ("coarse_weight", C.c_float), ("coarse_block", C.c_int32),
+                ("products", C.c_int32)]
 
 
 def _load_sg(L):
@@ -409,11 +410,16 @@ class Surrogate:
 
     def __init__(self, height=256, width=256, in_channels=4, out_channels=3, base=32,
                  max_batch=8, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8, seed=0, device=0,
-                 weight_decay=0.0, coarse_weight=0.0, coarse_block=8):
+                 weight_decay=0.0, coarse_weight=0.0, coarse_block=8, products="tcgen05"):
+        """products: "tcgen05" (the convolution products on the 5th-generation
+        tensor cores where the shapes allow) or "mma" (every product on the
+        mma.sync kernels)."""
         L = self.L = _load_sg(load())
+        if products not in ("tcgen05", "mma"):
+            raise ValueError("products must be 'tcgen05' or 'mma'")
         self.cfg = lbm_sg_config(height, width, in_channels, out_channels, base, max_batch, lr,
                                  beta1, beta2, eps, seed, device, weight_decay, coarse_weight,
-                                 coarse_block)
+                                 coarse_block, 0 if products == "tcgen05" else 1)
         self.h = C.c_void_p()
         _check(L.lbm_sg_create(C.byref(self.cfg), C.byref(self.h)), "lbm_sg_create")
         n = C.c_int64()

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "lbm_internal.h"
+#include "lbm_tc.cuh"
 
 using lbm::fail;
 typedef __nv_bfloat16 bf16;
@@ -643,6 +644,7 @@ struct lbm_sg {
   std::vector<void *> allocs;
   float *ds_x = nullptr, *ds_y = nullptr, *ds_m = nullptr;
   int ds_count = 0;
+  int *d_err = nullptr;  // set by a tcgen05 kernel whose bounded wait gave up
 };
 
 namespace {
@@ -668,6 +670,67 @@ const void *gemm_fn(int bn) {
   return bn == 32 ? (const void *)k_gemm<EPI, GATHER, 32> : (const void *)k_gemm<EPI, GATHER, 64>;
 }
 
+// After a synchronisation: a tcgen05 kernel whose bounded wait gave up set
+// the error word; report it (and clear it for the next call).
+lbm_status tc_status(lbm_sg *s) {
+  int h = 0;
+  if (cudaMemcpy(&h, s->d_err, sizeof h, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return fail(LBM_CUDA, "surrogate error word read-back");
+  if (h != 0) {
+    cudaMemset(s->d_err, 0, sizeof(int));
+    return fail(LBM_TIMEOUT, "a bounded wait of a tcgen05 product gave up");
+  }
+  return LBM_OK;
+}
+
+// tcgen05 convolution product (lbm_tc.cuh) of one epilogue and tile width.
+template <int EPI, int BN>
+cudaError_t tc_conv_launch(lbm_sg *s, const bf16 *X, int P, int H, int W, int C, int taps,
+                           const bf16 *Bt, int N, int Kp, const float *bias, bf16 *out) {
+  using S = sgtc::TcSmem<BN>;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(sgtc::k_tc_conv<EPI, BN>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, S::ALLOC);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  dim3 grid((P + sgtc::TC_BM - 1) / sgtc::TC_BM, (N + BN - 1) / BN);
+  sgtc::k_tc_conv<EPI, BN><<<grid, sgtc::TC_THREADS, S::ALLOC, s->stream>>>(
+      X, P, H, W, C, taps, Bt, N, Kp, bias, out, s->d_err);
+  return cudaGetLastError();
+}
+
+template <int EPI>
+cudaError_t tc_conv(lbm_sg *s, const bf16 *X, int P, int H, int W, int C, int taps,
+                    const bf16 *Bt, int N, int Kp, const float *bias, bf16 *out) {
+  if (N <= 32) return tc_conv_launch<EPI, 32>(s, X, P, H, W, C, taps, Bt, N, Kp, bias, out);
+  if (N <= 64) return tc_conv_launch<EPI, 64>(s, X, P, H, W, C, taps, Bt, N, Kp, bias, out);
+  return tc_conv_launch<EPI, 128>(s, X, P, H, W, C, taps, Bt, N, Kp, bias, out);
+}
+
+// tcgen05 weight gradient (lbm_tc.cuh), pixels split so that about four
+// blocks per SM run in all, at least 256 pixels each.
+template <int BN>
+cudaError_t tc_wgrad_launch(lbm_sg *s, const bf16 *dZ, const bf16 *X, int P, int H, int W, int C,
+                            int taps, int N, float *dW, int ldw) {
+  using S = sgtc::TcSmem<BN>;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(sgtc::k_tc_wgrad<BN>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, S::ALLOC);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  const int bm = (taps * C + sgtc::TC_BM - 1) / sgtc::TC_BM, bn = (N + BN - 1) / BN;
+  const int splits = std::max(1, std::min(P / 256, (152 * 4) / (bm * bn) + 1));
+  const int pchunk = rup((P + splits - 1) / splits, sgtc::TC_BK);
+  dim3 grid(bm, bn, (P + pchunk - 1) / pchunk);
+  sgtc::k_tc_wgrad<BN><<<grid, sgtc::TC_THREADS, S::ALLOC, s->stream>>>(
+      dZ, X, P, H, W, C, taps, N, dW, ldw, pchunk, s->d_err);
+  return cudaGetLastError();
+}
+
 // C = A x Bt^T with A explicit ([M][K]) or, when X is given, the implicit
 // im2col of X ([M pixels][H][W][C], K = taps * C).
 lbm_status gemm(lbm_sg *s, int epi, const bf16 *A, const bf16 *Bt, int M, int N, int K,
@@ -688,6 +751,20 @@ lbm_status gemm(lbm_sg *s, int epi, const bf16 *A, const bf16 *Bt, int M, int N,
   g.bias = bias;
   g.out_bf16 = ob;
   g.out_f32 = of;
+  if (X && s->cfg.products == 0 && splits == 1 &&
+      (epi == EPI_BIAS_RELU_BF16 || epi == EPI_BIAS_BF16 || epi == EPI_BF16)) {
+    // the implicit-GEMM convolution on tcgen05
+    cudaError_t e;
+    if (epi == EPI_BIAS_RELU_BF16)
+      e = tc_conv<sgtc::TC_BIAS_RELU>(s, X, M, H, W, C, taps, Bt, N, K, bias, ob);
+    else if (epi == EPI_BIAS_BF16)
+      e = tc_conv<sgtc::TC_BIAS>(s, X, M, H, W, C, taps, Bt, N, K, bias, ob);
+    else
+      e = tc_conv<sgtc::TC_PLAIN>(s, X, M, H, W, C, taps, Bt, N, K, nullptr, ob);
+    if (e != cudaSuccess)
+      return fail(LBM_CUDA, std::string("surrogate tcgen05 conv: ") + cudaGetErrorString(e));
+    return LBM_OK;
+  }
   const int bn = N <= 32 ? 32 : 64;
   dim3 grid((M + GBM - 1) / GBM, (N + bn - 1) / bn, (K + g.kchunk - 1) / g.kchunk);
   void *args[] = {&g};
@@ -755,7 +832,17 @@ lbm_status conv_bwd(lbm_sg *s, int li, int xi, int yi, int B, bool need_dx) {
     k_bias_grad<<<grid_for((size_t)M), 256, 0, s->stream>>>(Y.dx, s->g + c.boff, (size_t)M, c.cout);
   }
   lbm_status st = LBM_OK;
-  if (X.c % 8 == 0 && c.cout % 8 == 0) {
+  if (X.c % 8 == 0 && c.cout % 8 == 0 && s->cfg.products == 0) {
+    cudaError_t e;
+    if (c.cout <= 32)
+      e = tc_wgrad_launch<32>(s, Y.dx, X.x, M, X.h, X.w, X.c, c.taps, c.cout, s->g + c.woff, c.Kp);
+    else if (c.cout <= 64)
+      e = tc_wgrad_launch<64>(s, Y.dx, X.x, M, X.h, X.w, X.c, c.taps, c.cout, s->g + c.woff, c.Kp);
+    else
+      e = tc_wgrad_launch<128>(s, Y.dx, X.x, M, X.h, X.w, X.c, c.taps, c.cout, s->g + c.woff, c.Kp);
+    if (e != cudaSuccess)
+      return fail(LBM_CUDA, std::string("surrogate tcgen05 wgrad: ") + cudaGetErrorString(e));
+  } else if (X.c % 8 == 0 && c.cout % 8 == 0) {
     const int bm = (c.cout + DWM - 1) / DWM, bn = (c.Kp + DWN - 1) / DWN;
     const int splits = std::max(1, std::min(M / (DWK * 8), (152 * 6) / (bm * bn) + 1));
     const int pchunk = rup((M + splits - 1) / splits, DWK);
@@ -875,6 +962,7 @@ lbm_status loss_grads(lbm_sg *s, int B, double *loss_out) {
   cudaMemcpyAsync(&h, s->loss, sizeof h, cudaMemcpyDeviceToHost, s->stream);
   if (cudaStreamSynchronize(s->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess)
     return fail(LBM_CUDA, "surrogate step failed");
+  if ((st = tc_status(s)) != LBM_OK) return st;
   if (loss_out) *loss_out = h;
   return LBM_OK;
 }
@@ -986,6 +1074,10 @@ lbm_status lbm_sg_create(const lbm_sg_config *cfg, lbm_sg **out) {
       (st = salloc(s, &s->msk, P)) || (st = salloc(s, &s->xin, P * ci)) ||
       (st = salloc(s, &s->yout, P * co)) || (st = salloc(s, &s->loss, 3)))
     return bail(st);
+  if (cfg->products != 0 && cfg->products != 1)
+    return bail(fail(LBM_INVALID, "surrogate: products must be 0 (tcgen05) or 1 (mma.sync)"));
+  if ((st = salloc(s, &s->d_err, 1)) != LBM_OK) return bail(st);
+  cudaMemset(s->d_err, 0, sizeof(int));
   if (cfg->coarse_weight > 0.f) {
     const size_t nb = (size_t)B * (H / cfg->coarse_block) * (W / cfg->coarse_block);
     if ((st = salloc(s, &s->coarse_d, nb * co)) || (st = salloc(s, &s->coarse_w, nb))) return bail(st);
@@ -1036,7 +1128,7 @@ lbm_status lbm_sg_forward(lbm_sg *s, int32_t batch, const float *x, float *y) {
   k_bf16_to_f32<<<grid_for(P * c.out_channels), 256, 0, s->stream>>>(s->act[A_OUT].x, s->yout, P * c.out_channels);
   cudaMemcpyAsync(y, s->yout, P * c.out_channels * sizeof(float), cudaMemcpyDeviceToHost, s->stream);
   if (cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(LBM_CUDA, "surrogate forward failed");
-  return LBM_OK;
+  return tc_status(s);
 }
 
 lbm_status lbm_sg_loss_grads(lbm_sg *s, int32_t batch, const float *x, const float *target,
@@ -1109,6 +1201,7 @@ lbm_status lbm_sg_train(lbm_sg *s, int32_t batch, const int32_t *order, int32_t 
     steps++;
   }
   if (cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(LBM_CUDA, "surrogate training failed");
+  if (lbm_status ts = tc_status(s)) return ts;
   if (mean_loss) *mean_loss = steps ? total / steps : 0.0;
   return LBM_OK;
 }

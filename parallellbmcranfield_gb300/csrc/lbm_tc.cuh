@@ -1,0 +1,379 @@
+// tcgen05 products of the warm-start network (5th-generation tensor cores:
+// accumulators in tensor memory, operands read from shared memory by the
+// MMA unit, one thread issuing the MMAs).
+//
+//   k_tc_conv   C[p][n] = sum_k A[p][k] Bt[n][k] with A the implicit im2col
+//               of an NHWC tensor (forward: X and W; input gradient: dZ and
+//               the flipped W).  M = 128 pixels per block, N = BN outputs.
+//   k_tc_wgrad  dW[n][k] += sum_p im2col(X)[p][k] dZ[p][n], computed as the
+//               transposed product dW^T[k][n] (M = 128 values of k = tap*C + c
+//               per block, N = BN output channels), pixels split over
+//               blockIdx.z, FP32 atomics into dW.
+//
+// Pipeline: TC_STAGES shared-memory stages of TC_BK = 64 K values; all 128
+// threads fill a stage with 16-byte cp.async copies (zero-filled where the
+// im2col or the tile runs out), fence them to the async proxy, and thread 0
+// issues four 128 x BN x 16 MMAs (kind::f16, BF16 in, FP32 accumulate) and a
+// tcgen05.commit to the stage's mbarrier; a stage is refilled only after that
+// mbarrier reports the MMAs reading it complete.  Every mbarrier wait is
+// bounded: on expiry the block sets *err, stops issuing, waits (bounded) for
+// the MMAs in flight, frees its tensor memory and returns.
+//
+// Shared-memory operand layout (no swizzle, "interleaved"): 8 x 16-byte core
+// matrices of 128 contiguous bytes.
+//   K-major (row r of M or N, column k):   (r/8)*1024 + (k/8)*128 + (r%8)*16 + (k%8)*2
+//            descriptor LBO = 128 (next 8 k), SBO = 1024 (next 8 rows)
+//   MN-major (element r of M or N, k):     (k/8)*(R*16) + (r/8)*128 + (k%8)*16 + (r%8)*2
+//            descriptor LBO = 128 (next 8 r), SBO = R*16 (next 8 k)
+// (R = rows of the tile.)  Tensor memory holds D with row i of the tile in
+// lane i and column j in column j; warp w reads lanes 32w..32w+31.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace sgtc {
+
+using bf16 = __nv_bfloat16;
+
+constexpr int TC_BM = 128;
+constexpr int TC_BK = 64;
+constexpr int TC_STAGES = 3;
+constexpr int TC_THREADS = 128;
+constexpr long long TC_POLLS = 1ll << 20;  // mbarrier polls before a wait gives up (about a second)
+
+__device__ __forceinline__ uint32_t saddr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// tcgen05 shared-memory matrix descriptor without swizzling: start address,
+// leading and stride byte offsets (16-byte units), version field 0b001 at
+// bits 46-48, base offset 0, swizzle mode 0.
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo & 0x3FFFFu) >> 4) << 16) |
+         ((uint64_t)((sbo & 0x3FFFFu) >> 4) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9, 10-12 = 1), A / B major (bit 15 / 16: 0 K-major, 1 MN-major),
+// N >> 3 (bits 17-22), M >> 4 (bits 24-28).
+__host__ __device__ constexpr uint32_t tc_idesc(int n, int a_mn, int b_mn) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)a_mn << 15) | ((uint32_t)b_mn << 16) |
+         ((uint32_t)(n >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void cp16(uint32_t dst, const void *src, bool pred) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src),
+               "r"(pred ? 16 : 0));
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+__device__ __forceinline__ void mb_init(uint64_t *b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(saddr(b)), "r"(count));
+}
+__device__ __forceinline__ bool mb_try(uint64_t *b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(saddr(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mb_wait(uint64_t *b, uint32_t parity) {
+  for (long long i = 0; i < TC_POLLS; i++)
+    if (mb_try(b, parity)) return true;
+  return false;
+}
+
+// Tensor memory (warp-wide): allocate ncols columns (a power of two >= 32),
+// the address lands in *slot.
+__device__ __forceinline__ void tm_alloc(uint32_t *slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                   saddr(slot)),
+               "r"(ncols));
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+}
+__device__ __forceinline__ void tm_free(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(ncols));
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+
+// D[tmem] (+)= A[desc] x B[desc]^T, one thread.
+__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                       uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+// The mbarrier receives one arrival when every MMA this thread issued before is done.
+__device__ __forceinline__ void tc_commit(uint64_t *b) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                   saddr(b))
+               : "memory");
+}
+// 16 consecutive FP32 columns of this thread's lane.
+__device__ __forceinline__ void tm_ld16(uint32_t taddr, float v[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+      "[%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// Dynamic shared memory of a block: the stages, then the mbarriers and the
+// tensor-memory address (1024-byte aligned base).
+template <int BN>
+struct TcSmem {
+  static constexpr int A_BYTES = TC_BM * TC_BK * 2;
+  static constexpr int B_BYTES = BN * TC_BK * 2;
+  static constexpr int STAGE = A_BYTES + B_BYTES;
+  static constexpr int BYTES = TC_STAGES * STAGE + 64;
+  static constexpr int ALLOC = BYTES + 1024;  // room to align the base
+};
+
+// The main loop shared by both kernels.  load(stage_a, stage_b, kt) issues
+// this thread's cp.async copies of K tile kt; a_k16 / b_k16 are the byte
+// advances of the A / B descriptors per MMA (16 K values).  Returns false if
+// a bounded wait gave up (the MMAs issued are complete or abandoned).
+template <int BN, class Load>
+__device__ __forceinline__ bool tc_mainloop(uint8_t *sm, uint32_t tmem, int nk, uint32_t idesc,
+                                            uint32_t a_lbo, uint32_t a_sbo, uint32_t a_k16,
+                                            uint32_t b_lbo, uint32_t b_sbo, uint32_t b_k16,
+                                            Load load, int *err) {
+  using S = TcSmem<BN>;
+  uint64_t *bars = (uint64_t *)(sm + TC_STAGES * S::STAGE);
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int s = 0; s < TC_STAGES - 1; s++) {
+    if (s < nk) load(sm + s * S::STAGE, sm + s * S::STAGE + S::A_BYTES, s);
+    cp_commit();
+  }
+  bool ok = true;
+  for (int kt = 0; kt < nk; kt++) {
+    const int s = kt % TC_STAGES;
+    cp_wait<TC_STAGES - 2>();
+    fence_async_smem();
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t a0 = saddr(sm + s * S::STAGE), b0 = a0 + S::A_BYTES;
+#pragma unroll
+      for (int kk = 0; kk < TC_BK / 16; kk++)
+        tc_mma(tmem, tc_desc(a0 + kk * a_k16, a_lbo, a_sbo), tc_desc(b0 + kk * b_k16, b_lbo, b_sbo),
+               idesc, (kt | kk) != 0);
+      tc_commit(&bars[s]);
+    }
+    const int nt = kt + TC_STAGES - 1;
+    if (nt < nk) {
+      // stage nt % S was last read by the MMAs of tile kt - 1
+      if (kt >= 1 && !mb_wait(&bars[(kt - 1) % TC_STAGES], ((kt - 1) / TC_STAGES) & 1)) ok = false;
+      if (ok) load(sm + (nt % TC_STAGES) * S::STAGE, sm + (nt % TC_STAGES) * S::STAGE + S::A_BYTES, nt);
+    }
+    cp_commit();
+  }
+  cp_wait<0>();
+  // the last commit covers every MMA issued before it
+  if (nk > 0 && !mb_wait(&bars[(nk - 1) % TC_STAGES], ((nk - 1) / TC_STAGES) & 1)) ok = false;
+  ok = __syncthreads_and(ok) != 0;
+  tc_fence_after();
+  if (!ok && tid == 0) atomicExch(err, 1);
+  return ok;
+}
+
+// Block set-up: mbarriers (thread 0) and BN columns of tensor memory (warp 0).
+template <int BN>
+__device__ __forceinline__ uint32_t tc_setup(uint8_t *sm) {
+  using S = TcSmem<BN>;
+  uint64_t *bars = (uint64_t *)(sm + TC_STAGES * S::STAGE);
+  uint32_t *slot = (uint32_t *)(bars + TC_STAGES);
+  if (threadIdx.x == 0)
+    for (int s = 0; s < TC_STAGES; s++) mb_init(&bars[s], 1);
+  if (threadIdx.x < 32) tm_alloc(slot, BN < 32 ? 32 : BN);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  return *slot;
+}
+template <int BN>
+__device__ __forceinline__ void tc_teardown(uint32_t tmem) {
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x < 32) tm_free(tmem, BN < 32 ? 32 : BN);
+}
+
+__device__ __forceinline__ uint8_t *tc_smem_base() {
+  extern __shared__ uint8_t tc_dyn[];
+  return (uint8_t *)(((uintptr_t)tc_dyn + 1023) & ~(uintptr_t)1023);
+}
+
+enum TcEpi : int { TC_BIAS_RELU = 0, TC_BIAS = 1, TC_PLAIN = 2 };
+
+// Convolution as C[p][n] = im2col(X)[p][k] Bt[n][k]: X is [P][H][W][C] BF16
+// (C a multiple of 8: a 16-byte chunk never straddles two taps), taps 9
+// (3x3, pad 1) or 1, k = tap*C + c < taps*C, Bt is [N][Kp] (rows of Kp
+// values, zero beyond taps*C).  Output [P][N] BF16 with bias and ReLU per EPI.
+template <int EPI, int BN>
+__global__ void __launch_bounds__(TC_THREADS) k_tc_conv(const bf16 *__restrict__ X, int P, int H,
+                                                        int W, int C, int taps,
+                                                        const bf16 *__restrict__ Bt, int N, int Kp,
+                                                        const float *__restrict__ bias,
+                                                        bf16 *__restrict__ out, int *err) {
+  uint8_t *sm = tc_smem_base();
+  const uint32_t tmem = tc_setup<BN>(sm);
+  const int tid = threadIdx.x;
+  const int m0 = blockIdx.x * TC_BM, n0 = blockIdx.y * BN;
+  const int KC = taps * C;
+  const int nk = (Kp + TC_BK - 1) / TC_BK;
+  // this thread's pixel (row tid of the A tile)
+  const int p = m0 + tid;
+  const bool pin = p < P;
+  const int px = pin ? p % W : 0, py = pin ? (p / W) % H : 0;
+  auto load = [&](uint8_t *sa, uint8_t *sb, int kt) {
+    const uint32_t a = saddr(sa), b = saddr(sb);
+    const int k0 = kt * TC_BK;
+#pragma unroll
+    for (int kc = 0; kc < 8; kc++) {
+      const int k = k0 + kc * 8;
+      const int r = k / C, c = k - r * C;
+      const int dy = taps == 9 ? r / 3 - 1 : 0, dx = taps == 9 ? r % 3 - 1 : 0;
+      const int yy = py + dy, xx = px + dx;
+      const bool ok = pin && k < KC && yy >= 0 && yy < H && xx >= 0 && xx < W;
+      const bf16 *src = ok ? X + ((size_t)(p + dy * W + dx) * C + c) : X;
+      cp16(a + (tid >> 3) * 1024 + kc * 128 + (tid & 7) * 16, src, ok);
+    }
+    // B tile: BN rows x 8 chunks of 8 k values
+#pragma unroll
+    for (int i = 0; i < BN / 16; i++) {
+      const int ch = tid + i * TC_THREADS;
+      const int r = ch & (BN - 1), kc = ch / BN;
+      const int k = k0 + kc * 8;
+      const bool ok = n0 + r < N && k < Kp;
+      cp16(b + (r >> 3) * 1024 + kc * 128 + (r & 7) * 16, ok ? Bt + (size_t)(n0 + r) * Kp + k : Bt,
+           ok);
+    }
+  };
+  const bool ok = tc_mainloop<BN>(sm, tmem, nk, tc_idesc(BN, 0, 0), 128, 1024, 256, 128, 1024, 256,
+                                  load, err);
+  if (ok) {
+    const int warp = tid >> 5, lane = tid & 31;
+    const int row = m0 + warp * 32 + lane;
+#pragma unroll
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+      float v[16];
+      tm_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
+      if (row < P) {
+#pragma unroll
+        for (int j = 0; j < 16; j += 2) {
+          const int n = n0 + c0 + j;
+          float v0 = v[j], v1 = v[j + 1];
+          if (EPI != TC_PLAIN) {
+            if (n < N) v0 += bias[n];
+            if (n + 1 < N) v1 += bias[n + 1];
+          }
+          if (EPI == TC_BIAS_RELU) {
+            v0 = fmaxf(v0, 0.f);
+            v1 = fmaxf(v1, 0.f);
+          }
+          if (n + 1 < N && (N & 1) == 0)
+            *(__nv_bfloat162 *)(out + (size_t)row * N + n) = __floats2bfloat162_rn(v0, v1);
+          else {
+            if (n < N) out[(size_t)row * N + n] = __float2bfloat16_rn(v0);
+            if (n + 1 < N) out[(size_t)row * N + n + 1] = __float2bfloat16_rn(v1);
+          }
+        }
+      }
+    }
+  }
+  tc_teardown<BN>(tmem);
+}
+
+// Weight gradient dW[n][k] += sum over pixels p in [pbeg, pend) of
+// im2col(X)[p][k] * dZ[p][n], as the product dW^T[k][n] with both operands
+// MN-major in shared memory (pixels are the K of the MMA).  dZ is [P][N]
+// (N a multiple of 8), dW rows are ldw long; k < taps*C and n < N are written.
+template <int BN>
+__global__ void __launch_bounds__(TC_THREADS) k_tc_wgrad(const bf16 *__restrict__ dZ,
+                                                         const bf16 *__restrict__ X, int P, int H,
+                                                         int W, int C, int taps, int N,
+                                                         float *__restrict__ dW, int ldw,
+                                                         int pchunk, int *err) {
+  uint8_t *sm = tc_smem_base();
+  const uint32_t tmem = tc_setup<BN>(sm);
+  const int tid = threadIdx.x;
+  const int m0 = blockIdx.x * TC_BM, n0 = blockIdx.y * BN;
+  const int KC = taps * C;
+  const int pbeg = blockIdx.z * pchunk, pend = min(P, pbeg + pchunk);
+  const int nk = pend > pbeg ? (pend - pbeg + TC_BK - 1) / TC_BK : 0;
+  const int pk = tid & 63, half = tid >> 6;  // pixel of the K tile, half of the chunk range
+  auto load = [&](uint8_t *sa, uint8_t *sb, int kt) {
+    const uint32_t a = saddr(sa), b = saddr(sb);
+    const int p = pbeg + kt * TC_BK + pk;
+    const bool pin = p < pend;
+    const int px = pin ? p % W : 0, py = pin ? (p / W) % H : 0;
+    const uint32_t kofs = (pk >> 3) * (TC_BM * 16) + (pk & 7) * 16;
+    // A: 16 chunks of 8 k values at this pixel, 8 per thread
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      const int kc = half * 8 + i;
+      const int k = m0 + kc * 8;
+      const int r = k / C, c = k - r * C;
+      const int dy = taps == 9 ? r / 3 - 1 : 0, dx = taps == 9 ? r % 3 - 1 : 0;
+      const int yy = py + dy, xx = px + dx;
+      const bool ok = pin && k < KC && yy >= 0 && yy < H && xx >= 0 && xx < W;
+      const bf16 *src = ok ? X + ((size_t)(p + dy * W + dx) * C + c) : X;
+      cp16(a + kofs + kc * 128, src, ok);
+    }
+    // B: BN / 8 chunks of 8 output channels at this pixel, split over the halves
+    const uint32_t bofs = (pk >> 3) * (BN * 16) + (pk & 7) * 16;
+#pragma unroll
+    for (int i = 0; i < BN / 16; i++) {
+      const int cc = half * (BN / 16) + i;
+      const int n = n0 + cc * 8;
+      const bool ok = pin && n < N;
+      cp16(b + bofs + cc * 128, ok ? dZ + (size_t)p * N + n : dZ, ok);
+    }
+  };
+  const bool ok = tc_mainloop<BN>(sm, tmem, nk, tc_idesc(BN, 1, 1), 128, TC_BM * 16, 2 * TC_BM * 16,
+                                  128, BN * 16, 2 * BN * 16, load, err);
+  if (ok && nk > 0) {
+    const int warp = tid >> 5, lane = tid & 31;
+    const int k = m0 + warp * 32 + lane;
+#pragma unroll
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+      float v[16];
+      tm_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
+      if (k < KC) {
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          const int n = n0 + c0 + j;
+          if (n < N) atomicAdd(dW + (size_t)n * ldw + k, v[j]);
+        }
+      }
+    }
+  }
+  tc_teardown<BN>(tmem);
+}
+
+}  // namespace sgtc

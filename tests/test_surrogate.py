@@ -92,17 +92,21 @@ def test_bf16_rounding_helper():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("products", ["tcgen05", "mma"])
 @pytest.mark.parametrize("cin,base,h,coarse", [(CIN, BASE, H, 0.0), (7, 32, 32, 0.0),
-                                               (8, 32, 32, 0.0), (CIN, BASE, H, 2.0)])
-def test_gpu_gradients_match_oracle(cin, base, h, coarse):
+                                               (8, 32, 32, 0.0), (CIN, BASE, H, 2.0),
+                                               (8, 32, 64, 0.0)])
+def test_gpu_gradients_match_oracle(cin, base, h, coarse, products):
     """4 or 7 input channels: the first layer's products use an explicit im2col
     in memory; every layer with a multiple of 8 channels (all of them at 8
     inputs) uses the implicit-im2col forward/input-gradient products and the
-    pixel-split weight-gradient kernel, including K padded beyond taps*C."""
+    pixel-split weight-gradient kernel, including K padded beyond taps*C.
+    products="tcgen05" runs those on the 5th-generation tensor cores (tensor
+    memory accumulators, 128 x N x 16 MMAs), "mma" on mma.sync."""
     import parallellbmcranfield_gb300 as G
 
     s = G.Surrogate(height=h, width=h, in_channels=cin, out_channels=COUT, base=base, max_batch=2,
-                    seed=5, coarse_weight=coarse, coarse_block=4)
+                    seed=5, coarse_weight=coarse, coarse_block=4, products=products)
     params = s.params().astype(np.float64)
     x, t, m = sample(seed=2, h=h, cin=cin)
     loss, g = s.loss_grads(x, t, m)
@@ -272,3 +276,24 @@ def test_gap_flow_of_an_empty_channel_is_the_inlet_parabola():
     assert np.allclose(g[1:-1, 128], want, rtol=1e-6)
     assert abs(g[1:-1, 128].max() - 1.0) < 1e-3  # peak = umax
     assert (g[0] == 0).all() and (g[:, 0] == 0).all()
+
+
+@pytest.mark.gpu
+def test_tcgen05_and_mma_products_agree():
+    """Both product paths on a 64 x 64 batch at base width 32 (every tile width
+    32, 64, 128 and several K tiles): forward outputs and gradients agree to
+    the BF16 rounding of the activations."""
+    import parallellbmcranfield_gb300 as G
+
+    x, t, m = sample(seed=9, B=2, h=64, cin=8)
+    out = {}
+    for products in ("tcgen05", "mma"):
+        s = G.Surrogate(height=64, width=64, in_channels=8, out_channels=COUT, base=32,
+                        max_batch=2, seed=11, products=products)
+        loss, g = s.loss_grads(x, t, m)
+        out[products] = (s.forward(x), loss, g)
+        s.close()
+    (ya, la, ga), (yb, lb, gb) = out["tcgen05"], out["mma"]
+    assert np.abs(ya - yb).max() <= 1e-2 * np.abs(yb).max()
+    assert abs(la - lb) <= 1e-2 * lb
+    assert np.linalg.norm(ga - gb) <= 3e-2 * np.linalg.norm(gb)

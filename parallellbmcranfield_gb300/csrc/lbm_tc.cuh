@@ -24,7 +24,9 @@
 //   K-major (row r of M or N, column k):   (r/8)*1024 + (k/8)*128 + (r%8)*16 + (k%8)*2
 //            descriptor LBO = 128 (next 8 k), SBO = 1024 (next 8 rows)
 //   MN-major (element r of M or N, k):     (k/8)*(R*16) + (r/8)*128 + (k%8)*16 + (r%8)*2
-//            descriptor LBO = 128 (next 8 r), SBO = R*16 (next 8 k)
+//            descriptor LBO = R*16 (next 8 k), SBO = 128 (next 8 r): in the
+//            no-swizzle MN-major form the two offsets swap roles against the
+//            swizzled MN-major forms
 // (R = rows of the tile.)  Tensor memory holds D with row i of the tile in
 // lane i and column j in column j; warp w reads lanes 32w..32w+31.
 #pragma once
@@ -197,6 +199,7 @@ __device__ __forceinline__ bool tc_mainloop(uint8_t *sm, uint32_t tmem, int nk, 
   // the last commit covers every MMA issued before it
   if (nk > 0 && !mb_wait(&bars[(nk - 1) % TC_STAGES], ((nk - 1) / TC_STAGES) & 1)) ok = false;
   ok = __syncthreads_and(ok) != 0;
+  __syncwarp();  // thread 0 issued the MMAs alone; the epilogue's tcgen05.ld needs the whole warp
   tc_fence_after();
   if (!ok && tid == 0) atomicExch(err, 1);
   return ok;
@@ -210,6 +213,9 @@ __device__ __forceinline__ uint32_t tc_setup(uint8_t *sm) {
   uint32_t *slot = (uint32_t *)(bars + TC_STAGES);
   if (threadIdx.x == 0)
     for (int s = 0; s < TC_STAGES; s++) mb_init(&bars[s], 1);
+  // tcgen05.alloc / ld / dealloc are .sync.aligned: the warp must arrive
+  // converged, also after code that only one of its threads ran
+  __syncwarp();
   if (threadIdx.x < 32) tm_alloc(slot, BN < 32 ? 32 : BN);
   tc_fence_before();
   __syncthreads();
@@ -220,6 +226,7 @@ template <int BN>
 __device__ __forceinline__ void tc_teardown(uint32_t tmem) {
   tc_fence_before();
   __syncthreads();
+  __syncwarp();
   if (threadIdx.x < 32) tm_free(tmem, BN < 32 ? 32 : BN);
 }
 
@@ -355,8 +362,10 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_wgrad(const bf16 *__restrict_
       cp16(b + bofs + cc * 128, ok ? dZ + (size_t)p * N + n : dZ, ok);
     }
   };
-  const bool ok = tc_mainloop<BN>(sm, tmem, nk, tc_idesc(BN, 1, 1), 128, TC_BM * 16, 2 * TC_BM * 16,
-                                  128, BN * 16, 2 * BN * 16, load, err);
+  // MN-major without swizzle: LBO is the K-direction stride of 8-row groups,
+  // SBO the MN-direction stride of core matrices
+  const bool ok = tc_mainloop<BN>(sm, tmem, nk, tc_idesc(BN, 1, 1), TC_BM * 16, 128, 2 * TC_BM * 16,
+                                  BN * 16, 128, 2 * BN * 16, load, err);
   if (ok && nk > 0) {
     const int warp = tid >> 5, lane = tid & 31;
     const int k = m0 + warp * 32 + lane;

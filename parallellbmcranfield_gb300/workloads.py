@@ -11,8 +11,9 @@ cylinder: channel of 2048 x 512 nodes, MRT, parabolic inlet (u_max 0.04),
   FP32 and FP16-deviation storage.  The wake sheds vortices, so the comparison
   is on the statistics of the last 100k steps: mean drag coefficient,
   drag and lift amplitudes, Strouhal number (lift spectrum peak).
-steady: steady flows run to du_rel <= 1e-10 (or a step cap) in every precision;
-  velocity and density errors of each reduced precision against FP64.
+steady: steady flows: FP64 runs to du_rel <= 1e-10 (or a step cap), every other
+  precision the same number of steps; velocity and de-meaned density errors
+  against FP64.
 cavities: 256 lid-driven cavities in one batch, sides log-uniform in
   [64, 1024], Re uniform in [100, 3200], lid 0.05, TRT (magic parameter 3/16),
   FP32, autotuned tile, run until every case reaches du_rel <= 1e-6 or stops
@@ -79,7 +80,8 @@ def cylinder(precisions=("fp64", "fp32", "fp16dev"), steps=200000, sample_from=1
     return out
 
 
-def run_steady(mesh, kw, prec, max_steps, tol=1e-10, chunk=1000):
+def run_steady(mesh, kw, prec, max_steps, tol=1e-10, chunk=1000, fixed=False):
+    """Steps in chunks until du_rel <= tol or max_steps (fixed: exactly max_steps)."""
     s = G.Solver(mesh, precision=prec, **kw)
     s.set_state(None, np.ones(s.N), np.zeros(s.N), np.zeros(s.N))
     s.step(chunk)
@@ -89,7 +91,7 @@ def run_steady(mesh, kw, prec, max_steps, tol=1e-10, chunk=1000):
         s.step(chunk)
         it += chunk
         d = s.check()
-        if d["du_rel"] <= tol:
+        if not fixed and d["du_rel"] <= tol:
             break
     f = s.fields()
     s.close()
@@ -107,19 +109,25 @@ STEADY_CASES = {
 }
 
 
-def steady(precisions=("fp32", "fp16dev", "bf16dev")):
+def steady(precisions=("fp32", "fp16neq", "fp16dev", "bf16dev")):
+    """Every precision runs exactly as many steps as FP64 needed to reach
+    du_rel <= 1e-10, so the comparison is at the same iteration (the cavity's
+    lid treatment adds mass every step, so its mean density keeps rising)."""
     out = {}
     for name, (mk, kw, mx) in STEADY_CASES.items():
         mesh = mk()
+        fluid = G.inspect_mesh(mesh, **{k: v for k, v in kw.items() if k != "rho_out"})["cls"] > 0
         ref, it, du = run_steady(mesh, kw, "fp64", mx)
         r = {"fp64": dict(steps=it, du_rel=du)}
-        sp = np.sqrt(ref["u"] ** 2 + ref["v"] ** 2)
+        sp = np.sqrt(ref["u"] ** 2 + ref["v"] ** 2)[fluid]
         for prec in precisions:
-            f, it, du = run_steady(mesh, kw, prec, mx)
-            e = np.sqrt((f["u"] - ref["u"]) ** 2 + (f["v"] - ref["v"]) ** 2)
-            r[prec] = dict(steps=it, du_rel=du, vel_err_max_rel=float(e.max() / sp.max()),
+            f, _, dup = run_steady(mesh, kw, prec, it, fixed=True)
+            e = np.sqrt((f["u"] - ref["u"]) ** 2 + (f["v"] - ref["v"]) ** 2)[fluid]
+            dr = (f["rho"] - ref["rho"])[fluid]
+            r[prec] = dict(steps=it, du_rel=dup, vel_err_max_rel=float(e.max() / sp.max()),
                            vel_err_l2_rel=float(np.sqrt((e ** 2).sum() / (sp ** 2).sum())),
-                           rho_err_max=float(np.abs(f["rho"] - ref["rho"]).max()))
+                           rho_err_demeaned_max=float(np.abs(dr - dr.mean()).max()),
+                           rho_mean_offset=float(dr.mean()))
         out[name] = r
     return out
 

@@ -191,14 +191,14 @@ bool step_config(lbm_ctx *c, int var, dim3 *grid, dim3 *block, size_t *smem) {
   return true;
 }
 
-// Moment storage: the bulk kernel over pairs of nodes (NPT rows per thread)
-// and the special-node kernel over the compact list, both reading the same
-// generation (they write disjoint nodes).
+// Moment storage: the bulk kernel (blocks of 4 warps x 60 columns, NPT rows
+// per thread) and the special-node kernel over the compact list, both
+// reading the same generation (they write disjoint nodes).
 lbm_status launch_step_mom(lbm_ctx *c) {
   const int npt = lbm::MOM_NPT[c->variant];
   lbm::StepArgs a = args_now(c);
   void *args[] = {&a};
-  const dim3 grid((unsigned)((c->P.pitch + 255) / 256), (unsigned)((c->P.m + npt - 1) / npt));
+  const dim3 grid((unsigned)((c->P.n + 239) / 240), (unsigned)((c->P.m + npt - 1) / npt));
   cudaError_t e = cudaLaunchKernel(c->mk->step[c->p.collision_model][c->variant], grid, dim3(128),
                                    args, 0, c->stream);
   if (e == cudaSuccess && c->mlist_n > 0)

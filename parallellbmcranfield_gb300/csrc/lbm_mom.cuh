@@ -267,125 +267,273 @@ struct AccMom {
 };
 
 // ------------------------------------------------------------------ bulk step
+//
+// The two nodes of a pair (x0, x0+1) travel together: their 32-bit words of
+// the 16-bit planes, the 16-bit word of each byte plane, and packed FP32x2
+// arithmetic (one FFMA2 / FADD2 / FMUL2 for both nodes).
 
-// Decoded post-collision deviations of the two nodes (x0, x0+1) of row r.
-__device__ __forceinline__ void mom_pair(const StepArgs &a, const void *b, int r, int x0,
-                                         float2 d[9]) {
-  const long long z = (long long)r * a.pitch + x0;
-  MomSet s0, s1;
-  float q0[3], q1[3];
+// Raw stored words of one pair of one row.
+struct MomRaw {
+  uint32_t h[3];  // two int16 high parts
+  uint32_t l[3];  // two low bytes (in the low 16 bits)
+  uint32_t n[6];  // two FP16 non-equilibrium moments
+};
+
+__device__ __forceinline__ void mom_raw_load(const StepArgs &a, const void *b, long long z,
+                                             bool in, MomRaw &w) {
 #pragma unroll
   for (int p = 0; p < 3; p++) {
-    const uint32_t hw = __ldg((const unsigned *)(mom_hi(b, a, p) + z));
-    const uint32_t lw = __ldg((const unsigned short *)(mom_lo(b, a, p) + z));
-    const int h0 = (int)(int16_t)(hw & 0xffffu), h1 = (int)(int16_t)(hw >> 16);
-    q0[p] = (float)(h0 * 256 + (int)(lw & 0xffu)) * fx_step(a, p);
-    q1[p] = (float)(h1 * 256 + (int)(lw >> 8)) * fx_step(a, p);
+    w.h[p] = in ? __ldg((const unsigned *)(mom_hi(b, a, p) + z)) : 0u;
+    w.l[p] = in ? (uint32_t)__ldg((const unsigned short *)(mom_lo(b, a, p) + z)) : 0u;
   }
-  s0.r = q0[0]; s0.x = q0[1]; s0.y = q0[2];
-  s1.r = q1[0]; s1.x = q1[1]; s1.y = q1[2];
 #pragma unroll
-  for (int i = 0; i < 6; i++) {
-    const uint32_t w = __ldg((const unsigned *)(mom_n(b, a, i) + z));
-    __half2 h;
-    memcpy(&h, &w, 4);
-    const float2 f = __half22float2(h);
-    s0.n[i] = f.x * a.neq_is;
-    s1.n[i] = f.y * a.neq_is;
-  }
-  float p0[9], p1[9];
-  mom_to_pops(s0, a, p0);
-  mom_to_pops(s1, a, p1);
-#pragma unroll
-  for (int k = 0; k < 9; k++) d[k] = make_float2(p0[k], p1[k]);
+  for (int i = 0; i < 6; i++) w.n[i] = in ? __ldg((const unsigned *)(mom_n(b, a, i) + z)) : 0u;
 }
 
-// Bulk step of the moment storage (A-B): each thread owns the node pair
-// (x0, x0+1) of NPT consecutive rows.  It decodes the source rows y0-1 ..
-// y0+NPT in order; a decoded row r hands its populations with c_y = +1 to
-// destination row r+1, c_y = 0 to row r and c_y = -1 to row r-1, and the
-// +-1 x-shift comes from the neighbouring lane (warp shuffle; lanes 0 and 31
-// decode the node beyond the warp themselves).  When row r is decoded, row
-// r-1 has all nine pulled populations: it collides and stores.  Every lane
-// runs the same instructions; only class-1 nodes are stored (class 2/3 nodes
-// are k_special_mom's, solid nodes are never written).
+// Post-collision deviations of both nodes of a pair (the arithmetic of
+// mom_to_pops on FP32 pairs): the 24-bit codes are assembled by byte
+// permutes, [low byte, high int16, sign of the high int16].
+__device__ __forceinline__ void mom_decode2(const StepArgs &a, const MomRaw &w, float2 d[9]) {
+  float2 q[3];
+#pragma unroll
+  for (int p = 0; p < 3; p++) {
+    const int q0 = (int)__byte_perm(w.l[p], w.h[p], 0xD540);
+    const int q1 = (int)__byte_perm(w.l[p], w.h[p], 0xF761);
+    q[p] = mul2(make_float2((float)q0, (float)q1), bc2(fx_step(a, p)));
+  }
+  float2 n[6];
+#pragma unroll
+  for (int i = 0; i < 6; i++) {
+    __half2 h;
+    memcpy(&h, &w.n[i], 4);
+    n[i] = mul2(__half22float2(h), bc2(a.neq_is));
+  }
+  const float2 r = q[0], x = q[1], y = q[2];
+  const float2 i0 = bc2(a.fx_irho0);
+  const float2 jj = fma2(x, x, mul2(y, y));
+  const float2 m1 = add2(fma2(bc2(3.f), jj, mul2(bc2(-2.f), r)), n[0]);
+  const float2 m2 = add2(fma2(bc2(-3.f), jj, r), n[1]);
+  const float2 m4 = sub2(n[2], x), m6 = sub2(n[3], y);
+  const float2 m7 = fma2(mul2(sub2(x, y), add2(x, y)), i0, n[4]);
+  const float2 m8 = fma2(mul2(x, y), i0, n[5]);
+  const float2 ax = sub2(fma2(bc2(4.f), r, mul2(bc2(-2.f), m2)), m1);
+  const float2 dg = fma2(bc2(2.f), m1, fma2(bc2(4.f), r, m2));
+  const float2 P = mul2(bc2(9.f), m7), Q = mul2(bc2(9.f), m8);
+  const float2 Xd = fma2(bc2(3.f), m4, mul2(bc2(6.f), x));
+  const float2 Yd = fma2(bc2(3.f), m6, mul2(bc2(6.f), y));
+  const float2 c = bc2(1.f / 36.f);
+  const float2 gp = add2(dg, Q), gm = sub2(dg, Q), sp = add2(Xd, Yd), sm = sub2(Xd, Yd);
+  d[5] = mul2(c, add2(gp, sp));
+  d[6] = mul2(c, sub2(gm, sm));
+  d[7] = mul2(c, sub2(gp, sp));
+  d[8] = mul2(c, add2(gm, sm));
+  // conserved moments exact by construction (see mom_to_pops)
+  const float2 s13 = mul2(bc2(2.f / 36.f), add2(ax, P)), s24 = mul2(bc2(2.f / 36.f), sub2(ax, P));
+  const float2 e57 = sub2(d[5], d[7]);
+  const float2 dx = sub2(x, add2(e57, sub2(d[8], d[6])));
+  const float2 dy = sub2(y, add2(e57, sub2(d[6], d[8])));
+  const float2 h = bc2(0.5f);
+  d[1] = mul2(h, add2(s13, dx));
+  d[3] = mul2(h, sub2(s13, dx));
+  d[2] = mul2(h, add2(s24, dy));
+  d[4] = mul2(h, sub2(s24, dy));
+  d[0] = sub2(r, add2(add2(add2(d[1], d[3]), add2(d[2], d[4])),
+                      add2(add2(d[5], d[7]), add2(d[6], d[8]))));
+}
+
+// Moments of pulled deviations (pops_to_mom on pairs).
+__device__ __forceinline__ void pops_to_mom2(const float2 d[9], float2 &r, float2 &jx, float2 &jy,
+                                             float2 m[6]) {
+  const float2 a13 = add2(d[1], d[3]), a24 = add2(d[2], d[4]), a14 = add2(a13, a24);
+  const float2 p57 = add2(d[5], d[7]), p68 = add2(d[6], d[8]), a58 = add2(p57, p68);
+  r = add2(add2(d[0], a14), a58);
+  const float2 d13 = sub2(d[1], d[3]), d24 = sub2(d[2], d[4]);
+  const float2 e57 = sub2(d[5], d[7]), e86 = sub2(d[8], d[6]);
+  const float2 x58 = add2(e57, e86), y58 = sub2(e57, e86);
+  jx = add2(d13, x58);
+  jy = add2(d24, y58);
+  m[0] = sub2(fma2(bc2(2.f), a58, mul2(bc2(-4.f), d[0])), a14);
+  m[1] = fma2(bc2(-2.f), a14, fma2(bc2(4.f), d[0], a58));
+  m[2] = fma2(bc2(-2.f), d13, x58);
+  m[3] = fma2(bc2(-2.f), d24, y58);
+  m[4] = sub2(a13, a24);
+  m[5] = sub2(p57, p68);
+}
+
+// collide_mom on pairs.
+template <int MODEL>
+__device__ __forceinline__ void collide_mom2(float2 r, float2 jx, float2 jy, float2 m[6],
+                                            const StepArgs &a) {
+  const float2 rho = add2(bc2((float)a.rho0), r);
+  const float2 inv = make_float2(__frcp_rn(rho.x), __frcp_rn(rho.y));
+  const float2 jj = fma2(jx, jx, mul2(jy, jy));
+  const float2 q = MODEL == 3 ? jj : mul2(jj, inv);
+  const float2 e1 = fma2(bc2(3.f), q, mul2(bc2(-2.f), r)), e2 = fma2(bc2(-3.f), q, r);
+  const float2 e7 = mul2(mul2(sub2(jx, jy), add2(jx, jy)), inv), e8 = mul2(mul2(jx, jy), inv);
+  const float om = (float)a.omega;
+  const float s12 = MODEL == 3 ? 1.4f : om;
+  const float s46 = MODEL == 3 ? 1.2f : (MODEL == 2 ? (float)a.omegaA : om);
+  m[0] = fma2(bc2(-s12), sub2(m[0], e1), m[0]);
+  m[1] = fma2(bc2(-s12), sub2(m[1], e2), m[1]);
+  m[2] = fma2(bc2(-s46), add2(m[2], jx), m[2]);
+  m[3] = fma2(bc2(-s46), add2(m[3], jy), m[3]);
+  m[4] = fma2(bc2(-om), sub2(m[4], e7), m[4]);
+  m[5] = fma2(bc2(-om), sub2(m[5], e8), m[5]);
+}
+
+// Encodes the post-collision moments of a pair and stores the nodes whose
+// `own` flag is set (both: full words; one: its own elements).
+__device__ __forceinline__ void mom_encode_store2(const StepArgs &a, void *b, long long z,
+                                                  uint32_t hseed, float2 r, float2 jx, float2 jy,
+                                                  const float2 m[6], bool own0, bool own1,
+                                                  bool &ok) {
+  float u0[3], u1[3];
+  {
+    const uint32_t h0 = mix32((uint32_t)z ^ hseed), h1 = mix32((uint32_t)(z + 1) ^ hseed);
+#pragma unroll
+    for (int p = 0; p < 3; p++) {
+      u0[p] = (float)((h0 >> (10 * p)) & 1023u) * (1.f / 1024.f) + (1.f / 2048.f);
+      u1[p] = (float)((h1 >> (10 * p)) & 1023u) * (1.f / 1024.f) + (1.f / 2048.f);
+    }
+  }
+  const float2 v[3] = {r, jx, jy};
+  int q0[3], q1[3];
+  bool ok0 = true, ok1 = true;
+#pragma unroll
+  for (int p = 0; p < 3; p++) {
+    q0[p] = fx_code(v[p].x, fx_istep(a, p), u0[p], ok0);
+    q1[p] = fx_code(v[p].y, fx_istep(a, p), u1[p], ok1);
+  }
+  if (own0) ok = ok && ok0;
+  if (own1) ok = ok && ok1;
+  float2 s[3];
+#pragma unroll
+  for (int p = 0; p < 3; p++) s[p] = mul2(make_float2((float)q0[p], (float)q1[p]), bc2(fx_step(a, p)));
+  const float2 i0 = bc2(a.fx_irho0);
+  const float2 jj = fma2(s[1], s[1], mul2(s[2], s[2]));
+  const float2 bb[6] = {fma2(bc2(3.f), jj, mul2(bc2(-2.f), s[0])), fma2(bc2(-3.f), jj, s[0]),
+                        mul2(bc2(-1.f), s[1]), mul2(bc2(-1.f), s[2]),
+                        mul2(mul2(sub2(s[1], s[2]), add2(s[1], s[2])), i0), mul2(mul2(s[1], s[2]), i0)};
+  uint32_t nw[6];
+#pragma unroll
+  for (int i = 0; i < 6; i++) {
+    const __half2 h = __float22half2_rn(mul2(sub2(m[i], bb[i]), bc2(a.neq_s)));
+    memcpy(&nw[i], &h, 4);
+  }
+  if (own0 && own1) {
+#pragma unroll
+    for (int p = 0; p < 3; p++) {
+      *(uint32_t *)(mom_hi(b, a, p) + z) = __byte_perm((uint32_t)q0[p], (uint32_t)q1[p], 0x6521);
+      *(unsigned short *)(mom_lo(b, a, p) + z) =
+          (unsigned short)__byte_perm((uint32_t)q0[p], (uint32_t)q1[p], 0x0040);
+    }
+#pragma unroll
+    for (int i = 0; i < 6; i++) *(uint32_t *)(mom_n(b, a, i) + z) = nw[i];
+  } else if (own0 || own1) {
+    const int e = own0 ? 0 : 1;
+#pragma unroll
+    for (int p = 0; p < 3; p++) {
+      const int q = e ? q1[p] : q0[p];
+      *(int16_t *)(mom_hi(b, a, p) + z + e) = (int16_t)(q >> 8);
+      *(uint8_t *)(mom_lo(b, a, p) + z + e) = (uint8_t)(q & 0xff);
+    }
+#pragma unroll
+    for (int i = 0; i < 6; i++)
+      *(unsigned short *)(mom_n(b, a, i) + z + e) = (unsigned short)(e ? nw[i] >> 16 : nw[i] & 0xffffu);
+  }
+}
+
+// Bulk step of the moment storage (A-B).  A warp covers 60 columns: lane l
+// holds the pair (x0, x0+1), x0 = 60 w - 2 + 2 l; lanes 1..30 own their
+// destination nodes and lanes 0 and 31 decode the pairs just outside, so
+// that every +-1 x-shift is a warp shuffle and all lanes run the same
+// instructions (no divergent halo path).  Each thread walks NPT destination
+// rows: source row r, decoded once, hands its populations with c_y = +1 to
+// destination row r+1, c_y = 0 to row r and c_y = -1 to row r-1, which is
+// then complete: it collides and stores (class-1 nodes only; class 2 and 3
+// belong to k_special_mom, solid nodes are never written).  The raw words of
+// source rows are loaded two rows ahead, and lanes 0..11 prefetch the warp's
+// span of row r + MOM_PF into L2 (a hint: nothing waits for it, every
+// prefetched byte lies inside the buffer and its guard bytes).
+constexpr int MOM_PF = 6;
 template <int MODEL, int NPT>
 __global__ void __launch_bounds__(128) k_step_mom(const __grid_constant__ StepArgs a) {
   const unsigned FULL = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
-  const int x0 = (blockIdx.x * 128 + threadIdx.x) * 2;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wx = (blockIdx.x * 4 + warp) * 60;
+  if (wx >= a.n) return;  // the whole warp lies past the row
+  const int x0 = wx - 2 + 2 * lane;
+  const bool inx = x0 >= 0 && x0 < a.pitch;  // the pitch is even, so x0 + 1 < pitch too
+  const bool owner = lane >= 1 && lane <= 30 && x0 < a.n;
   const int y0 = blockIdx.y * NPT;
-  if (x0 - lane * 2 >= a.pitch) return;  // the whole warp lies past the row
-  bool any = false;
-  uint8_t cl[NPT][2];
+  const uint32_t hseed = mix32(a.gen * 0x9e3779b9u + 0x632be5abu);
+  MomRaw raw[3];
+  mom_raw_load(a, a.src, (long long)(y0 - 1) * a.pitch + x0, inx && y0 >= 1 && y0 - 1 < a.m, raw[0]);
+  mom_raw_load(a, a.src, (long long)y0 * a.pitch + x0, inx && y0 < a.m, raw[1]);
+  float2 Fa[9], Fb[9], Fc[9];
 #pragma unroll
-  for (int j = 0; j < NPT; j++) {
-    const int y = y0 + j;
-#pragma unroll
-    for (int i = 0; i < 2; i++) {
-      cl[j][i] = (y < a.m && x0 + i < a.n) ? a.cls[(long long)y * a.pitch + x0 + i] : (uint8_t)0;
-      any = any || cl[j][i] == CLS_BULK;
-    }
-  }
-  if (!__any_sync(FULL, any)) return;
-  float2 F[NPT][9];
+  for (int k = 0; k < 9; k++) Fa[k] = Fb[k] = Fc[k] = make_float2(0.f, 0.f);
   bool ok = true;
+  float probe = 0.f;
 #pragma unroll
   for (int j = -1; j <= NPT; j++) {
     const int r = y0 + j;
+    if (j + 2 <= NPT) {
+      const int r2 = r + 2;
+      mom_raw_load(a, a.src, (long long)r2 * a.pitch + x0, inx && r2 < a.m, raw[(j + 3) % 3]);
+    }
+    if (lane < 12) {
+      const int rp = r + MOM_PF;
+      if (rp >= 0 && rp < a.m && j + MOM_PF <= NPT) {
+        const long long e = (long long)rp * a.pitch + wx - 2;
+        const char *base = (const char *)a.src;
+        const char *p = lane < 9 ? base + (long long)lane * 2 * a.plane + 2 * e
+                                 : base + 18 * a.plane + (long long)(lane - 9) * a.plane + e;
+        const char *al = (const char *)((uintptr_t)p & ~(uintptr_t)15);
+        if (lane < 9)
+          asm volatile("cp.async.bulk.prefetch.L2.global [%0], 144;" ::"l"(al) : "memory");
+        else
+          asm volatile("cp.async.bulk.prefetch.L2.global [%0], 80;" ::"l"(al) : "memory");
+      }
+    }
     float2 d[9];
-    const bool in = r >= 0 && r < a.m;  // warp-uniform
-    if (in) {
-      mom_pair(a, a.src, r, x0, d);
-    } else {
-#pragma unroll
-      for (int k = 0; k < 9; k++) d[k] = make_float2(0.f, 0.f);
-    }
-    // the node beyond the warp's edge: x0-1 for lane 0, x0+2 for lane 31
-    float h[9];
-#pragma unroll
-    for (int k = 0; k < 9; k++) h[k] = 0.f;
-    if (in && (lane == 0 || lane == 31)) {
-      const int hx = lane == 0 ? x0 - 1 : x0 + 2;
-      if (hx >= 0 && hx < a.n) mom_to_pops(mom_load(a, a.src, (long long)r * a.pitch + hx), a, h);
-    }
-    // shifted pairs for the destinations of this source row
+    mom_decode2(a, raw[(j + 1) % 3], d);
 #pragma unroll
     for (int k = 0; k < 9; k++) {
-      const int dj = j + CY[k];  // destination row index (y + c_y)
-      if (dj < 0 || dj >= NPT) continue;
       float2 v = d[k];
       if (CX[k] == 1) {
-        float left = __shfl_up_sync(FULL, d[k].y, 1);
-        if (lane == 0) left = h[k];
+        const float left = __shfl_up_sync(FULL, d[k].y, 1);
         v = make_float2(left, d[k].x);
       } else if (CX[k] == -1) {
-        float right = __shfl_down_sync(FULL, d[k].x, 1);
-        if (lane == 31) right = h[k];
+        const float right = __shfl_down_sync(FULL, d[k].x, 1);
         v = make_float2(d[k].y, right);
       }
-      F[dj][k] = v;
+      if (CY[k] == 1) Fc[k] = v;
+      else if (CY[k] == 0) Fb[k] = v;
+      else Fa[k] = v;
     }
-    // destination row j-1 is complete
-    const int jd = j - 1;
-    if (jd >= 0 && jd < NPT) {
-      const int y = y0 + jd;
-#pragma unroll
-      for (int i = 0; i < 2; i++) {
-        if (cl[jd][i] != CLS_BULK) continue;
-        float f[9];
-#pragma unroll
-        for (int k = 0; k < 9; k++) f[k] = i ? F[jd][k].y : F[jd][k].x;
-        float rr, jx, jy, m[6];
-        pops_to_mom(f, rr, jx, jy, m);
-        collide_mom<MODEL>(rr, jx, jy, m, a);
-        const long long z = (long long)y * a.pitch + x0 + i;
-        const MomCode c = mom_encode(rr, jx, jy, m, a, z, ok);
-        mom_flag(a, ok, rr + m[4]);
-        mom_store(a, a.dst, z, c);
+    if (j >= 1) {  // destination row r - 1 is complete
+      const int y = r - 1;
+      bool own0 = false, own1 = false;
+      if (owner && y < a.m) {
+        const uint32_t cw = __ldg((const unsigned short *)(a.cls + (long long)y * a.pitch + x0));
+        own0 = (cw & 0xffu) == CLS_BULK;
+        own1 = (cw >> 8) == CLS_BULK && x0 + 1 < a.n;
       }
+      float2 rr, jx, jy, m[6];
+      pops_to_mom2(Fa, rr, jx, jy, m);
+      collide_mom2<MODEL>(rr, jx, jy, m, a);
+      if (own0) probe += rr.x + m[4].x;
+      if (own1) probe += rr.y + m[4].y;
+      mom_encode_store2(a, a.dst, (long long)y * a.pitch + x0, hseed, rr, jx, jy, m, own0, own1, ok);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      Fa[k] = Fb[k];
+      Fb[k] = Fc[k];
     }
   }
+  mom_flag(a, ok, probe);
 }
 
 // Nodes with boundary work (class 3) and their fluid neighbours (class 2),

@@ -57,9 +57,10 @@ constexpr int NVAR = 6;
 constexpr TileVariant VARS[NVAR] = {
     {0, 128, 1, 1, 0, 0, 0},   {0, 64, 1, 4, 0, 0, 0},   {1, 128, 4, 1, 0, 0, 0},
     {2, 0, 0, 0, 128, 4, 2},   {3, 128, 2, 2, 0, 0, 0},  {3, 128, 2, 4, 0, 0, 0}};
-// Bulk-step tiles of the moment storage: 128 threads x 2 nodes, these rows per thread.
+// Bulk-step tiles of the moment storage: blocks of 4 warps x 60 columns, these
+// rows per thread.
 constexpr int MOM_NVAR = 3;
-constexpr int MOM_NPT[MOM_NVAR] = {2, 4, 8};
+constexpr int MOM_NPT[MOM_NVAR] = {8, 16, 32};
 constexpr int TMA_MAX_SMEM = 200 * 1024;  // dynamic shared memory budget of one TMA block
 constexpr int TMA_MAX_STAGES = 4;
 

@@ -212,14 +212,14 @@ def cosine_lr(lr, lr_min, epoch, epochs):
 
 
 def train(X, Y, M, train_idx, epochs, batch, lr, seed, lr_min=None, weight_decay=0.0,
-          coarse_weight=0.0, coarse_block=32):
+          coarse_weight=0.0, coarse_block=32, base=32, products="tcgen05"):
     """Adam with a cosine learning-rate schedule over the samples train_idx of
     (X, Y, M); returns the network, the mean loss of every epoch and the time."""
     if len(train_idx) == 0:
         raise ValueError("no training samples (no case reached the generation tolerance)")
-    net = G.Surrogate(height=GRID, width=GRID, in_channels=X.shape[-1], out_channels=3, base=32,
+    net = G.Surrogate(height=GRID, width=GRID, in_channels=X.shape[-1], out_channels=3, base=base,
                       max_batch=batch, lr=lr, seed=seed, weight_decay=weight_decay,
-                      coarse_weight=coarse_weight, coarse_block=coarse_block)
+                      coarse_weight=coarse_weight, coarse_block=coarse_block, products=products)
     net.set_dataset(X, Y, M)
     rng = np.random.default_rng(seed)
     lr_min = lr * 0.02 if lr_min is None else lr_min
@@ -300,15 +300,15 @@ def evaluate(net, cases, meshes, X, Y, M, idx, max_steps, check_every, tol):
         wall_speedup=cold_s / (warm_s + infer_s), per_case=per_case)
 
 
-def train_throughput(batch=8, samples=16, epochs=3, seed=1):
+def train_throughput(batch=8, samples=16, epochs=3, seed=1, products="tcgen05", base=32):
     """Training samples per second of the warm-start network on random
     256 x 256 inputs (the cost does not depend on the values)."""
     rng = np.random.default_rng(seed)
     x = rng.normal(size=(samples, GRID, GRID, IN_CH)).astype(np.float32)
     t = rng.normal(size=(samples, GRID, GRID, 3)).astype(np.float32)
     m = np.ones((samples, GRID, GRID), np.float32)
-    net = G.Surrogate(height=GRID, width=GRID, in_channels=IN_CH, out_channels=3, base=32,
-                      max_batch=batch, seed=seed)
+    net = G.Surrogate(height=GRID, width=GRID, in_channels=IN_CH, out_channels=3, base=base,
+                      max_batch=batch, seed=seed, products=products)
     net.set_dataset(x, t, m)
     net.train(np.arange(samples), batch)  # warm-up
     t0 = time.perf_counter()
@@ -343,10 +343,14 @@ def main(argv=None):
                    help="only time training on random inputs (samples/s)")
     p.add_argument("--reference-start", action="store_true",
                    help="no network: seed the warm starts with the reference fields")
+    p.add_argument("--products", default="tcgen05", choices=["tcgen05", "mma"],
+                   help="tensor-core path of the network's convolution products")
+    p.add_argument("--base", type=int, default=32, help="channels of the first level")
     a = p.parse_args(argv)
     if a.throughput:
-        rate = train_throughput(batch=a.batch)
-        print(json.dumps({"train_samples_per_s": rate, "batch": a.batch, "grid": GRID}))
+        rate = train_throughput(batch=a.batch, products=a.products, base=a.base)
+        print(json.dumps({"train_samples_per_s": rate, "batch": a.batch, "grid": GRID,
+                          "products": a.products, "base": a.base}))
         return {"train_samples_per_s": rate}
     cases = make_cases(a.cavities, a.channels, a.seed, cavity_re=(100.0, a.cavity_re_max))
     meshes, X, Y, M, gen, gen_s = generate(cases, a.max_steps, a.check_every, a.gen_tol)
@@ -369,7 +373,7 @@ def main(argv=None):
     n_samples = len(Xt)
     net, hist, train_s = train(Xt, Yt, Mt, np.arange(len(Xt)), a.epochs, a.batch, a.lr, a.seed,
                                weight_decay=a.weight_decay, coarse_weight=a.coarse_weight,
-                               coarse_block=a.coarse_block)
+                               coarse_block=a.coarse_block, base=a.base, products=a.products)
     del Xt, Yt, Mt
     test_mse = masked_mse(net, X, Y, M, te)[0] if len(te) else None
     ev = evaluate(net, cases, meshes, X, Y, M, te[: a.eval], a.max_steps, a.check_every, a.tol)

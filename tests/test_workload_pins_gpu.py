@@ -9,6 +9,10 @@ serial/CellFunctions.c:372-395): both diverge, at the same step, so the NaN
 is the reference arithmetic's instability at that viscosity, not the
 library's.  A cavity of the same size at cell Re 6 stays finite, and a batch
 of the three freezes the two diverging cases without stopping the third.
+
+Cylinder wake (the 2048 x 512 channel at Re 200, scaled to 512 x 128 at the
+same Reynolds number): mean drag coefficient and Strouhal number of each
+reduced storage against FP64 (test_cylinder_wake_statistics_against_fp64).
 """
 import numpy as np
 import pytest
@@ -89,3 +93,51 @@ def test_batch_freezes_the_diverging_cases():
     assert r["steps"][2] == 2000 and r["steps"][0] < 1000 and r["steps"][1] < 1000
     assert np.isfinite(b.fields(2)["u"]).all()
     b.close()
+
+
+# ---------------------------------------------------------------------------
+# Cylinder wake at Re 200 (the 2048 x 512 channel of diameter 64, scaled to a
+# 512 x 128 channel and diameter 16 at the same Reynolds number, parabolic
+# inlet u_max 0.04, constant-pressure outlet, the cylinder one node off the
+# axis): the vortex street's mean drag coefficient and Strouhal number in
+# each reduced storage against FP64, over 80k steps after 60k steps of
+# development (about 25 shedding periods).
+
+def cylinder_stats(precision, warm=60000, sample=80000, every=25):
+    from parallellbmcranfield_gb300.workloads import cylinder_stats as stats
+
+    d, re, u_mean = 16, 200.0, 0.04 / 1.5
+    mesh = G.Mesh.channel(510, 126, [(100.0, 64.5, d / 2)])
+    s = G.Solver(mesh, uavg=u_mean, viscosity=u_mean * d / re, inlet_profile=1,
+                 collision_model=G.MRT, curved_boundaries=1, outlet_profile=4, rho_out=1.0,
+                 drag_lift_id=5, precision=precision)
+    s.set_state(None, np.ones(s.N), np.zeros(s.N), np.zeros(s.N))
+    s.step(warm)
+    fx, fy = [], []
+    for _ in range(sample // every):
+        s.step(every)
+        dg = s.check()
+        fx.append(dg["force"][0])
+        fy.append(dg["force"][1])
+    s.close()
+    return stats(np.array(fx), np.array(fy), every, u_mean, d)
+
+
+_cyl64 = {}
+
+
+@pytest.mark.parametrize("precision,tol_cd,tol_st", [(G.FP32, 0.005, 0.005),
+                                                     (G.FP16NEQ, 0.01, 0.01),
+                                                     (G.FP16DEV, 0.01, 0.02)])
+def test_cylinder_wake_statistics_against_fp64(precision, tol_cd, tol_st):
+    """Mean drag within 1 % of FP64 in every reduced storage (0.5 % FP32), the
+    Strouhal number within 1 % (FP16-dev: 2 %: its shedding phase drifts)."""
+    if "ref" not in _cyl64:
+        _cyl64["ref"] = cylinder_stats(G.FP64)
+    ref = _cyl64["ref"]
+    got = cylinder_stats(precision)
+    print(f"precision {precision}: C_D {got['cd_mean']:.4f} (FP64 {ref['cd_mean']:.4f}), "
+          f"St {got['strouhal']:.4f} (FP64 {ref['strouhal']:.4f})")
+    assert 0.2 < ref["strouhal"] < 0.35 and ref["cl_amp"] > 0.5  # a shedding wake
+    assert abs(got["cd_mean"] - ref["cd_mean"]) <= tol_cd * ref["cd_mean"]
+    assert abs(got["strouhal"] - ref["strouhal"]) <= tol_st * ref["strouhal"]

@@ -189,8 +189,8 @@ lbm_status lbm_inspect_mesh(const lbm_mesh *mesh, const lbm_params *params, int3
  * many independent domains (cavities, channels of different sizes and
  * parameters) advanced together: per step one launch over a device-side
  * list of (case, tile), and alongside it one over the (case, node)
- * list of boundary nodes; both lists are compacted to the cases still stepping
- * at the start of every run segment.  Per-case convergence flags live on the
+ * list of boundary nodes (sorted by boundary kind); the tile list is compacted
+ * to the cases still stepping at the start of every run segment.  Per-case convergence flags live on the
  * device; each run segment (check_every steps and one check) is one CUDA graph
  * replay.  All cases share precision (FP64, FP32 or FP16-dev), the A-B pattern,
  * the collision model and the device; everything else is per case.

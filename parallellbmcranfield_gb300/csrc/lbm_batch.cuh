@@ -256,7 +256,6 @@ struct BatchKernels {
   const void *advance;
   const void *converge;
   const void *compact_tiles;    // k_batch_compact<int4>
-  const void *compact_special;  // k_batch_compact<int2>
 };
 
 }  // namespace lbm

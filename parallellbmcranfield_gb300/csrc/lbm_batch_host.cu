@@ -59,11 +59,11 @@ struct lbm_batch {
   int ntiles[lbm::BVAR] = {};
   int4 *d_rows = nullptr;
   int nrows = 0;
-  int2 *d_special = nullptr;  // (case, node) of every node with boundary work
+  int2 *d_special = nullptr;  // (case, node) of every node with boundary work, sorted by kind
   int nspecial = 0;
+  int *d_nspecial = nullptr;  // nspecial on the device (the boundary-node kernel's count)
   int4 *d_live_tiles = nullptr;   // compacted work lists of the cases still stepping
-  int2 *d_live_special = nullptr;
-  int *d_live_n = nullptr;        // [0]: live tiles, [1]: live special nodes
+  int *d_live_n = nullptr;        // [0]: live tiles
   int variant = 1;
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;  // boundary-node pass, concurrent with the bulk pass
@@ -157,17 +157,13 @@ lbm_status set_rest(lbm_batch *b) {
 // The work lists of the cases still stepping (start of every run segment).
 lbm_status launch_compact(lbm_batch *b) {
   LBM_BCK(cudaMemsetAsync(b->d_live_n, 0, 2 * sizeof(int), b->stream));
-  int *cnt_t = b->d_live_n, *cnt_s = b->d_live_n + 1;
+  int *cnt_t = b->d_live_n;
   int nt = b->ntiles[b->variant];
   void *targs[] = {&b->d_tiles[b->variant], &nt, &b->s.active, &b->d_live_tiles, &cnt_t};
   cudaError_t e = cudaLaunchKernel(b->bk->compact_tiles, dim3(std::min((nt + 255) / 256, 152 * 8)),
                                    dim3(256), targs, 0, b->stream);
-  if (e == cudaSuccess && b->nspecial > 0) {
-    void *sargs[] = {&b->d_special, &b->nspecial, &b->s.active, &b->d_live_special, &cnt_s};
-    e = cudaLaunchKernel(b->bk->compact_special,
-                         dim3(std::min((b->nspecial + 255) / 256, 152 * 8)), dim3(256), sargs, 0,
-                         b->stream);
-  }
+  // the boundary-node list is not compacted: an atomic compaction would
+  // scatter its sorted order; entries of converged cases return at once
   if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch compact: ") + cudaGetErrorString(e));
   return LBM_OK;
 }
@@ -182,7 +178,7 @@ lbm_status launch_steps(lbm_batch *b, int k) {
   void *step_args0 = b->bk->per_tile ? (void *)b->d_bulk : (void *)b->d_cases;
   lbm_status st = launch_compact(b);
   if (st != LBM_OK) return st;
-  int *cnt_t = b->d_live_n, *cnt_s = b->d_live_n + 1;
+  int *cnt_t = b->d_live_n;
   for (int i = 0; i < k; i++) {
     // the boundary-node pass writes other nodes than the bulk pass and both
     // only read the source state, so it runs on a second stream alongside
@@ -195,7 +191,7 @@ lbm_status launch_steps(lbm_batch *b, int k) {
     cudaError_t e = cudaLaunchKernel(fn, dim3(grid), dim3(bx), args, 0, b->stream);
     if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
     if (b->nspecial > 0) {
-      void *sargs[] = {&b->d_cases, &b->d_live_special, &cnt_s, &b->s.active, &b->s.gpar};
+      void *sargs[] = {&b->d_cases, &b->d_special, &b->d_nspecial, &b->s.active, &b->s.gpar};
       const int sg = std::min((b->nspecial + 127) / 128, 152 * 16);
       e = cudaLaunchKernel(b->bk->special[b->model], dim3(sg), dim3(128), sargs, 0, b->side);
       if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch special: ") + cudaGetErrorString(e));
@@ -292,6 +288,7 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
   std::vector<std::vector<int4>> tiles(lbm::BVAR);
   std::vector<int4> rows;
   std::vector<int2> specials;
+  std::vector<uint32_t> special_key;
   const size_t es = (size_t)b->ks->elem_size;
   const double w[9] = {4. / 9., 1. / 9., 1. / 9., 1. / 9., 1. / 9., 1. / 36., 1. / 36., 1. / 36., 1. / 36.};
   for (int c = 0; c < ncases; c++) {
@@ -358,7 +355,22 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
     }
     for (int y = 0; y < P.m; y++)
       for (int tx = 0; tx < (P.n + 127) / 128; tx++) rows.push_back(make_int4(c, tx, y, 0));
-    for (const lbm::BRec &r : P.rec) specials.push_back(make_int2(c, (int)r.node));
+    for (const lbm::BRec &r : P.rec) {
+      specials.push_back(make_int2(c, (int)r.node));
+      special_key.push_back(r.flags);
+    }
+  }
+  {
+    // nodes of the same boundary kind (equal flags: streamed links, walls,
+    // lid / inlet / outlet) next to each other, so that the warps of the
+    // boundary-node pass take one path through the treatment instead of all
+    std::vector<size_t> ord(specials.size());
+    for (size_t i = 0; i < ord.size(); i++) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](size_t x, size_t y) { return special_key[x] < special_key[y]; });
+    std::vector<int2> sorted(specials.size());
+    for (size_t i = 0; i < ord.size(); i++) sorted[i] = specials[ord[i]];
+    specials.swap(sorted);
   }
   if ((st = balloc(b, &b->d_cases, (size_t)ncases)) != LBM_OK) return bail(st);
   cudaMemcpy(b->d_cases, b->hcases.data(), ncases * sizeof(lbm::BatchCase), cudaMemcpyHostToDevice);
@@ -395,11 +407,12 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
   size_t max_tiles = 0;
   for (int v = 0; v < lbm::BVAR; v++) max_tiles = std::max(max_tiles, tiles[v].size());
   if ((st = balloc(b, &b->d_live_tiles, max_tiles)) != LBM_OK ||
-      (st = balloc(b, &b->d_live_special, specials.size())) != LBM_OK ||
       (st = balloc(b, &b->d_live_n, 2)) != LBM_OK)
     return bail(st);
   b->nspecial = (int)specials.size();
   if ((st = balloc(b, &b->d_special, specials.size())) != LBM_OK) return bail(st);
+  if ((st = balloc(b, &b->d_nspecial, 1)) != LBM_OK) return bail(st);
+  cudaMemcpy(b->d_nspecial, &b->nspecial, sizeof(int), cudaMemcpyHostToDevice);
   if (!specials.empty())
     cudaMemcpy(b->d_special, specials.data(), specials.size() * sizeof(int2), cudaMemcpyHostToDevice);
   b->nrows = (int)rows.size();

@@ -52,7 +52,6 @@ const BatchKernels &LBM_BATCH_FN(LBM_PREC)() {
     k.advance = (const void *)k_batch_advance;
     k.converge = (const void *)k_batch_converge;
     k.compact_tiles = (const void *)k_batch_compact<int4>;
-    k.compact_special = (const void *)k_batch_compact<int2>;
     return k;
   }();
   return bk;

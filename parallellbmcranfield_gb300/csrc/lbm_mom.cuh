@@ -291,14 +291,14 @@ __device__ __forceinline__ void mom_raw_load(const StepArgs &a, const void *b, l
 }
 
 // Post-collision deviations of both nodes of a pair (the arithmetic of
-// mom_to_pops on FP32 pairs): the 24-bit codes are assembled by byte
-// permutes, [low byte, high int16, sign of the high int16].
+// mom_to_pops on FP32 pairs): each 24-bit code is its int16 high part
+// shifted into bits 8..31 with its sign, or the low byte.
 __device__ __forceinline__ void mom_decode2(const StepArgs &a, const MomRaw &w, float2 d[9]) {
   float2 q[3];
 #pragma unroll
   for (int p = 0; p < 3; p++) {
-    const int q0 = (int)__byte_perm(w.l[p], w.h[p], 0xD540);
-    const int q1 = (int)__byte_perm(w.l[p], w.h[p], 0xF761);
+    const int q0 = ((int)(w.h[p] << 16) >> 8) | (int)(w.l[p] & 0xffu);
+    const int q1 = ((int)(w.h[p] & 0xffff0000u) >> 8) | (int)((w.l[p] >> 8) & 0xffu);
     q[p] = mul2(make_float2((float)q0, (float)q1), bc2(fx_step(a, p)));
   }
   float2 n[6];

@@ -10,7 +10,7 @@
 //               per block, N = BN output channels), pixels split over
 //               blockIdx.z, FP32 atomics into dW.
 //
-// Pipeline: TC_STAGES shared-memory stages of TC_BK = 64 K values; all 128
+// Pipeline: 3 or 4 shared-memory stages of TC_BK = 64 K values; all 128
 // threads fill a stage with 16-byte cp.async copies (zero-filled where the
 // im2col or the tile runs out), fence them to the async proxy, and thread 0
 // issues four 128 x BN x 16 MMAs (kind::f16, BF16 in, FP32 accumulate) and a
@@ -41,7 +41,6 @@ using bf16 = __nv_bfloat16;
 
 constexpr int TC_BM = 128;
 constexpr int TC_BK = 64;
-constexpr int TC_STAGES = 3;
 constexpr int TC_THREADS = 128;
 constexpr long long TC_POLLS = 1ll << 20;  // mbarrier polls before a wait gives up (about a second)
 
@@ -143,12 +142,14 @@ __device__ __forceinline__ void tm_ld16(uint32_t taddr, float v[16]) {
 
 // Dynamic shared memory of a block: the stages, then the mbarriers and the
 // tensor-memory address (1024-byte aligned base).
+// Ring depth: 4 stages up to 64 columns (two blocks fit an SM), 3 at 128.
 template <int BN>
 struct TcSmem {
+  static constexpr int STAGES = BN >= 128 ? 3 : 4;
   static constexpr int A_BYTES = TC_BM * TC_BK * 2;
   static constexpr int B_BYTES = BN * TC_BK * 2;
   static constexpr int STAGE = A_BYTES + B_BYTES;
-  static constexpr int BYTES = TC_STAGES * STAGE + 64;
+  static constexpr int BYTES = STAGES * STAGE + 64;
   static constexpr int ALLOC = BYTES + 1024;  // room to align the base
 };
 
@@ -162,17 +163,17 @@ __device__ __forceinline__ bool tc_mainloop(uint8_t *sm, uint32_t tmem, int nk, 
                                             uint32_t b_lbo, uint32_t b_sbo, uint32_t b_k16,
                                             Load load, int *err) {
   using S = TcSmem<BN>;
-  uint64_t *bars = (uint64_t *)(sm + TC_STAGES * S::STAGE);
+  uint64_t *bars = (uint64_t *)(sm + S::STAGES * S::STAGE);
   const int tid = threadIdx.x;
 #pragma unroll
-  for (int s = 0; s < TC_STAGES - 1; s++) {
+  for (int s = 0; s < S::STAGES - 1; s++) {
     if (s < nk) load(sm + s * S::STAGE, sm + s * S::STAGE + S::A_BYTES, s);
     cp_commit();
   }
   bool ok = true;
   for (int kt = 0; kt < nk; kt++) {
-    const int s = kt % TC_STAGES;
-    cp_wait<TC_STAGES - 2>();
+    const int s = kt % S::STAGES;
+    cp_wait<S::STAGES - 2>();
     fence_async_smem();
     if (!__syncthreads_and(ok)) {
       ok = false;
@@ -187,17 +188,17 @@ __device__ __forceinline__ bool tc_mainloop(uint8_t *sm, uint32_t tmem, int nk, 
                idesc, (kt | kk) != 0);
       tc_commit(&bars[s]);
     }
-    const int nt = kt + TC_STAGES - 1;
+    const int nt = kt + S::STAGES - 1;
     if (nt < nk) {
       // stage nt % S was last read by the MMAs of tile kt - 1
-      if (kt >= 1 && !mb_wait(&bars[(kt - 1) % TC_STAGES], ((kt - 1) / TC_STAGES) & 1)) ok = false;
-      if (ok) load(sm + (nt % TC_STAGES) * S::STAGE, sm + (nt % TC_STAGES) * S::STAGE + S::A_BYTES, nt);
+      if (kt >= 1 && !mb_wait(&bars[(kt - 1) % S::STAGES], ((kt - 1) / S::STAGES) & 1)) ok = false;
+      if (ok) load(sm + (nt % S::STAGES) * S::STAGE, sm + (nt % S::STAGES) * S::STAGE + S::A_BYTES, nt);
     }
     cp_commit();
   }
   cp_wait<0>();
   // the last commit covers every MMA issued before it
-  if (nk > 0 && !mb_wait(&bars[(nk - 1) % TC_STAGES], ((nk - 1) / TC_STAGES) & 1)) ok = false;
+  if (nk > 0 && !mb_wait(&bars[(nk - 1) % S::STAGES], ((nk - 1) / S::STAGES) & 1)) ok = false;
   ok = __syncthreads_and(ok) != 0;
   __syncwarp();  // thread 0 issued the MMAs alone; the epilogue's tcgen05.ld needs the whole warp
   tc_fence_after();
@@ -209,10 +210,10 @@ __device__ __forceinline__ bool tc_mainloop(uint8_t *sm, uint32_t tmem, int nk, 
 template <int BN>
 __device__ __forceinline__ uint32_t tc_setup(uint8_t *sm) {
   using S = TcSmem<BN>;
-  uint64_t *bars = (uint64_t *)(sm + TC_STAGES * S::STAGE);
-  uint32_t *slot = (uint32_t *)(bars + TC_STAGES);
+  uint64_t *bars = (uint64_t *)(sm + S::STAGES * S::STAGE);
+  uint32_t *slot = (uint32_t *)(bars + S::STAGES);
   if (threadIdx.x == 0)
-    for (int s = 0; s < TC_STAGES; s++) mb_init(&bars[s], 1);
+    for (int s = 0; s < S::STAGES; s++) mb_init(&bars[s], 1);
   // tcgen05.alloc / ld / dealloc are .sync.aligned: the warp must arrive
   // converged, also after code that only one of its threads ran
   __syncwarp();
@@ -253,38 +254,47 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_conv(const bf16 *__restrict__
   const int m0 = blockIdx.x * TC_BM, n0 = blockIdx.y * BN;
   const int KC = taps * C;
   const int nk = (Kp + TC_BK - 1) / TC_BK;
-  // this thread's pixel (row tid of the A tile)
-  const int p = m0 + tid;
-  const bool pin = p < P;
-  const int px = pin ? p % W : 0, py = pin ? (p / W) % H : 0;
+  // Copy pattern: one warp instruction moves 8 rows x 4 consecutive 16-byte
+  // chunks (64 contiguous bytes of a pixel's tap in global memory; in shared
+  // memory 8 distinct row slots of 16 bytes, the minimum 4 wavefronts).
+  // This thread's rows of the A tile: rb * 8 + lane / 4 for rb = 4 j + warp.
+  const int lane = tid & 31, warp = tid >> 5, l4 = lane & 3, r8 = lane >> 2;
+  int pp[4], px[4], py[4];
+  bool pin[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    pp[j] = m0 + (j * 4 + warp) * 8 + r8;
+    pin[j] = pp[j] < P;
+    px[j] = pin[j] ? pp[j] % W : 0;
+    py[j] = pin[j] ? (pp[j] / W) % H : 0;
+  }
   auto load = [&](uint8_t *sa, uint8_t *sb, int kt) {
     const uint32_t a = saddr(sa), b = saddr(sb);
     const int k0 = kt * TC_BK;
 #pragma unroll
-    for (int kc = 0; kc < 8; kc++) {
+    for (int i = 0; i < 8; i++) {
+      const int j = i >> 1, kc = (i & 1) * 4 + l4;
       const int k = k0 + kc * 8;
       const int r = k / C, c = k - r * C;
       const int dy = taps == 9 ? r / 3 - 1 : 0, dx = taps == 9 ? r % 3 - 1 : 0;
-      const int yy = py + dy, xx = px + dx;
-      const bool ok = pin && k < KC && yy >= 0 && yy < H && xx >= 0 && xx < W;
-      const bf16 *src = ok ? X + ((size_t)(p + dy * W + dx) * C + c) : X;
-      cp16(a + (tid >> 3) * 1024 + kc * 128 + (tid & 7) * 16, src, ok);
+      const int yy = py[j] + dy, xx = px[j] + dx;
+      const bool ok = pin[j] && k < KC && yy >= 0 && yy < H && xx >= 0 && xx < W;
+      const bf16 *src = ok ? X + ((size_t)(pp[j] + dy * W + dx) * C + c) : X;
+      cp16(a + (j * 4 + warp) * 1024 + kc * 128 + r8 * 16, src, ok);
     }
-    // B tile: BN rows x 8 chunks of 8 k values
+    // B tile: BN rows x 8 chunks, row blocks of 8 by the same pattern
 #pragma unroll
     for (int i = 0; i < BN / 16; i++) {
-      const int ch = tid + i * TC_THREADS;
-      const int r = ch & (BN - 1), kc = ch / BN;
+      const int rb = (i >> 1) * 4 + warp, kc = (i & 1) * 4 + l4;
+      const int r = rb * 8 + r8;
       const int k = k0 + kc * 8;
       const bool ok = n0 + r < N && k < Kp;
-      cp16(b + (r >> 3) * 1024 + kc * 128 + (r & 7) * 16, ok ? Bt + (size_t)(n0 + r) * Kp + k : Bt,
-           ok);
+      cp16(b + rb * 1024 + kc * 128 + r8 * 16, ok ? Bt + (size_t)(n0 + r) * Kp + k : Bt, ok);
     }
   };
   const bool ok = tc_mainloop<BN>(sm, tmem, nk, tc_idesc(BN, 0, 0), 128, 1024, 256, 128, 1024, 256,
                                   load, err);
   if (ok) {
-    const int warp = tid >> 5, lane = tid & 31;
     const int row = m0 + warp * 32 + lane;
 #pragma unroll
     for (int c0 = 0; c0 < BN; c0 += 16) {
@@ -333,33 +343,42 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_wgrad(const bf16 *__restrict_
   const int KC = taps * C;
   const int pbeg = blockIdx.z * pchunk, pend = min(P, pbeg + pchunk);
   const int nk = pend > pbeg ? (pend - pbeg + TC_BK - 1) / TC_BK : 0;
-  const int pk = tid & 63, half = tid >> 6;  // pixel of the K tile, half of the chunk range
+  // Copy pattern: one warp instruction moves 8 pixels x 4 consecutive
+  // 16-byte chunks (64 contiguous bytes per pixel in global memory, 8 distinct
+  // pixel slots in shared memory).  This thread's pixels of a K tile:
+  // (2 warp + h) * 8 + lane / 4 for h = 0, 1.
+  const int lane = tid & 31, warp = tid >> 5, l4 = lane & 3, r8 = lane >> 2;
   auto load = [&](uint8_t *sa, uint8_t *sb, int kt) {
     const uint32_t a = saddr(sa), b = saddr(sb);
-    const int p = pbeg + kt * TC_BK + pk;
-    const bool pin = p < pend;
-    const int px = pin ? p % W : 0, py = pin ? (p / W) % H : 0;
-    const uint32_t kofs = (pk >> 3) * (TC_BM * 16) + (pk & 7) * 16;
-    // A: 16 chunks of 8 k values at this pixel, 8 per thread
+    int p[2], px[2], py[2];
+    bool pin[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      p[h] = pbeg + kt * TC_BK + (2 * warp + h) * 8 + r8;
+      pin[h] = p[h] < pend;
+      px[h] = pin[h] ? p[h] % W : 0;
+      py[h] = pin[h] ? (p[h] / W) % H : 0;
+    }
+    // A: 16 chunks of 8 k values per pixel
 #pragma unroll
     for (int i = 0; i < 8; i++) {
-      const int kc = half * 8 + i;
+      const int h = i & 1, kc = (i >> 1) * 4 + l4;
       const int k = m0 + kc * 8;
       const int r = k / C, c = k - r * C;
       const int dy = taps == 9 ? r / 3 - 1 : 0, dx = taps == 9 ? r % 3 - 1 : 0;
-      const int yy = py + dy, xx = px + dx;
-      const bool ok = pin && k < KC && yy >= 0 && yy < H && xx >= 0 && xx < W;
-      const bf16 *src = ok ? X + ((size_t)(p + dy * W + dx) * C + c) : X;
-      cp16(a + kofs + kc * 128, src, ok);
+      const int yy = py[h] + dy, xx = px[h] + dx;
+      const bool ok = pin[h] && k < KC && yy >= 0 && yy < H && xx >= 0 && xx < W;
+      const bf16 *src = ok ? X + ((size_t)(p[h] + dy * W + dx) * C + c) : X;
+      cp16(a + (2 * warp + h) * (TC_BM * 16) + kc * 128 + r8 * 16, src, ok);
     }
-    // B: BN / 8 chunks of 8 output channels at this pixel, split over the halves
-    const uint32_t bofs = (pk >> 3) * (BN * 16) + (pk & 7) * 16;
+    // B: BN / 8 chunks of 8 output channels per pixel
 #pragma unroll
     for (int i = 0; i < BN / 16; i++) {
-      const int cc = half * (BN / 16) + i;
+      const int h = i & 1, cc = (i >> 1) * 4 + l4;
       const int n = n0 + cc * 8;
-      const bool ok = pin && n < N;
-      cp16(b + bofs + cc * 128, ok ? dZ + (size_t)p * N + n : dZ, ok);
+      const bool ok = pin[h] && n < N;
+      cp16(b + (2 * warp + h) * (BN * 16) + cc * 128 + r8 * 16, ok ? dZ + (size_t)p[h] * N + n : dZ,
+           ok);
     }
   };
   // MN-major without swizzle: LBO is the K-direction stride of 8-row groups,
@@ -367,7 +386,6 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_wgrad(const bf16 *__restrict_
   const bool ok = tc_mainloop<BN>(sm, tmem, nk, tc_idesc(BN, 1, 1), TC_BM * 16, 128, 2 * TC_BM * 16,
                                   BN * 16, 128, 2 * BN * 16, load, err);
   if (ok && nk > 0) {
-    const int warp = tid >> 5, lane = tid & 31;
     const int k = m0 + warp * 32 + lane;
 #pragma unroll
     for (int c0 = 0; c0 < BN; c0 += 16) {

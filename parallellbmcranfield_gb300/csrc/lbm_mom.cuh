@@ -301,21 +301,22 @@ __device__ __forceinline__ void mom_decode2(const StepArgs &a, const MomRaw &w, 
     const int q1 = ((int)(w.h[p] & 0xffff0000u) >> 8) | (int)((w.l[p] >> 8) & 0xffu);
     q[p] = mul2(make_float2((float)q0, (float)q1), bc2(fx_step(a, p)));
   }
-  float2 n[6];
+  float2 n[6];  // stored units (n_i * neq_s); the inverse scale enters the FMAs below
 #pragma unroll
   for (int i = 0; i < 6; i++) {
     __half2 h;
     memcpy(&h, &w.n[i], 4);
-    n[i] = mul2(__half22float2(h), bc2(a.neq_is));
+    n[i] = __half22float2(h);
   }
+  const float2 is = bc2(a.neq_is);
   const float2 r = q[0], x = q[1], y = q[2];
   const float2 i0 = bc2(a.fx_irho0);
   const float2 jj = fma2(x, x, mul2(y, y));
-  const float2 m1 = add2(fma2(bc2(3.f), jj, mul2(bc2(-2.f), r)), n[0]);
-  const float2 m2 = add2(fma2(bc2(-3.f), jj, r), n[1]);
-  const float2 m4 = sub2(n[2], x), m6 = sub2(n[3], y);
-  const float2 m7 = fma2(mul2(sub2(x, y), add2(x, y)), i0, n[4]);
-  const float2 m8 = fma2(mul2(x, y), i0, n[5]);
+  const float2 m1 = fma2(n[0], is, fma2(bc2(3.f), jj, mul2(bc2(-2.f), r)));
+  const float2 m2 = fma2(n[1], is, fma2(bc2(-3.f), jj, r));
+  const float2 m4 = fma2(n[2], is, mul2(bc2(-1.f), x)), m6 = fma2(n[3], is, mul2(bc2(-1.f), y));
+  const float2 m7 = fma2(n[4], is, mul2(mul2(sub2(x, y), add2(x, y)), i0));
+  const float2 m8 = fma2(n[5], is, mul2(mul2(x, y), i0));
   const float2 ax = sub2(fma2(bc2(4.f), r, mul2(bc2(-2.f), m2)), m1);
   const float2 dg = fma2(bc2(2.f), m1, fma2(bc2(4.f), r, m2));
   const float2 P = mul2(bc2(9.f), m7), Q = mul2(bc2(9.f), m8);
@@ -365,7 +366,9 @@ template <int MODEL>
 __device__ __forceinline__ void collide_mom2(float2 r, float2 jx, float2 jy, float2 m[6],
                                             const StepArgs &a) {
   const float2 rho = add2(bc2((float)a.rho0), r);
-  const float2 inv = make_float2(__frcp_rn(rho.x), __frcp_rn(rho.y));
+  // 1 / rho enters only the equilibria of the non-conserved moments, whose
+  // stored form keeps 11 bits: the approximate reciprocal is ample
+  const float2 inv = make_float2(__fdividef(1.f, rho.x), __fdividef(1.f, rho.y));
   const float2 jj = fma2(jx, jx, mul2(jy, jy));
   const float2 q = MODEL == 3 ? jj : mul2(jj, inv);
   const float2 e1 = fma2(bc2(3.f), q, mul2(bc2(-2.f), r)), e2 = fma2(bc2(-3.f), q, r);
@@ -387,38 +390,50 @@ __device__ __forceinline__ void mom_encode_store2(const StepArgs &a, void *b, lo
                                                   uint32_t hseed, float2 r, float2 jx, float2 jy,
                                                   const float2 m[6], bool own0, bool own1,
                                                   bool &ok) {
-  float u0[3], u1[3];
-  {
-    const uint32_t h0 = mix32((uint32_t)z ^ hseed), h1 = mix32((uint32_t)(z + 1) ^ hseed);
-#pragma unroll
-    for (int p = 0; p < 3; p++) {
-      u0[p] = (float)((h0 >> (10 * p)) & 1023u) * (1.f / 1024.f) + (1.f / 2048.f);
-      u1[p] = (float)((h1 >> (10 * p)) & 1023u) * (1.f / 1024.f) + (1.f / 2048.f);
-    }
-  }
+  // dithers of the pair from one hash: node 0 in bits 0..15, node 1 in
+  // 16..31, 6 bits for rho and 5 each for j (bias below 1/64 of a step)
+  const uint32_t h = mix32((uint32_t)z ^ hseed);
   const float2 v[3] = {r, jx, jy};
-  int q0[3], q1[3];
+  const int sh[3] = {0, 6, 11}, nb[3] = {6, 5, 5};
+  float2 t[3];
   bool ok0 = true, ok1 = true;
 #pragma unroll
   for (int p = 0; p < 3; p++) {
-    q0[p] = fx_code(v[p].x, fx_istep(a, p), u0[p], ok0);
-    q1[p] = fx_code(v[p].y, fx_istep(a, p), u1[p], ok1);
+    const uint32_t mask = (1u << nb[p]) - 1u;
+    const float sc = 1.f / (float)(1u << nb[p]);
+    const float u0 = ((float)((h >> sh[p]) & mask) + 0.5f) * sc;
+    const float u1 = ((float)((h >> (16 + sh[p])) & mask) + 0.5f) * sc;
+    const float2 x = mul2(v[p], bc2(fx_istep(a, p)));
+    const float2 xi = make_float2(floorf(x.x), floorf(x.y));
+    const float2 fr = sub2(x, xi);
+    t[p] = make_float2(xi.x + (fr.x > u0 ? 1.f : 0.f), xi.y + (fr.y > u1 ? 1.f : 0.f));
+    ok0 = ok0 && fabsf(t[p].x) <= (float)MOM_QMAX;
+    ok1 = ok1 && fabsf(t[p].y) <= (float)MOM_QMAX;
   }
   if (own0) ok = ok && ok0;
   if (own1) ok = ok && ok1;
-  float2 s[3];
-#pragma unroll
-  for (int p = 0; p < 3; p++) s[p] = mul2(make_float2((float)q0[p], (float)q1[p]), bc2(fx_step(a, p)));
-  const float2 i0 = bc2(a.fx_irho0);
-  const float2 jj = fma2(s[1], s[1], mul2(s[2], s[2]));
-  const float2 bb[6] = {fma2(bc2(3.f), jj, mul2(bc2(-2.f), s[0])), fma2(bc2(-3.f), jj, s[0]),
-                        mul2(bc2(-1.f), s[1]), mul2(bc2(-1.f), s[2]),
-                        mul2(mul2(sub2(s[1], s[2]), add2(s[1], s[2])), i0), mul2(mul2(s[1], s[2]), i0)};
+  // references b_i (times neq_s) of the stored conserved moments
+  const float ns = a.neq_s;
+  const float2 sr = mul2(t[0], bc2(fx_step(a, 0))), sx = mul2(t[1], bc2(fx_step(a, 1))),
+               sy = mul2(t[2], bc2(fx_step(a, 2)));
+  const float2 i0 = bc2(a.fx_irho0 * ns);
+  const float2 jj = fma2(sx, sx, mul2(sy, sy));
+  // minus the references, so that each stored value is one multiply-add
+  const float2 mref[6] = {fma2(bc2(-3.f * ns), jj, mul2(bc2(2.f * ns), sr)),
+                        fma2(bc2(3.f * ns), jj, mul2(bc2(-ns), sr)), mul2(bc2(ns), sx),
+                        mul2(bc2(ns), sy), mul2(mul2(sub2(sy, sx), add2(sx, sy)), i0),
+                        mul2(mul2(sx, sy), bc2(-a.fx_irho0 * ns))};
   uint32_t nw[6];
 #pragma unroll
   for (int i = 0; i < 6; i++) {
-    const __half2 h = __float22half2_rn(mul2(sub2(m[i], bb[i]), bc2(a.neq_s)));
-    memcpy(&nw[i], &h, 4);
+    const __half2 hh = __float22half2_rn(fma2(m[i], bc2(ns), mref[i]));
+    memcpy(&nw[i], &hh, 4);
+  }
+  int q0[3], q1[3];
+#pragma unroll
+  for (int p = 0; p < 3; p++) {
+    q0[p] = (int)t[p].x;
+    q1[p] = (int)t[p].y;
   }
   if (own0 && own1) {
 #pragma unroll
@@ -452,13 +467,90 @@ __device__ __forceinline__ void mom_encode_store2(const StepArgs &a, void *b, lo
 // destination row r+1, c_y = 0 to row r and c_y = -1 to row r-1, which is
 // then complete: it collides and stores (class-1 nodes only; class 2 and 3
 // belong to k_special_mom, solid nodes are never written).  The raw words of
-// source rows are loaded two rows ahead, and lanes 0..11 prefetch the warp's
-// span of row r + MOM_PF into L2 (a hint: nothing waits for it, every
-// prefetched byte lies inside the buffer and its guard bytes).
+// source rows are loaded two rows ahead into a ring of three, and lanes 0..11
+// prefetch the warp's span of row r + MOM_PF into L2 (a hint: nothing waits
+// for it, every prefetched byte lies inside the buffer and its guard bytes).
+// The row walk is a loop over groups of three rows, the period of the ring
+// and of the three population rows, so that the code stays small.
 constexpr int MOM_PF = 6;
-template <int MODEL, int NPT>
-__global__ void __launch_bounds__(128) k_step_mom(const __grid_constant__ StepArgs a) {
+
+struct MomWalk {
+  MomRaw raw[3];
+  float2 Fa[9], Fb[9], Fc[9];
+  bool ok;
+  float probe;
+};
+
+// Row j of the walk (source row y0 + j); PH = (j + 1) mod 3 selects the ring
+// slots: row j decodes slot PH and loads row j + 2 into slot (PH + 2) mod 3.
+template <int MODEL, int NPT, int PH>
+__device__ __forceinline__ void mom_walk_row(const StepArgs &a, MomWalk &w, int j, int y0, int wx,
+                                             int x0, int lane, bool inx, bool owner,
+                                             uint32_t hseed) {
   const unsigned FULL = 0xffffffffu;
+  const int r = y0 + j;
+  if (j + 2 <= NPT) {
+    const int r2 = r + 2;
+    mom_raw_load(a, a.src, (long long)r2 * a.pitch + x0, inx && r2 < a.m, w.raw[(PH + 2) % 3]);
+  }
+  if (lane < 12) {
+    const int rp = r + MOM_PF;
+    if (rp < a.m && j + MOM_PF <= NPT) {
+      const long long e = (long long)rp * a.pitch + wx - 2;
+      const char *base = (const char *)a.src;
+      const char *p = lane < 9 ? base + (long long)lane * 2 * a.plane + 2 * e
+                               : base + 18 * a.plane + (long long)(lane - 9) * a.plane + e;
+      const char *al = (const char *)((uintptr_t)p & ~(uintptr_t)15);
+      if (lane < 9)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], 144;" ::"l"(al) : "memory");
+      else
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], 80;" ::"l"(al) : "memory");
+    }
+  }
+  float2 d[9];
+  mom_decode2(a, w.raw[PH], d);
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    float2 v = d[k];
+    if (CX[k] == 1) {
+      const float left = __shfl_up_sync(FULL, d[k].y, 1);
+      v = make_float2(left, d[k].x);
+    } else if (CX[k] == -1) {
+      const float right = __shfl_down_sync(FULL, d[k].x, 1);
+      v = make_float2(d[k].y, right);
+    }
+    if (CY[k] == 1) w.Fc[k] = v;
+    else if (CY[k] == 0) w.Fb[k] = v;
+    else w.Fa[k] = v;
+  }
+  if (j >= 1) {  // destination row r - 1 is complete
+    const int y = r - 1;
+    bool own0 = false, own1 = false;
+    if (owner && y < a.m) {
+      const uint32_t cw = __ldg((const unsigned short *)(a.cls + (long long)y * a.pitch + x0));
+      own0 = (cw & 0xffu) == CLS_BULK;
+      own1 = (cw >> 8) == CLS_BULK && x0 + 1 < a.n;
+    }
+    if (own0 || own1) {
+      float2 rr, jx, jy, m[6];
+      pops_to_mom2(w.Fa, rr, jx, jy, m);
+      collide_mom2<MODEL>(rr, jx, jy, m, a);
+      if (own0) w.probe += rr.x + m[4].x;
+      if (own1) w.probe += rr.y + m[4].y;
+      mom_encode_store2(a, a.dst, (long long)y * a.pitch + x0, hseed, rr, jx, jy, m, own0, own1,
+                        w.ok);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    w.Fa[k] = w.Fb[k];
+    w.Fb[k] = w.Fc[k];
+  }
+}
+
+template <int MODEL, int NPT, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_step_mom(const __grid_constant__ StepArgs a) {
+  static_assert((NPT + 2) % 3 == 0, "the row walk runs in groups of three rows");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int wx = (blockIdx.x * 4 + warp) * 60;
   if (wx >= a.n) return;  // the whole warp lies past the row
@@ -466,74 +558,25 @@ __global__ void __launch_bounds__(128) k_step_mom(const __grid_constant__ StepAr
   const bool inx = x0 >= 0 && x0 < a.pitch;  // the pitch is even, so x0 + 1 < pitch too
   const bool owner = lane >= 1 && lane <= 30 && x0 < a.n;
   const int y0 = blockIdx.y * NPT;
+  if (y0 - 1 >= a.m) return;
   const uint32_t hseed = mix32(a.gen * 0x9e3779b9u + 0x632be5abu);
-  MomRaw raw[3];
-  mom_raw_load(a, a.src, (long long)(y0 - 1) * a.pitch + x0, inx && y0 >= 1 && y0 - 1 < a.m, raw[0]);
-  mom_raw_load(a, a.src, (long long)y0 * a.pitch + x0, inx && y0 < a.m, raw[1]);
-  float2 Fa[9], Fb[9], Fc[9];
+  MomWalk w;
+  mom_raw_load(a, a.src, (long long)(y0 - 1) * a.pitch + x0, inx && y0 >= 1 && y0 - 1 < a.m,
+               w.raw[0]);
+  mom_raw_load(a, a.src, (long long)y0 * a.pitch + x0, inx && y0 < a.m, w.raw[1]);
 #pragma unroll
-  for (int k = 0; k < 9; k++) Fa[k] = Fb[k] = Fc[k] = make_float2(0.f, 0.f);
-  bool ok = true;
-  float probe = 0.f;
-#pragma unroll
-  for (int j = -1; j <= NPT; j++) {
-    const int r = y0 + j;
-    if (j + 2 <= NPT) {
-      const int r2 = r + 2;
-      mom_raw_load(a, a.src, (long long)r2 * a.pitch + x0, inx && r2 < a.m, raw[(j + 3) % 3]);
-    }
-    if (lane < 12) {
-      const int rp = r + MOM_PF;
-      if (rp >= 0 && rp < a.m && j + MOM_PF <= NPT) {
-        const long long e = (long long)rp * a.pitch + wx - 2;
-        const char *base = (const char *)a.src;
-        const char *p = lane < 9 ? base + (long long)lane * 2 * a.plane + 2 * e
-                                 : base + 18 * a.plane + (long long)(lane - 9) * a.plane + e;
-        const char *al = (const char *)((uintptr_t)p & ~(uintptr_t)15);
-        if (lane < 9)
-          asm volatile("cp.async.bulk.prefetch.L2.global [%0], 144;" ::"l"(al) : "memory");
-        else
-          asm volatile("cp.async.bulk.prefetch.L2.global [%0], 80;" ::"l"(al) : "memory");
-      }
-    }
-    float2 d[9];
-    mom_decode2(a, raw[(j + 1) % 3], d);
-#pragma unroll
-    for (int k = 0; k < 9; k++) {
-      float2 v = d[k];
-      if (CX[k] == 1) {
-        const float left = __shfl_up_sync(FULL, d[k].y, 1);
-        v = make_float2(left, d[k].x);
-      } else if (CX[k] == -1) {
-        const float right = __shfl_down_sync(FULL, d[k].x, 1);
-        v = make_float2(d[k].y, right);
-      }
-      if (CY[k] == 1) Fc[k] = v;
-      else if (CY[k] == 0) Fb[k] = v;
-      else Fa[k] = v;
-    }
-    if (j >= 1) {  // destination row r - 1 is complete
-      const int y = r - 1;
-      bool own0 = false, own1 = false;
-      if (owner && y < a.m) {
-        const uint32_t cw = __ldg((const unsigned short *)(a.cls + (long long)y * a.pitch + x0));
-        own0 = (cw & 0xffu) == CLS_BULK;
-        own1 = (cw >> 8) == CLS_BULK && x0 + 1 < a.n;
-      }
-      float2 rr, jx, jy, m[6];
-      pops_to_mom2(Fa, rr, jx, jy, m);
-      collide_mom2<MODEL>(rr, jx, jy, m, a);
-      if (own0) probe += rr.x + m[4].x;
-      if (own1) probe += rr.y + m[4].y;
-      mom_encode_store2(a, a.dst, (long long)y * a.pitch + x0, hseed, rr, jx, jy, m, own0, own1, ok);
-    }
-#pragma unroll
-    for (int k = 0; k < 9; k++) {
-      Fa[k] = Fb[k];
-      Fb[k] = Fc[k];
-    }
+  for (int k = 0; k < 9; k++) w.Fa[k] = w.Fb[k] = w.Fc[k] = make_float2(0.f, 0.f);
+  w.ok = true;
+  w.probe = 0.f;
+  // the last group may run past the domain's last row: rows past it load
+  // nothing and store nothing
+#pragma unroll 1
+  for (int j = -1; j <= NPT && y0 + j - 1 < a.m; j += 3) {
+    mom_walk_row<MODEL, NPT, 0>(a, w, j, y0, wx, x0, lane, inx, owner, hseed);
+    mom_walk_row<MODEL, NPT, 1>(a, w, j + 1, y0, wx, x0, lane, inx, owner, hseed);
+    mom_walk_row<MODEL, NPT, 2>(a, w, j + 2, y0, wx, x0, lane, inx, owner, hseed);
   }
-  mom_flag(a, ok, probe);
+  mom_flag(a, w.ok, w.probe);
 }
 
 // Nodes with boundary work (class 3) and their fluid neighbours (class 2),

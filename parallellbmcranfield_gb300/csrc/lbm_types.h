@@ -60,7 +60,8 @@ constexpr TileVariant VARS[NVAR] = {
 // Bulk-step tiles of the moment storage: blocks of 4 warps x 60 columns, these
 // rows per thread.
 constexpr int MOM_NVAR = 3;
-constexpr int MOM_NPT[MOM_NVAR] = {8, 16, 32};
+constexpr int MOM_NPT[MOM_NVAR] = {16, 34, 34};  // (NPT + 2) % 3 == 0
+constexpr int MOM_MINB[MOM_NVAR] = {5, 5, 4};    // resident blocks per SM (register cap)
 constexpr int TMA_MAX_SMEM = 200 * 1024;  // dynamic shared memory budget of one TMA block
 constexpr int TMA_MAX_STAGES = 4;
 

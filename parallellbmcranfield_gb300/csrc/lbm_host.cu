@@ -509,6 +509,9 @@ lbm_status lbm_create(const lbm_mesh *mesh, const lbm_params *params, lbm_ctx **
     a.fx_irho0 = (float)(1.0 / r0);
     a.neq_s = 4096.f;
     a.neq_is = 1.f / 4096.f;
+    a.f_rho0 = (float)a.rho0;
+    a.f_om = (float)a.omega;
+    a.f_omA = (float)a.omegaA;
     a.mlist = c->d_mlist;
     a.mlist_n = c->mlist_n;
   }

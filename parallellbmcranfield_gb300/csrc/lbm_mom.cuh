@@ -290,15 +290,24 @@ __device__ __forceinline__ void mom_raw_load(const StepArgs &a, const void *b, l
   for (int i = 0; i < 6; i++) w.n[i] = in ? __ldg((const unsigned *)(mom_n(b, a, i) + z)) : 0u;
 }
 
+// Byte permute with the PTX default mode: a selector nibble with bit 3 set
+// replicates the sign bit of the byte it selects (the __byte_perm intrinsic
+// keeps only 3 bits per selector).
+__device__ __forceinline__ int prmt_s(uint32_t a, uint32_t b, uint32_t sel) {
+  uint32_t d;
+  asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(sel));
+  return (int)d;
+}
+
 // Post-collision deviations of both nodes of a pair (the arithmetic of
-// mom_to_pops on FP32 pairs): each 24-bit code is its int16 high part
-// shifted into bits 8..31 with its sign, or the low byte.
+// mom_to_pops on FP32 pairs): each 24-bit code is the low byte, then the
+// int16 high part, then the high part's sign replicated, in one permute.
 __device__ __forceinline__ void mom_decode2(const StepArgs &a, const MomRaw &w, float2 d[9]) {
   float2 q[3];
 #pragma unroll
   for (int p = 0; p < 3; p++) {
-    const int q0 = ((int)(w.h[p] << 16) >> 8) | (int)(w.l[p] & 0xffu);
-    const int q1 = ((int)(w.h[p] & 0xffff0000u) >> 8) | (int)((w.l[p] >> 8) & 0xffu);
+    const int q0 = prmt_s(w.l[p], w.h[p], 0xD540u);  // l.b0, h.b0, h.b1, sign(h.b1)
+    const int q1 = prmt_s(w.l[p], w.h[p], 0xF761u);  // l.b1, h.b2, h.b3, sign(h.b3)
     q[p] = mul2(make_float2((float)q0, (float)q1), bc2(fx_step(a, p)));
   }
   float2 n[6];  // stored units (n_i * neq_s); the inverse scale enters the FMAs below
@@ -365,7 +374,7 @@ __device__ __forceinline__ void pops_to_mom2(const float2 d[9], float2 &r, float
 template <int MODEL>
 __device__ __forceinline__ void collide_mom2(float2 r, float2 jx, float2 jy, float2 m[6],
                                             const StepArgs &a) {
-  const float2 rho = add2(bc2((float)a.rho0), r);
+  const float2 rho = add2(bc2(a.f_rho0), r);
   // 1 / rho enters only the equilibria of the non-conserved moments, whose
   // stored form keeps 11 bits: the approximate reciprocal is ample
   const float2 inv = make_float2(__fdividef(1.f, rho.x), __fdividef(1.f, rho.y));
@@ -373,9 +382,9 @@ __device__ __forceinline__ void collide_mom2(float2 r, float2 jx, float2 jy, flo
   const float2 q = MODEL == 3 ? jj : mul2(jj, inv);
   const float2 e1 = fma2(bc2(3.f), q, mul2(bc2(-2.f), r)), e2 = fma2(bc2(-3.f), q, r);
   const float2 e7 = mul2(mul2(sub2(jx, jy), add2(jx, jy)), inv), e8 = mul2(mul2(jx, jy), inv);
-  const float om = (float)a.omega;
+  const float om = a.f_om;
   const float s12 = MODEL == 3 ? 1.4f : om;
-  const float s46 = MODEL == 3 ? 1.2f : (MODEL == 2 ? (float)a.omegaA : om);
+  const float s46 = MODEL == 3 ? 1.2f : (MODEL == 2 ? a.f_omA : om);
   m[0] = fma2(bc2(-s12), sub2(m[0], e1), m[0]);
   m[1] = fma2(bc2(-s12), sub2(m[1], e2), m[1]);
   m[2] = fma2(bc2(-s46), add2(m[2], jx), m[2]);
@@ -390,50 +399,46 @@ __device__ __forceinline__ void mom_encode_store2(const StepArgs &a, void *b, lo
                                                   uint32_t hseed, float2 r, float2 jx, float2 jy,
                                                   const float2 m[6], bool own0, bool own1,
                                                   bool &ok) {
-  // dithers of the pair from one hash: node 0 in bits 0..15, node 1 in
-  // 16..31, 6 bits for rho and 5 each for j (bias below 1/64 of a step)
+  // Dithered codes in integers: R = round(2^D v / step), t = (R + u) >> D
+  // with u uniform in 0 .. 2^D - 1, so that E[t] = R / 2^D, within 2^-(D+1)
+  // of v / step.  The pair's dithers come from one hash: node 0 in bits
+  // 0..15, node 1 in 16..31; D = 6 for rho, 5 for each j.  Out of range
+  // (|t| > MOM_QMAX, or R saturated by the conversion) clears `ok`; a NaN
+  // converts to 0 and is caught by the caller's probe instead.
   const uint32_t h = mix32((uint32_t)z ^ hseed);
   const float2 v[3] = {r, jx, jy};
   const int sh[3] = {0, 6, 11}, nb[3] = {6, 5, 5};
-  float2 t[3];
-  bool ok0 = true, ok1 = true;
+  int q0[3], q1[3];
+  bool bad = false;
 #pragma unroll
   for (int p = 0; p < 3; p++) {
     const uint32_t mask = (1u << nb[p]) - 1u;
-    const float sc = 1.f / (float)(1u << nb[p]);
-    const float u0 = ((float)((h >> sh[p]) & mask) + 0.5f) * sc;
-    const float u1 = ((float)((h >> (16 + sh[p])) & mask) + 0.5f) * sc;
-    const float2 x = mul2(v[p], bc2(fx_istep(a, p)));
-    const float2 xi = make_float2(floorf(x.x), floorf(x.y));
-    const float2 fr = sub2(x, xi);
-    t[p] = make_float2(xi.x + (fr.x > u0 ? 1.f : 0.f), xi.y + (fr.y > u1 ? 1.f : 0.f));
-    ok0 = ok0 && fabsf(t[p].x) <= (float)MOM_QMAX;
-    ok1 = ok1 && fabsf(t[p].y) <= (float)MOM_QMAX;
+    const float2 x = mul2(v[p], bc2(fx_istep(a, p) * (float)(1u << nb[p])));
+    const uint32_t R0 = (uint32_t)__float2int_rn(x.x), R1 = (uint32_t)__float2int_rn(x.y);
+    q0[p] = (int)(R0 + ((h >> sh[p]) & mask)) >> nb[p];
+    q1[p] = (int)(R1 + ((h >> (16 + sh[p])) & mask)) >> nb[p];
+    const bool b0 = (uint32_t)(q0[p] + MOM_QMAX) > 2u * (uint32_t)MOM_QMAX;
+    const bool b1 = (uint32_t)(q1[p] + MOM_QMAX) > 2u * (uint32_t)MOM_QMAX;
+    bad = bad || (own0 && b0) || (own1 && b1);
   }
-  if (own0) ok = ok && ok0;
-  if (own1) ok = ok && ok1;
-  // references b_i (times neq_s) of the stored conserved moments
+  ok = ok && !bad;
+  // minus the references b_i (times neq_s) of the stored conserved moments,
+  // so that each stored value is one multiply-add
   const float ns = a.neq_s;
-  const float2 sr = mul2(t[0], bc2(fx_step(a, 0))), sx = mul2(t[1], bc2(fx_step(a, 1))),
-               sy = mul2(t[2], bc2(fx_step(a, 2)));
+  const float2 sr = mul2(make_float2((float)q0[0], (float)q1[0]), bc2(fx_step(a, 0)));
+  const float2 sx = mul2(make_float2((float)q0[1], (float)q1[1]), bc2(fx_step(a, 1)));
+  const float2 sy = mul2(make_float2((float)q0[2], (float)q1[2]), bc2(fx_step(a, 2)));
   const float2 i0 = bc2(a.fx_irho0 * ns);
   const float2 jj = fma2(sx, sx, mul2(sy, sy));
-  // minus the references, so that each stored value is one multiply-add
   const float2 mref[6] = {fma2(bc2(-3.f * ns), jj, mul2(bc2(2.f * ns), sr)),
-                        fma2(bc2(3.f * ns), jj, mul2(bc2(-ns), sr)), mul2(bc2(ns), sx),
-                        mul2(bc2(ns), sy), mul2(mul2(sub2(sy, sx), add2(sx, sy)), i0),
-                        mul2(mul2(sx, sy), bc2(-a.fx_irho0 * ns))};
+                          fma2(bc2(3.f * ns), jj, mul2(bc2(-ns), sr)), mul2(bc2(ns), sx),
+                          mul2(bc2(ns), sy), mul2(mul2(sub2(sy, sx), add2(sx, sy)), i0),
+                          mul2(mul2(sx, sy), bc2(-a.fx_irho0 * ns))};
   uint32_t nw[6];
 #pragma unroll
   for (int i = 0; i < 6; i++) {
     const __half2 hh = __float22half2_rn(fma2(m[i], bc2(ns), mref[i]));
     memcpy(&nw[i], &hh, 4);
-  }
-  int q0[3], q1[3];
-#pragma unroll
-  for (int p = 0; p < 3; p++) {
-    q0[p] = (int)t[p].x;
-    q1[p] = (int)t[p].y;
   }
   if (own0 && own1) {
 #pragma unroll
@@ -483,7 +488,7 @@ struct MomWalk {
 
 // Row j of the walk (source row y0 + j); PH = (j + 1) mod 3 selects the ring
 // slots: row j decodes slot PH and loads row j + 2 into slot (PH + 2) mod 3.
-template <int MODEL, int NPT, int PH>
+template <int MODEL, int NPT, bool PF, int PH>
 __device__ __forceinline__ void mom_walk_row(const StepArgs &a, MomWalk &w, int j, int y0, int wx,
                                              int x0, int lane, bool inx, bool owner,
                                              uint32_t hseed) {
@@ -493,18 +498,18 @@ __device__ __forceinline__ void mom_walk_row(const StepArgs &a, MomWalk &w, int 
     const int r2 = r + 2;
     mom_raw_load(a, a.src, (long long)r2 * a.pitch + x0, inx && r2 < a.m, w.raw[(PH + 2) % 3]);
   }
-  if (lane < 12) {
+  if (PF && lane < 24) {
+    // one 128-byte line per lane: the warp's span of row r + MOM_PF covers at
+    // most two lines of each of the nine 16-bit planes (lanes 0..17) and of
+    // the three byte planes (lanes 18..23); every address lies in the span
     const int rp = r + MOM_PF;
     if (rp < a.m && j + MOM_PF <= NPT) {
       const long long e = (long long)rp * a.pitch + wx - 2;
+      const int pl = lane >> 1, hi = lane & 1;
       const char *base = (const char *)a.src;
-      const char *p = lane < 9 ? base + (long long)lane * 2 * a.plane + 2 * e
-                               : base + 18 * a.plane + (long long)(lane - 9) * a.plane + e;
-      const char *al = (const char *)((uintptr_t)p & ~(uintptr_t)15);
-      if (lane < 9)
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], 144;" ::"l"(al) : "memory");
-      else
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], 80;" ::"l"(al) : "memory");
+      const char *p = pl < 9 ? base + (long long)pl * 2 * a.plane + 2 * e + hi * 127
+                             : base + (long long)(9 + pl) * a.plane + e + hi * 63;
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
     }
   }
   float2 d[9];
@@ -548,7 +553,7 @@ __device__ __forceinline__ void mom_walk_row(const StepArgs &a, MomWalk &w, int 
   }
 }
 
-template <int MODEL, int NPT, int MINB>
+template <int MODEL, int NPT, int MINB, bool PF>
 __global__ void __launch_bounds__(128, MINB) k_step_mom(const __grid_constant__ StepArgs a) {
   static_assert((NPT + 2) % 3 == 0, "the row walk runs in groups of three rows");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -572,9 +577,9 @@ __global__ void __launch_bounds__(128, MINB) k_step_mom(const __grid_constant__ 
   // nothing and store nothing
 #pragma unroll 1
   for (int j = -1; j <= NPT && y0 + j - 1 < a.m; j += 3) {
-    mom_walk_row<MODEL, NPT, 0>(a, w, j, y0, wx, x0, lane, inx, owner, hseed);
-    mom_walk_row<MODEL, NPT, 1>(a, w, j + 1, y0, wx, x0, lane, inx, owner, hseed);
-    mom_walk_row<MODEL, NPT, 2>(a, w, j + 2, y0, wx, x0, lane, inx, owner, hseed);
+    mom_walk_row<MODEL, NPT, PF, 0>(a, w, j, y0, wx, x0, lane, inx, owner, hseed);
+    mom_walk_row<MODEL, NPT, PF, 1>(a, w, j + 1, y0, wx, x0, lane, inx, owner, hseed);
+    mom_walk_row<MODEL, NPT, PF, 2>(a, w, j + 2, y0, wx, x0, lane, inx, owner, hseed);
   }
   mom_flag(a, w.ok, w.probe);
 }

@@ -61,7 +61,8 @@ constexpr TileVariant VARS[NVAR] = {
 // rows per thread.
 constexpr int MOM_NVAR = 3;
 constexpr int MOM_NPT[MOM_NVAR] = {16, 34, 34};  // (NPT + 2) % 3 == 0
-constexpr int MOM_MINB[MOM_NVAR] = {5, 5, 4};    // resident blocks per SM (register cap)
+constexpr int MOM_MINB[MOM_NVAR] = {4, 4, 5};    // resident blocks per SM (register cap)
+constexpr bool MOM_PFL[MOM_NVAR] = {true, false, true};  // L2 prefetch of the rows ahead
 constexpr int TMA_MAX_SMEM = 200 * 1024;  // dynamic shared memory budget of one TMA block
 constexpr int TMA_MAX_STAGES = 4;
 
@@ -101,6 +102,7 @@ struct StepArgs {
   float fx_irho0;           // 1 / rho0
   float neq_s, neq_is;      // scale of the stored non-equilibrium moments and its inverse
   unsigned gen;             // generation written by this launch (seed of the rounding dither)
+  float f_rho0, f_om, f_omA;  // rho0, omega, omegaA in FP32 (moment storage)
 };
 
 // Outputs of the read-only finish kernel (any pointer may be null).

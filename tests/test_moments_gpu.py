@@ -49,9 +49,9 @@ def test_fp16neq_against_fp64(name):
 
 @pytest.mark.parametrize("tile", [1, 2, 3])
 def test_every_tile_against_fp64(tile):
-    """The three bulk tiles (16, 34, 34 rows per thread; 5, 5, 4 blocks per SM)
-    do the same arithmetic per node, but the compiler may fuse multiply-adds
-    differently in each; a
+    """The three bulk tiles (16, 34, 34 rows per thread; the last one without
+    L2 prefetch) do the same arithmetic per node, but the compiler may fuse
+    multiply-adds differently in each; a
     last-bit difference can move a dithered fixed-point code by one step, so
     the tiles are not bitwise equal: each meets the FP64 tolerances."""
     ref, _ = run("cavity_mrt_curved", G.FP64)

@@ -86,7 +86,8 @@ typedef struct lbm_params {
   int32_t device;            /* CUDA device ordinal */
   double rho_out;            /* outlet density for outlet_profile 4 */
   void *stream;              /* cudaStream_t to run on; NULL = a stream owned by the context */
-  int32_t tile_variant;      /* fused-step tile: 0 = default or lbm_autotune's choice, 1..6 fixed */
+  int32_t tile_variant;      /* fused-step tile: 0 = default or lbm_autotune's choice, 1..6 fixed
+                                (1..4 for LBM_FP16NEQ) */
 } lbm_params;
 
 typedef struct lbm_ctx lbm_ctx;

@@ -64,23 +64,44 @@ __global__ void __launch_bounds__(BX) k_batch_step(const BatchCase *cases, const
   }
 }
 
-// The nodes with boundary work of every case, one thread each (x: case,
-// y: linear node index), after or alongside k_batch_step in the same step.
+// One special node whose boundary record is known: the special branch of
+// step_one (the same treatment and collision) without the class, index and
+// record lookups that find it.
+template <class ST, int MODEL>
+__device__ __forceinline__ void step_special_rec(const StepArgs &a, long long node,
+                                                 const BRec &r) {
+  using R = typename ST::R;
+  constexpr bool SH = ST::SHIFT;
+  R F[9], mac[3];
+  special_node_rec<R>(a, AccMain<ST, PH_AB, SH>(a, a.src), node, r, F, mac);
+  if constexpr (SH) {
+    R M[9];
+    collide_dev<MODEL>(F, mac[0], mac[1], mac[2], a, M);
+    store_node_dev<ST, PH_AB>(a, node, (uint8_t)CLS_SPECIAL, M);
+  } else {
+    collide_store<ST, MODEL, PH_AB>(a, node, (uint8_t)CLS_SPECIAL, F, mac[0], mac[1], mac[2]);
+  }
+}
+
+// The nodes with boundary work of every case, one thread each, from a list
+// of (case, linear node index, boundary record, record flags) sorted by the
+// flags: consecutive threads take the same path through the treatment, and
+// the record comes with the entry (no class or index lookups on the node).
 // The case arguments are read through restrict pointers: they do not alias
 // the population stores, so the compiler may keep them in registers across
 // the node's stores instead of reloading them.
 template <class ST, int MODEL>
 __global__ void __launch_bounds__(128) k_batch_special(const BatchCase *__restrict__ cases,
-                                                       const int2 *__restrict__ list,
+                                                       const int4 *__restrict__ list,
                                                        const int *__restrict__ nlist_live,
                                                        const int *__restrict__ active,
                                                        const int *__restrict__ gpar) {
   const int nlist = *nlist_live;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nlist; i += gridDim.x * blockDim.x) {
-    const int2 e = list[i];
+    const int4 e = list[i];
     if (!active[e.x]) continue;
     const StepArgs &a = cases[e.x].args[gpar[e.x] & 1];
-    step_one<ST, MODEL, PH_AB>(a, (long long)e.y, (uint8_t)CLS_SPECIAL);
+    step_special_rec<ST, MODEL>(a, (long long)e.y, a.rec[e.z]);
   }
 }
 

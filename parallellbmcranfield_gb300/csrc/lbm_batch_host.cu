@@ -59,7 +59,7 @@ struct lbm_batch {
   int ntiles[lbm::BVAR] = {};
   int4 *d_rows = nullptr;
   int nrows = 0;
-  int2 *d_special = nullptr;  // (case, node) of every node with boundary work, sorted by kind
+  int4 *d_special = nullptr;  // (case, node, record, flags) of every node with boundary work, sorted by kind
   int nspecial = 0;
   int *d_nspecial = nullptr;  // nspecial on the device (the boundary-node kernel's count)
   int4 *d_live_tiles = nullptr;   // compacted work lists of the cases still stepping
@@ -287,7 +287,7 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
   b->hcases.resize(ncases);
   std::vector<std::vector<int4>> tiles(lbm::BVAR);
   std::vector<int4> rows;
-  std::vector<int2> specials;
+  std::vector<int4> specials;
   std::vector<uint32_t> special_key;
   const size_t es = (size_t)b->ks->elem_size;
   const double w[9] = {4. / 9., 1. / 9., 1. / 9., 1. / 9., 1. / 9., 1. / 36., 1. / 36., 1. / 36., 1. / 36.};
@@ -355,8 +355,9 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
     }
     for (int y = 0; y < P.m; y++)
       for (int tx = 0; tx < (P.n + 127) / 128; tx++) rows.push_back(make_int4(c, tx, y, 0));
-    for (const lbm::BRec &r : P.rec) {
-      specials.push_back(make_int2(c, (int)r.node));
+    for (size_t ri = 0; ri < P.rec.size(); ri++) {
+      const lbm::BRec &r = P.rec[ri];
+      specials.push_back(make_int4(c, (int)r.node, (int)ri, (int)r.flags));
       special_key.push_back(r.flags);
     }
   }
@@ -368,7 +369,7 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
     for (size_t i = 0; i < ord.size(); i++) ord[i] = i;
     std::stable_sort(ord.begin(), ord.end(),
                      [&](size_t x, size_t y) { return special_key[x] < special_key[y]; });
-    std::vector<int2> sorted(specials.size());
+    std::vector<int4> sorted(specials.size());
     for (size_t i = 0; i < ord.size(); i++) sorted[i] = specials[ord[i]];
     specials.swap(sorted);
   }
@@ -414,7 +415,7 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
   if ((st = balloc(b, &b->d_nspecial, 1)) != LBM_OK) return bail(st);
   cudaMemcpy(b->d_nspecial, &b->nspecial, sizeof(int), cudaMemcpyHostToDevice);
   if (!specials.empty())
-    cudaMemcpy(b->d_special, specials.data(), specials.size() * sizeof(int2), cudaMemcpyHostToDevice);
+    cudaMemcpy(b->d_special, specials.data(), specials.size() * sizeof(int4), cudaMemcpyHostToDevice);
   b->nrows = (int)rows.size();
   if ((st = balloc(b, &b->d_rows, rows.size())) != LBM_OK) return bail(st);
   cudaMemcpy(b->d_rows, rows.data(), rows.size() * sizeof(int4), cudaMemcpyHostToDevice);

@@ -590,6 +590,11 @@ __device__ __noinline__ void boundary_F_noout(const StepArgs &a, const ACC &acc,
   boundary_F<false, R, ACC>(a, acc, node, F);
 }
 
+// The treatment of a special node whose boundary record is `r`.
+template <bool OUTLET, class R, class ACC>
+__device__ __forceinline__ void boundary_F_rec(const StepArgs &a, const ACC &acc, long long node,
+                                               const BRec &r, R F[9]);
+
 template <bool OUTLET, class R, class ACC>
 __device__ void boundary_F(const StepArgs &a, const ACC &acc, long long node, R F[9]) {
   constexpr bool DEV = ACC::dev;
@@ -605,7 +610,14 @@ __device__ void boundary_F(const StepArgs &a, const ACC &acc, long long node, R 
     for (int k = 0; k < 9; k++) F[k] = acc.meta(node - nb(k, a.pitch), k);
     return;
   }
-  const BRec &r = a.rec[a.aux[node]];
+  boundary_F_rec<OUTLET, R, ACC>(a, acc, node, a.rec[a.aux[node]], F);
+}
+
+template <bool OUTLET, class R, class ACC>
+__device__ __forceinline__ void boundary_F_rec(const StepArgs &a, const ACC &acc, long long node,
+                                               const BRec &r, R F[9]) {
+  constexpr bool DEV = ACC::dev;
+  const R rho0 = DEV ? (R)a.rho0 : R(0);
   const uint32_t fl = r.flags;
   // StreamingStep, serial/Iterate.c:478-484 (F = own METAF where not streamed)
 #pragma unroll
@@ -688,9 +700,9 @@ __device__ void boundary_F(const StepArgs &a, const ACC &acc, long long node, R 
 // macroscopic fields (V = 0 on east-outlet cells,
 // serial/CellFunctions.c:483-486).
 template <class R, class ACC>
-__device__ __noinline__ void special_node(const StepArgs &a, const ACC &acc, long long node,
-                                          R F[9], R *mac) {
-  boundary_F<true, R, ACC>(a, acc, node, F);
+__device__ __forceinline__ void special_node_rec(const StepArgs &a, const ACC &acc, long long node,
+                                                 const BRec &r, R F[9], R *mac) {
+  boundary_F_rec<true, R, ACC>(a, acc, node, r, F);
   R rho, u, v;
   if constexpr (ACC::dev) {
     R rt = ((F[0] + F[1]) + (F[2] + F[3])) + ((F[4] + F[5]) + (F[6] + F[7])) + F[8];
@@ -703,10 +715,16 @@ __device__ __noinline__ void special_node(const StepArgs &a, const ACC &acc, lon
   } else {
     moments<R>(F, rho, u, v);
   }
-  if (a.rec[a.aux[node]].flags & FL_EAST) v = R(0.0);
+  if (r.flags & FL_EAST) v = R(0.0);
   mac[0] = rho;
   mac[1] = u;
   mac[2] = v;
+}
+
+template <class R, class ACC>
+__device__ __noinline__ void special_node(const StepArgs &a, const ACC &acc, long long node,
+                                          R F[9], R *mac) {
+  special_node_rec<R, ACC>(a, acc, node, a.rec[a.aux[node]], F, mac);
 }
 
 // Collision of deviations d = F - w rho0 with given rho, u, v (the special

@@ -55,7 +55,7 @@ struct KernelSet {
 };
 // Launch table of the moment storage (LBM_FP16NEQ, lbm_mom_inst.cu).
 struct MomKernels {
-  const void *step[4][3];  // [model 1..3][tile variant: MOM_NPT rows per thread]
+  const void *step[4][MOM_NVAR];  // [model 1..3][tile variant: MOM_NPT rows per thread]
   const void *special[4];  // [model] class-3 / class-2 nodes from the compact list
   const void *init[4];     // [model]
   const void *finish;

@@ -59,10 +59,10 @@ constexpr TileVariant VARS[NVAR] = {
     {2, 0, 0, 0, 128, 4, 2},   {3, 128, 2, 2, 0, 0, 0},  {3, 128, 2, 4, 0, 0, 0}};
 // Bulk-step tiles of the moment storage: blocks of 4 warps x 60 columns, these
 // rows per thread.
-constexpr int MOM_NVAR = 3;
-constexpr int MOM_NPT[MOM_NVAR] = {16, 34, 34};  // (NPT + 2) % 3 == 0
-constexpr int MOM_MINB[MOM_NVAR] = {4, 4, 5};    // resident blocks per SM (register cap)
-constexpr bool MOM_PFL[MOM_NVAR] = {true, false, true};  // L2 prefetch of the rows ahead
+constexpr int MOM_NVAR = 4;
+constexpr int MOM_NPT[MOM_NVAR] = {16, 34, 34, 34};  // (NPT + 2) % 3 == 0
+constexpr int MOM_MINB[MOM_NVAR] = {4, 4, 4, 3};     // resident blocks per SM (register cap)
+constexpr bool MOM_PFL[MOM_NVAR] = {true, false, true, true};  // L2 prefetch of the rows ahead
 constexpr int TMA_MAX_SMEM = 200 * 1024;  // dynamic shared memory budget of one TMA block
 constexpr int TMA_MAX_STAGES = 4;
 

@@ -118,10 +118,21 @@ struct BulkArgs {
 };
 static_assert(sizeof(BulkArgs) == 128, "BulkArgs layout");
 
-// Bulk nodes (class 1) of one column of NPT rows; every other class is left
-// to the boundary-node pass.  The loads of all NPT nodes go out first.
+// A special node met by the per-tile bulk pass, out of line so that its
+// registers stay out of the bulk path's allocation: the full case arguments
+// (records, boundary kinds) are read from global memory.  The sectors of its
+// populations were just loaded by the neighbouring lanes of the same warp.
+template <class ST, int MODEL>
+__device__ __noinline__ void batch_special_cold(const StepArgs &a, long long node) {
+  step_special_rec<ST, MODEL>(a, node, a.rec[a.aux[node]]);
+}
+
+// One column of NPT rows: bulk nodes (class 1) with all their loads issued
+// first, then the special nodes of the column (class 3) through
+// batch_special_cold with the case's full arguments `full`.
 template <class ST, int MODEL, int NPT>
-__device__ __forceinline__ void bulk_column(const StepArgs &a, int x, int y0) {
+__device__ __forceinline__ void bulk_column(const StepArgs &a, int x, int y0,
+                                            const StepArgs *full) {
   using R = typename ST::R;
   using T = typename ST::T;
   if (x >= a.n) return;
@@ -142,24 +153,31 @@ __device__ __forceinline__ void bulk_column(const StepArgs &a, int x, int y0) {
   for (int j = 0; j < NPT; j++)
     if (c[j] == CLS_BULK)
       bulk_store<ST, MODEL, PH_AB>(a, (long long)(y0 + j) * a.pitch + x, c[j], F[j]);
+#pragma unroll
+  for (int j = 0; j < NPT; j++)
+    if (c[j] == CLS_SPECIAL) batch_special_cold<ST, MODEL>(*full, (long long)(y0 + j) * a.pitch + x);
 }
 
-// Batched bulk pass with one block per live (case, tile): no persistent loop
-// and no shared-memory copy of the case arguments, so a block's loads go out
-// as soon as it starts and the hardware keeps every SM filled with blocks.
-// Blocks past the live count (the grid is sized for all tiles when the
-// graph is captured) return at once.
+// Batched step with one block per live (case, tile): no persistent loop and
+// no shared-memory copy of the case arguments, so a block's loads go out as
+// soon as it starts and the hardware keeps every SM filled with blocks.  The
+// tiles cover every node, the special ones included (a separate pass over a
+// node list paid a warp's latency chain and a whole sector per population
+// for each node of a vertical wall).  Blocks past the live count (the grid
+// is sized for all tiles when the graph is captured) return at once.
 template <class ST, int MODEL, int BX, int NPT>
 __global__ void __launch_bounds__(BX) k_batch_bulk(const BulkArgs *__restrict__ args,
                                                    const int4 *__restrict__ tiles,
                                                    const int *__restrict__ ntiles_live,
                                                    const int *__restrict__ active,
-                                                   const int *__restrict__ gpar) {
+                                                   const int *__restrict__ gpar,
+                                                   const BatchCase *__restrict__ cases) {
   const int t = blockIdx.x;
   if (t >= __ldg(ntiles_live)) return;
   const int4 tl = __ldg(&tiles[t]);
   if (!__ldg(&active[tl.x])) return;
-  const BulkArgs &b = args[2 * tl.x + (__ldg(&gpar[tl.x]) & 1)];
+  const int par = __ldg(&gpar[tl.x]) & 1;
+  const BulkArgs &b = args[2 * tl.x + par];
   StepArgs a;
   a.src = const_cast<void *>(b.src);
   a.dst = b.dst;
@@ -179,7 +197,7 @@ __global__ void __launch_bounds__(BX) k_batch_bulk(const BulkArgs *__restrict__ 
       a.inv_scale[k] = b.inv_scale[k];
     }
   }
-  bulk_column<ST, MODEL, NPT>(a, tl.y * BX + threadIdx.x, tl.z * NPT);
+  bulk_column<ST, MODEL, NPT>(a, tl.y * BX + threadIdx.x, tl.z * NPT, &cases[tl.x].args[par]);
 }
 
 // After a step: active cases advance their parity and counters.

@@ -183,14 +183,16 @@ lbm_status launch_steps(lbm_batch *b, int k) {
     // the boundary-node pass writes other nodes than the bulk pass and both
     // only read the source state, so it runs on a second stream alongside
     // (fork and join by events: two parallel branches when captured)
-    if (b->nspecial > 0) {
+    // (the per-tile kernels update the special nodes of their tiles themselves)
+    const bool side = b->nspecial > 0 && !b->bk->per_tile;
+    if (side) {
       LBM_BCK(cudaEventRecord(b->ev_fork, b->stream));
       LBM_BCK(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
     }
-    void *args[] = {&step_args0, &b->d_live_tiles, &cnt_t, &b->s.active, &b->s.gpar};
+    void *args[] = {&step_args0, &b->d_live_tiles, &cnt_t, &b->s.active, &b->s.gpar, &b->d_cases};
     cudaError_t e = cudaLaunchKernel(fn, dim3(grid), dim3(bx), args, 0, b->stream);
     if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
-    if (b->nspecial > 0) {
+    if (side) {
       void *sargs[] = {&b->d_cases, &b->d_special, &b->d_nspecial, &b->s.active, &b->s.gpar};
       const int sg = std::min((b->nspecial + 127) / 128, 152 * 16);
       e = cudaLaunchKernel(b->bk->special[b->model], dim3(sg), dim3(128), sargs, 0, b->side);

@@ -67,13 +67,14 @@ __global__ void __launch_bounds__(BX) k_batch_step(const BatchCase *cases, const
 // One special node whose boundary record is known: the special branch of
 // step_one (the same treatment and collision) without the class, index and
 // record lookups that find it.
-template <class ST, int MODEL>
+template <class ST, int MODEL, bool EXTRAP = true>
 __device__ __forceinline__ void step_special_rec(const StepArgs &a, long long node,
                                                  const BRec &r) {
   using R = typename ST::R;
   constexpr bool SH = ST::SHIFT;
   R F[9], mac[3];
-  special_node_rec<R>(a, AccMain<ST, PH_AB, SH>(a, a.src), node, r, F, mac);
+  special_node_rec<R, AccMain<ST, PH_AB, SH>, EXTRAP>(a, AccMain<ST, PH_AB, SH>(a, a.src), node, r,
+                                                      F, mac);
   if constexpr (SH) {
     R M[9];
     collide_dev<MODEL>(F, mac[0], mac[1], mac[2], a, M);
@@ -118,21 +119,10 @@ struct BulkArgs {
 };
 static_assert(sizeof(BulkArgs) == 128, "BulkArgs layout");
 
-// A special node met by the per-tile bulk pass, out of line so that its
-// registers stay out of the bulk path's allocation: the full case arguments
-// (records, boundary kinds) are read from global memory.  The sectors of its
-// populations were just loaded by the neighbouring lanes of the same warp.
-template <class ST, int MODEL>
-__device__ __noinline__ void batch_special_cold(const StepArgs &a, long long node) {
-  step_special_rec<ST, MODEL>(a, node, a.rec[a.aux[node]]);
-}
-
-// One column of NPT rows: bulk nodes (class 1) with all their loads issued
-// first, then the special nodes of the column (class 3) through
-// batch_special_cold with the case's full arguments `full`.
+// Bulk nodes (class 1) of one column of NPT rows; every other class is left
+// to the boundary-node pass.  The loads of all NPT nodes go out first.
 template <class ST, int MODEL, int NPT>
-__device__ __forceinline__ void bulk_column(const StepArgs &a, int x, int y0,
-                                            const StepArgs *full) {
+__device__ __forceinline__ void bulk_column(const StepArgs &a, int x, int y0) {
   using R = typename ST::R;
   using T = typename ST::T;
   if (x >= a.n) return;
@@ -153,31 +143,24 @@ __device__ __forceinline__ void bulk_column(const StepArgs &a, int x, int y0,
   for (int j = 0; j < NPT; j++)
     if (c[j] == CLS_BULK)
       bulk_store<ST, MODEL, PH_AB>(a, (long long)(y0 + j) * a.pitch + x, c[j], F[j]);
-#pragma unroll
-  for (int j = 0; j < NPT; j++)
-    if (c[j] == CLS_SPECIAL) batch_special_cold<ST, MODEL>(*full, (long long)(y0 + j) * a.pitch + x);
 }
 
-// Batched step with one block per live (case, tile): no persistent loop and
-// no shared-memory copy of the case arguments, so a block's loads go out as
-// soon as it starts and the hardware keeps every SM filled with blocks.  The
-// tiles cover every node, the special ones included (a separate pass over a
-// node list paid a warp's latency chain and a whole sector per population
-// for each node of a vertical wall).  Blocks past the live count (the grid
-// is sized for all tiles when the graph is captured) return at once.
+// Batched bulk pass with one block per live (case, tile): no persistent loop
+// and no shared-memory copy of the case arguments, so a block's loads go out
+// as soon as it starts and the hardware keeps every SM filled with blocks.
+// Blocks past the live count (the grid is sized for all tiles when the
+// graph is captured) return at once.
 template <class ST, int MODEL, int BX, int NPT>
 __global__ void __launch_bounds__(BX) k_batch_bulk(const BulkArgs *__restrict__ args,
                                                    const int4 *__restrict__ tiles,
                                                    const int *__restrict__ ntiles_live,
                                                    const int *__restrict__ active,
-                                                   const int *__restrict__ gpar,
-                                                   const BatchCase *__restrict__ cases) {
+                                                   const int *__restrict__ gpar) {
   const int t = blockIdx.x;
   if (t >= __ldg(ntiles_live)) return;
   const int4 tl = __ldg(&tiles[t]);
   if (!__ldg(&active[tl.x])) return;
-  const int par = __ldg(&gpar[tl.x]) & 1;
-  const BulkArgs &b = args[2 * tl.x + par];
+  const BulkArgs &b = args[2 * tl.x + (__ldg(&gpar[tl.x]) & 1)];
   StepArgs a;
   a.src = const_cast<void *>(b.src);
   a.dst = b.dst;
@@ -197,7 +180,77 @@ __global__ void __launch_bounds__(BX) k_batch_bulk(const BulkArgs *__restrict__ 
       a.inv_scale[k] = b.inv_scale[k];
     }
   }
-  bulk_column<ST, MODEL, NPT>(a, tl.y * BX + threadIdx.x, tl.z * NPT, &cases[tl.x].args[par]);
+  bulk_column<ST, MODEL, NPT>(a, tl.y * BX + threadIdx.x, tl.z * NPT);
+}
+
+// Per-case fields the boundary-node pass needs beyond BulkArgs.
+struct SpecExtra {
+  const BRec *rec;
+  const uint32_t *aux;
+  int *nanflag;
+  int curved, outlet;
+  double rho_out;
+};
+
+// A node of an extrapolating outlet: the full treatment with the case's
+// arguments in global memory (it treats the two nodes upstream as well).
+template <class ST, int MODEL>
+__device__ __noinline__ void batch_special_full(const StepArgs &a, long long node, int rec) {
+  step_special_rec<ST, MODEL>(a, node, a.rec[rec]);
+}
+
+// Boundary-node pass of the per-tile batches (FP32, FP16-dev): one thread per
+// entry of the (case, node, record, flags) list.  The case arguments are
+// assembled in registers from the 128-byte BulkArgs of the case's parity and
+// its SpecExtra, both read once, so the chain of dependent loads per node is
+// entry -> (parity, arguments, record) -> populations, and no argument is
+// reloaded after the node's stores.  Nodes of an extrapolating outlet take
+// the full path with the arguments in global memory.
+template <class ST, int MODEL>
+__global__ void __launch_bounds__(128) k_batch_special_c(const BulkArgs *__restrict__ args,
+                                                         const SpecExtra *__restrict__ extra,
+                                                         const BatchCase *__restrict__ cases,
+                                                         const int4 *__restrict__ list,
+                                                         const int *__restrict__ nlist_live,
+                                                         const int *__restrict__ active,
+                                                         const int *__restrict__ gpar) {
+  const int nlist = __ldg(nlist_live);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nlist) return;
+  const int4 e = __ldg(&list[i]);
+  if (!__ldg(&active[e.x])) return;
+  const int par = __ldg(&gpar[e.x]) & 1;
+  const SpecExtra &x = extra[e.x];
+  if (x.outlet == 2 && ((uint32_t)e.w & FL_EAST)) {
+    batch_special_full<ST, MODEL>(cases[e.x].args[par], (long long)e.y, e.z);
+    return;
+  }
+  const BulkArgs &b = args[2 * e.x + par];
+  StepArgs a;
+  a.src = const_cast<void *>(b.src);
+  a.dst = b.dst;
+  a.cls = b.cls;
+  a.plane = b.plane;
+  a.pitch = b.pitch;
+  a.n = b.n;
+  a.m = b.m;
+  a.omega = b.omega;
+  a.omegaA = b.omegaA;
+  a.rho0 = b.rho0;
+  a.rec = x.rec;
+  a.aux = x.aux;
+  a.nanflag = x.nanflag;
+  a.curved = x.curved;
+  a.outlet = x.outlet;
+  a.rho_out = x.rho_out;
+  if constexpr (sizeof(typename ST::T) == 2) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      a.scale[k] = b.scale[k];
+      a.inv_scale[k] = b.inv_scale[k];
+    }
+  }
+  step_special_rec<ST, MODEL, false>(a, (long long)e.y, x.rec[e.z]);
 }
 
 // After a step: active cases advance their parity and counters.
@@ -290,7 +343,8 @@ struct BatchKernels {
   const void *step[4][BVAR];  // [model 1..3][tile shape]
   int per_tile;               // 1: step kernels take BulkArgs and one block per tile
                               // (k_batch_bulk); 0: BatchCase and a persistent grid
-  const void *special[4];     // [model 1..3]
+  const void *special[4];     // [model 1..3]: k_batch_special (persistent kinds) or
+                              // k_batch_special_c (per-tile kinds)
   const void *du;
   const void *advance;
   const void *converge;

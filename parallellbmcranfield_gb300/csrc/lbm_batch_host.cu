@@ -54,6 +54,7 @@ struct lbm_batch {
   std::vector<lbm::BatchCase> hcases;
   lbm::BatchCase *d_cases = nullptr;
   lbm::BulkArgs *d_bulk = nullptr;  // per case and parity: the bulk pass's arguments
+  lbm::SpecExtra *d_extra = nullptr;  // per case: the rest of the boundary-node pass's arguments
   lbm::BatchState s{};
   int4 *d_tiles[lbm::BVAR] = {};
   int ntiles[lbm::BVAR] = {};
@@ -102,6 +103,16 @@ void bfree(lbm_batch *b) {
   if (b->ev_join) cudaEventDestroy(b->ev_join);
   if (b->side) cudaStreamDestroy(b->side);
   if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+// The boundary-node pass's stream, at the highest priority the device
+// offers: its blocks are latency-bound and few, so the block scheduler should
+// place them as soon as a slot frees instead of after the bulk pass's
+// remaining blocks (graphs keep the priority: see ensure_graph).
+bool create_side_stream(cudaStream_t *s) {
+  int lo = 0, hi = 0;
+  if (cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess) return false;
+  return cudaStreamCreateWithPriority(s, cudaStreamNonBlocking, hi) == cudaSuccess;
 }
 
 int persistent_blocks(const void *fn, int threads, int device) {
@@ -183,19 +194,22 @@ lbm_status launch_steps(lbm_batch *b, int k) {
     // the boundary-node pass writes other nodes than the bulk pass and both
     // only read the source state, so it runs on a second stream alongside
     // (fork and join by events: two parallel branches when captured)
-    // (the per-tile kernels update the special nodes of their tiles themselves)
-    const bool side = b->nspecial > 0 && !b->bk->per_tile;
-    if (side) {
+    if (b->nspecial > 0) {
       LBM_BCK(cudaEventRecord(b->ev_fork, b->stream));
       LBM_BCK(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
     }
-    void *args[] = {&step_args0, &b->d_live_tiles, &cnt_t, &b->s.active, &b->s.gpar, &b->d_cases};
+    void *args[] = {&step_args0, &b->d_live_tiles, &cnt_t, &b->s.active, &b->s.gpar};
     cudaError_t e = cudaLaunchKernel(fn, dim3(grid), dim3(bx), args, 0, b->stream);
     if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
-    if (side) {
+    if (b->nspecial > 0) {
       void *sargs[] = {&b->d_cases, &b->d_special, &b->d_nspecial, &b->s.active, &b->s.gpar};
-      const int sg = std::min((b->nspecial + 127) / 128, 152 * 16);
-      e = cudaLaunchKernel(b->bk->special[b->model], dim3(sg), dim3(128), sargs, 0, b->side);
+      void *cargs[] = {&b->d_bulk,     &b->d_extra,    &b->d_cases, &b->d_special,
+                       &b->d_nspecial, &b->s.active, &b->s.gpar};
+      // k_batch_special_c: one thread per entry; k_batch_special: grid-stride
+      const int sg = b->bk->per_tile ? (b->nspecial + 127) / 128
+                                     : std::min((b->nspecial + 127) / 128, 152 * 16);
+      e = cudaLaunchKernel(b->bk->special[b->model], dim3(sg), dim3(128),
+                           b->bk->per_tile ? cargs : sargs, 0, b->side);
       if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch special: ") + cudaGetErrorString(e));
       LBM_BCK(cudaEventRecord(b->ev_join, b->side));
       LBM_BCK(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
@@ -234,7 +248,7 @@ lbm_status ensure_graph(lbm_batch *b, int k, double tol) {
   cudaError_t e = cudaStreamEndCapture(b->stream, &g);
   if (s != LBM_OK) return s;
   if (e != cudaSuccess) return fail(LBM_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-  e = cudaGraphInstantiate(&b->graph, g, 0);
+  e = cudaGraphInstantiate(&b->graph, g, cudaGraphInstantiateFlagUseNodePriority);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(LBM_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
   b->graph_k = k;
@@ -278,7 +292,7 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
   }
   if (cudaSetDevice(p0.device) != cudaSuccess) return bail(fail(LBM_CUDA, "cudaSetDevice failed"));
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+      !create_side_stream(&b->side) ||
       cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess)
     return bail(fail(LBM_CUDA, "cudaStreamCreate failed"));
@@ -401,6 +415,20 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
       }
     if ((st = balloc(b, &b->d_bulk, bulk.size())) != LBM_OK) return bail(st);
     cudaMemcpy(b->d_bulk, bulk.data(), bulk.size() * sizeof(lbm::BulkArgs), cudaMemcpyHostToDevice);
+    std::vector<lbm::SpecExtra> extra((size_t)ncases);
+    for (int c = 0; c < ncases; c++) {
+      const lbm::StepArgs &a = b->hcases[c].args[0];
+      lbm::SpecExtra &x = extra[c];
+      std::memset(&x, 0, sizeof x);
+      x.rec = a.rec;
+      x.aux = a.aux;
+      x.nanflag = a.nanflag;
+      x.curved = a.curved;
+      x.outlet = a.outlet;
+      x.rho_out = a.rho_out;
+    }
+    if ((st = balloc(b, &b->d_extra, extra.size())) != LBM_OK) return bail(st);
+    cudaMemcpy(b->d_extra, extra.data(), extra.size() * sizeof(lbm::SpecExtra), cudaMemcpyHostToDevice);
   }
   for (int v = 0; v < lbm::BVAR; v++) {
     b->ntiles[v] = (int)tiles[v].size();

@@ -590,8 +590,11 @@ __device__ __noinline__ void boundary_F_noout(const StepArgs &a, const ACC &acc,
   boundary_F<false, R, ACC>(a, acc, node, F);
 }
 
-// The treatment of a special node whose boundary record is `r`.
-template <bool OUTLET, class R, class ACC>
+// The treatment of a special node whose boundary record is `r`.  Without
+// EXTRAP the extrapolating outlet (outlet 2, which treats the two nodes
+// upstream through an out-of-line call) is left out, so that `a` need not
+// live in memory; the caller routes those nodes elsewhere.
+template <bool OUTLET, class R, class ACC, bool EXTRAP = true>
 __device__ __forceinline__ void boundary_F_rec(const StepArgs &a, const ACC &acc, long long node,
                                                const BRec &r, R F[9]);
 
@@ -613,7 +616,7 @@ __device__ void boundary_F(const StepArgs &a, const ACC &acc, long long node, R 
   boundary_F_rec<OUTLET, R, ACC>(a, acc, node, a.rec[a.aux[node]], F);
 }
 
-template <bool OUTLET, class R, class ACC>
+template <bool OUTLET, class R, class ACC, bool EXTRAP>
 __device__ __forceinline__ void boundary_F_rec(const StepArgs &a, const ACC &acc, long long node,
                                                const BRec &r, R F[9]) {
   constexpr bool DEV = ACC::dev;
@@ -674,12 +677,14 @@ __device__ __forceinline__ void boundary_F_rec(const StepArgs &a, const ACC &acc
     } else if (a.outlet == 2) {
       // 2nd-order extrapolation from the already treated i-1, i-2 cells,
       // serial/Iterate.c:535-541
-      R A[9], B[9];
-      boundary_F_noout<R, ACC>(a, acc, node - 1, A);
-      boundary_F_noout<R, ACC>(a, acc, node - 2, B);
-      F[1] = R(2) * (A[1]) - B[1];
-      F[5] = R(2) * (A[5]) - B[5];
-      F[8] = R(2) * (A[8]) - B[8];
+      if constexpr (EXTRAP) {
+        R A[9], B[9];
+        boundary_F_noout<R, ACC>(a, acc, node - 1, A);
+        boundary_F_noout<R, ACC>(a, acc, node - 2, B);
+        F[1] = R(2) * (A[1]) - B[1];
+        F[5] = R(2) * (A[5]) - B[5];
+        F[8] = R(2) * (A[8]) - B[8];
+      }
     } else if (a.outlet == 4) {
       // constant-pressure east outlet (Zou-He density condition; not in the reference)
       const R ro = (R)a.rho_out;
@@ -699,10 +704,10 @@ __device__ __forceinline__ void boundary_F_rec(const StepArgs &a, const ACC &acc
 // path's register budget small).  Returns F (in the accessor's form) and the
 // macroscopic fields (V = 0 on east-outlet cells,
 // serial/CellFunctions.c:483-486).
-template <class R, class ACC>
+template <class R, class ACC, bool EXTRAP = true>
 __device__ __forceinline__ void special_node_rec(const StepArgs &a, const ACC &acc, long long node,
                                                  const BRec &r, R F[9], R *mac) {
-  boundary_F_rec<true, R, ACC>(a, acc, node, r, F);
+  boundary_F_rec<true, R, ACC, EXTRAP>(a, acc, node, r, F);
   R rho, u, v;
   if constexpr (ACC::dev) {
     R rt = ((F[0] + F[1]) + (F[2] + F[3])) + ((F[4] + F[5]) + (F[6] + F[7])) + F[8];

@@ -145,44 +145,6 @@ __device__ __forceinline__ void bulk_column(const StepArgs &a, int x, int y0) {
       bulk_store<ST, MODEL, PH_AB>(a, (long long)(y0 + j) * a.pitch + x, c[j], F[j]);
 }
 
-// Batched bulk pass with one block per live (case, tile): no persistent loop
-// and no shared-memory copy of the case arguments, so a block's loads go out
-// as soon as it starts and the hardware keeps every SM filled with blocks.
-// Blocks past the live count (the grid is sized for all tiles when the
-// graph is captured) return at once.
-template <class ST, int MODEL, int BX, int NPT>
-__global__ void __launch_bounds__(BX) k_batch_bulk(const BulkArgs *__restrict__ args,
-                                                   const int4 *__restrict__ tiles,
-                                                   const int *__restrict__ ntiles_live,
-                                                   const int *__restrict__ active,
-                                                   const int *__restrict__ gpar) {
-  const int t = blockIdx.x;
-  if (t >= __ldg(ntiles_live)) return;
-  const int4 tl = __ldg(&tiles[t]);
-  if (!__ldg(&active[tl.x])) return;
-  const BulkArgs &b = args[2 * tl.x + (__ldg(&gpar[tl.x]) & 1)];
-  StepArgs a;
-  a.src = const_cast<void *>(b.src);
-  a.dst = b.dst;
-  a.cls = b.cls;
-  a.plane = b.plane;
-  a.pitch = b.pitch;
-  a.n = b.n;
-  a.m = b.m;
-  a.omega = b.omega;
-  a.omegaA = b.omegaA;
-  a.rho0 = b.rho0;
-  a.nanflag = nullptr;
-  if constexpr (sizeof(typename ST::T) == 2) {
-#pragma unroll
-    for (int k = 0; k < 9; k++) {
-      a.scale[k] = b.scale[k];
-      a.inv_scale[k] = b.inv_scale[k];
-    }
-  }
-  bulk_column<ST, MODEL, NPT>(a, tl.y * BX + threadIdx.x, tl.z * NPT);
-}
-
 // Per-case fields the boundary-node pass needs beyond BulkArgs.
 struct SpecExtra {
   const BRec *rec;
@@ -199,34 +161,9 @@ __device__ __noinline__ void batch_special_full(const StepArgs &a, long long nod
   step_special_rec<ST, MODEL>(a, node, a.rec[rec]);
 }
 
-// Boundary-node pass of the per-tile batches (FP32, FP16-dev): one thread per
-// entry of the (case, node, record, flags) list.  The case arguments are
-// assembled in registers from the 128-byte BulkArgs of the case's parity and
-// its SpecExtra, both read once, so the chain of dependent loads per node is
-// entry -> (parity, arguments, record) -> populations, and no argument is
-// reloaded after the node's stores.  Nodes of an extrapolating outlet take
-// the full path with the arguments in global memory.
-template <class ST, int MODEL>
-__global__ void __launch_bounds__(128) k_batch_special_c(const BulkArgs *__restrict__ args,
-                                                         const SpecExtra *__restrict__ extra,
-                                                         const BatchCase *__restrict__ cases,
-                                                         const int4 *__restrict__ list,
-                                                         const int *__restrict__ nlist_live,
-                                                         const int *__restrict__ active,
-                                                         const int *__restrict__ gpar) {
-  const int nlist = __ldg(nlist_live);
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nlist) return;
-  const int4 e = __ldg(&list[i]);
-  if (!__ldg(&active[e.x])) return;
-  const int par = __ldg(&gpar[e.x]) & 1;
-  const SpecExtra &x = extra[e.x];
-  if (x.outlet == 2 && ((uint32_t)e.w & FL_EAST)) {
-    batch_special_full<ST, MODEL>(cases[e.x].args[par], (long long)e.y, e.z);
-    return;
-  }
-  const BulkArgs &b = args[2 * e.x + par];
-  StepArgs a;
+// A case's arguments for the boundary treatment, in registers: the 128-byte
+// BulkArgs of its parity and its SpecExtra.
+__device__ __forceinline__ void spec_args(const BulkArgs &b, const SpecExtra &x, StepArgs &a) {
   a.src = const_cast<void *>(b.src);
   a.dst = b.dst;
   a.cls = b.cls;
@@ -243,14 +180,76 @@ __global__ void __launch_bounds__(128) k_batch_special_c(const BulkArgs *__restr
   a.curved = x.curved;
   a.outlet = x.outlet;
   a.rho_out = x.rho_out;
-  if constexpr (sizeof(typename ST::T) == 2) {
 #pragma unroll
-    for (int k = 0; k < 9; k++) {
-      a.scale[k] = b.scale[k];
-      a.inv_scale[k] = b.inv_scale[k];
-    }
+  for (int k = 0; k < 9; k++) {
+    a.scale[k] = b.scale[k];
+    a.inv_scale[k] = b.inv_scale[k];
   }
-  step_special_rec<ST, MODEL, false>(a, (long long)e.y, x.rec[e.z]);
+}
+
+// Batched step with one block per live (case, tile): no persistent loop and
+// no shared-memory copy of the case arguments, so a block's loads go out as
+// soon as it starts and the hardware keeps every SM filled with blocks.
+// Warps 0 .. BX/32-1 update the tile's bulk nodes; the extra warp updates
+// its special nodes (the tile's entries of a tile-ordered list of (case,
+// node, record, flags), sorted by flags within the tile) at the same time.
+// The special warp's chain of dependent loads overlaps the bulk warps'
+// streaming instead of stalling a warp of them, and the sectors it reads at
+// a wall are the ones the bulk warps read for their pulls from the wall.
+// Tile entry: (case, tx | special count << 16, row block, first special).
+// Registers are capped at 72 per thread (the special warp's treatment would
+// take more and cost the bulk warps occupancy).  Blocks past the live count (the grid is sized for all tiles when the
+// graph is captured) return at once.
+template <class ST, int MODEL, int BX, int NPT>
+__global__ void __launch_bounds__(BX + 32, 65536 / (72 * (BX + 32))) k_batch_bulk(const BulkArgs *__restrict__ args,
+                                                        const int4 *__restrict__ tiles,
+                                                        const int *__restrict__ ntiles_live,
+                                                        const int *__restrict__ active,
+                                                        const int *__restrict__ gpar,
+                                                        const SpecExtra *__restrict__ extra,
+                                                        const int4 *__restrict__ tspec,
+                                                        const BatchCase *__restrict__ cases) {
+  const int t = blockIdx.x;
+  if (t >= __ldg(ntiles_live)) return;
+  const int4 tl = __ldg(&tiles[t]);
+  if (!__ldg(&active[tl.x])) return;
+  const int par = __ldg(&gpar[tl.x]) & 1;
+  const BulkArgs &b = args[2 * tl.x + par];
+  const int tx = tl.y & 0xffff, nspec = (int)((unsigned)tl.y >> 16);
+  if (threadIdx.x < BX) {
+    StepArgs a;
+    a.src = const_cast<void *>(b.src);
+    a.dst = b.dst;
+    a.cls = b.cls;
+    a.plane = b.plane;
+    a.pitch = b.pitch;
+    a.n = b.n;
+    a.m = b.m;
+    a.omega = b.omega;
+    a.omegaA = b.omegaA;
+    a.rho0 = b.rho0;
+    a.nanflag = nullptr;
+    if constexpr (sizeof(typename ST::T) == 2) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) {
+        a.scale[k] = b.scale[k];
+        a.inv_scale[k] = b.inv_scale[k];
+      }
+    }
+    bulk_column<ST, MODEL, NPT>(a, tx * BX + threadIdx.x, tl.z * NPT);
+    return;
+  }
+  if (nspec == 0) return;
+  const SpecExtra &x = extra[tl.x];
+  StepArgs a;
+  spec_args(b, x, a);
+  for (int i = threadIdx.x - BX; i < nspec; i += 32) {
+    const int4 e = __ldg(&tspec[tl.w + i]);
+    if (x.outlet == 2 && ((uint32_t)e.w & FL_EAST))
+      batch_special_full<ST, MODEL>(cases[tl.x].args[par], (long long)e.y, e.z);
+    else
+      step_special_rec<ST, MODEL, false>(a, (long long)e.y, x.rec[e.z]);
+  }
 }
 
 // After a step: active cases advance their parity and counters.
@@ -343,8 +342,8 @@ struct BatchKernels {
   const void *step[4][BVAR];  // [model 1..3][tile shape]
   int per_tile;               // 1: step kernels take BulkArgs and one block per tile
                               // (k_batch_bulk); 0: BatchCase and a persistent grid
-  const void *special[4];     // [model 1..3]: k_batch_special (persistent kinds) or
-                              // k_batch_special_c (per-tile kinds)
+  const void *special[4];     // [model 1..3]: k_batch_special (persistent kinds only;
+                              // the per-tile kernels update their special nodes)
   const void *du;
   const void *advance;
   const void *converge;

@@ -61,6 +61,7 @@ struct lbm_batch {
   int4 *d_rows = nullptr;
   int nrows = 0;
   int4 *d_special = nullptr;  // (case, node, record, flags) of every node with boundary work, sorted by kind
+  int4 *d_tspec[lbm::BVAR] = {};  // per tile shape: the same entries in tile order (per-tile kernels)
   int nspecial = 0;
   int *d_nspecial = nullptr;  // nspecial on the device (the boundary-node kernel's count)
   int4 *d_live_tiles = nullptr;   // compacted work lists of the cases still stepping
@@ -181,7 +182,8 @@ lbm_status launch_compact(lbm_batch *b) {
 
 lbm_status launch_steps(lbm_batch *b, int k) {
   const void *fn = b->bk->step[b->model][b->variant];
-  const int bx = lbm::BVAR_BX[b->variant];
+  // per-tile kernels: BX bulk threads and one warp for the tile's special nodes
+  const int bx = lbm::BVAR_BX[b->variant] + (b->bk->per_tile ? 32 : 0);
   // per-tile kernels: one block per tile of the full list (blocks past the
   // live count return); persistent kernels: one wave of resident blocks
   const int grid = b->bk->per_tile ? b->ntiles[b->variant]
@@ -194,22 +196,20 @@ lbm_status launch_steps(lbm_batch *b, int k) {
     // the boundary-node pass writes other nodes than the bulk pass and both
     // only read the source state, so it runs on a second stream alongside
     // (fork and join by events: two parallel branches when captured)
-    if (b->nspecial > 0) {
+    // (the per-tile kernels update the special nodes of their tiles themselves)
+    const bool side = b->nspecial > 0 && !b->bk->per_tile;
+    if (side) {
       LBM_BCK(cudaEventRecord(b->ev_fork, b->stream));
       LBM_BCK(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
     }
-    void *args[] = {&step_args0, &b->d_live_tiles, &cnt_t, &b->s.active, &b->s.gpar};
+    void *args[] = {&step_args0, &b->d_live_tiles, &cnt_t,   &b->s.active,
+                    &b->s.gpar,  &b->d_extra,      &b->d_tspec[b->variant], &b->d_cases};
     cudaError_t e = cudaLaunchKernel(fn, dim3(grid), dim3(bx), args, 0, b->stream);
     if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
-    if (b->nspecial > 0) {
+    if (side) {
       void *sargs[] = {&b->d_cases, &b->d_special, &b->d_nspecial, &b->s.active, &b->s.gpar};
-      void *cargs[] = {&b->d_bulk,     &b->d_extra,    &b->d_cases, &b->d_special,
-                       &b->d_nspecial, &b->s.active, &b->s.gpar};
-      // k_batch_special_c: one thread per entry; k_batch_special: grid-stride
-      const int sg = b->bk->per_tile ? (b->nspecial + 127) / 128
-                                     : std::min((b->nspecial + 127) / 128, 152 * 16);
-      e = cudaLaunchKernel(b->bk->special[b->model], dim3(sg), dim3(128),
-                           b->bk->per_tile ? cargs : sargs, 0, b->side);
+      const int sg = std::min((b->nspecial + 127) / 128, 152 * 16);
+      e = cudaLaunchKernel(b->bk->special[b->model], dim3(sg), dim3(128), sargs, 0, b->side);
       if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch special: ") + cudaGetErrorString(e));
       LBM_BCK(cudaEventRecord(b->ev_join, b->side));
       LBM_BCK(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
@@ -304,6 +304,7 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
   std::vector<std::vector<int4>> tiles(lbm::BVAR);
   std::vector<int4> rows;
   std::vector<int4> specials;
+  std::vector<int4> tspec[lbm::BVAR];  // per tile shape, tile-ordered (per-tile kernels)
   std::vector<uint32_t> special_key;
   const size_t es = (size_t)b->ks->elem_size;
   const double w[9] = {4. / 9., 1. / 9., 1. / 9., 1. / 9., 1. / 9., 1. / 36., 1. / 36., 1. / 36., 1. / 36.};
@@ -366,8 +367,32 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
     b->hcases[c].vprev = d.vprev;
     for (int v = 0; v < lbm::BVAR; v++) {
       const int bx = lbm::BVAR_BX[v], npt = lbm::BVAR_NPT[v];
-      for (int by = 0; by < (P.m + npt - 1) / npt; by++)
-        for (int tx = 0; tx < (P.n + bx - 1) / bx; tx++) tiles[v].push_back(make_int4(c, tx, by, 0));
+      const int ntx = (P.n + bx - 1) / bx, nby = (P.m + npt - 1) / npt;
+      if (!b->bk->per_tile) {
+        for (int by = 0; by < nby; by++)
+          for (int tx = 0; tx < ntx; tx++) tiles[v].push_back(make_int4(c, tx, by, 0));
+        continue;
+      }
+      // per-tile kernels: each tile carries the range of its special nodes in
+      // the tile-ordered list (sorted by flags within the tile)
+      std::vector<std::vector<int>> bucket((size_t)ntx * nby);
+      for (size_t ri = 0; ri < P.rec.size(); ri++) {
+        const long long node = P.rec[ri].node;
+        const int x = (int)(node % P.pitch), y = (int)(node / P.pitch);
+        bucket[(size_t)(y / npt) * ntx + x / bx].push_back((int)ri);
+      }
+      for (int by = 0; by < nby; by++)
+        for (int tx = 0; tx < ntx; tx++) {
+          std::vector<int> &bk = bucket[(size_t)by * ntx + tx];
+          std::stable_sort(bk.begin(), bk.end(),
+                           [&](int i, int j) { return P.rec[i].flags < P.rec[j].flags; });
+          if (tx > 0xffff || bk.size() > 0xffff || tspec[v].size() > (size_t)INT32_MAX)
+            return bail(fail(LBM_INVALID, "batch: tile list too large"));
+          const int begin = (int)tspec[v].size();
+          for (int ri : bk)
+            tspec[v].push_back(make_int4(c, (int)P.rec[ri].node, ri, (int)P.rec[ri].flags));
+          tiles[v].push_back(make_int4(c, (int)((unsigned)tx | ((unsigned)bk.size() << 16)), by, begin));
+        }
     }
     for (int y = 0; y < P.m; y++)
       for (int tx = 0; tx < (P.n + 127) / 128; tx++) rows.push_back(make_int4(c, tx, y, 0));
@@ -429,6 +454,11 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
     }
     if ((st = balloc(b, &b->d_extra, extra.size())) != LBM_OK) return bail(st);
     cudaMemcpy(b->d_extra, extra.data(), extra.size() * sizeof(lbm::SpecExtra), cudaMemcpyHostToDevice);
+  }
+  for (int v = 0; v < lbm::BVAR; v++) {
+    if ((st = balloc(b, &b->d_tspec[v], tspec[v].size())) != LBM_OK) return bail(st);
+    if (!tspec[v].empty())
+      cudaMemcpy(b->d_tspec[v], tspec[v].data(), tspec[v].size() * sizeof(int4), cudaMemcpyHostToDevice);
   }
   for (int v = 0; v < lbm::BVAR; v++) {
     b->ntiles[v] = (int)tiles[v].size();

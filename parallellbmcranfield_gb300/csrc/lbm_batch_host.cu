@@ -38,6 +38,7 @@ struct CaseDev {
   uint8_t *cls = nullptr;
   uint32_t *aux = nullptr;
   lbm::BRec *rec = nullptr;
+  lbm::WRec *wrec = nullptr;  // FP32 copies of rec (per-tile kernels)
   float *uprev = nullptr, *vprev = nullptr;
   int n = 0, m = 0;
   long long fluid = 0;
@@ -61,7 +62,6 @@ struct lbm_batch {
   int4 *d_rows = nullptr;
   int nrows = 0;
   int4 *d_special = nullptr;  // (case, node, record, flags) of every node with boundary work, sorted by kind
-  int4 *d_tspec[lbm::BVAR] = {};  // per tile shape: the same entries in tile order (per-tile kernels)
   int nspecial = 0;
   int *d_nspecial = nullptr;  // nspecial on the device (the boundary-node kernel's count)
   int4 *d_live_tiles = nullptr;   // compacted work lists of the cases still stepping
@@ -182,8 +182,7 @@ lbm_status launch_compact(lbm_batch *b) {
 
 lbm_status launch_steps(lbm_batch *b, int k) {
   const void *fn = b->bk->step[b->model][b->variant];
-  // per-tile kernels: BX bulk threads and one warp for the tile's special nodes
-  const int bx = lbm::BVAR_BX[b->variant] + (b->bk->per_tile ? 32 : 0);
+  const int bx = lbm::BVAR_BX[b->variant];
   // per-tile kernels: one block per tile of the full list (blocks past the
   // live count return); persistent kernels: one wave of resident blocks
   const int grid = b->bk->per_tile ? b->ntiles[b->variant]
@@ -196,20 +195,25 @@ lbm_status launch_steps(lbm_batch *b, int k) {
     // the boundary-node pass writes other nodes than the bulk pass and both
     // only read the source state, so it runs on a second stream alongside
     // (fork and join by events: two parallel branches when captured)
-    // (the per-tile kernels update the special nodes of their tiles themselves)
-    const bool side = b->nspecial > 0 && !b->bk->per_tile;
+    // (per-tile kernels: only the inlet / outlet nodes are in the list; the
+    // tiles update their wall and lid nodes themselves)
+    const bool side = b->nspecial > 0;
     if (side) {
       LBM_BCK(cudaEventRecord(b->ev_fork, b->stream));
       LBM_BCK(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
     }
-    void *args[] = {&step_args0, &b->d_live_tiles, &cnt_t,   &b->s.active,
-                    &b->s.gpar,  &b->d_extra,      &b->d_tspec[b->variant], &b->d_cases};
+    void *args[] = {&step_args0, &b->d_live_tiles, &cnt_t, &b->s.active, &b->s.gpar, &b->d_extra};
     cudaError_t e = cudaLaunchKernel(fn, dim3(grid), dim3(bx), args, 0, b->stream);
     if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
     if (side) {
       void *sargs[] = {&b->d_cases, &b->d_special, &b->d_nspecial, &b->s.active, &b->s.gpar};
-      const int sg = std::min((b->nspecial + 127) / 128, 152 * 16);
-      e = cudaLaunchKernel(b->bk->special[b->model], dim3(sg), dim3(128), sargs, 0, b->side);
+      void *cargs[] = {&b->d_bulk,     &b->d_extra,  &b->d_cases, &b->d_special,
+                       &b->d_nspecial, &b->s.active, &b->s.gpar};
+      // k_batch_special_c: one thread per entry; k_batch_special: grid-stride
+      const int sg = b->bk->per_tile ? (b->nspecial + 127) / 128
+                                     : std::min((b->nspecial + 127) / 128, 152 * 16);
+      e = cudaLaunchKernel(b->bk->special[b->model], dim3(sg), dim3(128),
+                           b->bk->per_tile ? cargs : sargs, 0, b->side);
       if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch special: ") + cudaGetErrorString(e));
       LBM_BCK(cudaEventRecord(b->ev_join, b->side));
       LBM_BCK(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
@@ -304,7 +308,6 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
   std::vector<std::vector<int4>> tiles(lbm::BVAR);
   std::vector<int4> rows;
   std::vector<int4> specials;
-  std::vector<int4> tspec[lbm::BVAR];  // per tile shape, tile-ordered (per-tile kernels)
   std::vector<uint32_t> special_key;
   const size_t es = (size_t)b->ks->elem_size;
   const double w[9] = {4. / 9., 1. / 9., 1. / 9., 1. / 9., 1. / 9., 1. / 36., 1. / 36., 1. / 36., 1. / 36.};
@@ -334,6 +337,21 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
     cudaMemcpy(d.aux, P.aux.data(), P.aux.size() * 4, cudaMemcpyHostToDevice);
     if (!P.rec.empty())
       cudaMemcpy(d.rec, P.rec.data(), P.rec.size() * sizeof(lbm::BRec), cudaMemcpyHostToDevice);
+    {
+      // FP32 copies of the records for the per-tile kernels' wall treatment
+      std::vector<lbm::WRec> wr(P.rec.size());
+      for (size_t ri = 0; ri < P.rec.size(); ri++) {
+        const lbm::BRec &r = P.rec[ri];
+        lbm::WRec &w = wr[ri];
+        std::memset(&w, 0, sizeof w);
+        w.flags = r.flags | ((r.flags & (lbm::FL_WEST | lbm::FL_EAST)) ? 0u : lbm::FL_SIMPLE);
+        w.uo = (float)r.uo;
+        for (int k = 0; k < 9; k++) w.q[k] = (float)r.q[k];
+      }
+      if ((st = balloc(b, &d.wrec, wr.size())) != LBM_OK) return bail(st);
+      if (!wr.empty())
+        cudaMemcpy(d.wrec, wr.data(), wr.size() * sizeof(lbm::WRec), cudaMemcpyHostToDevice);
+    }
     lbm::StepArgs a;
     std::memset(&a, 0, sizeof a);
     a.n = P.n;
@@ -367,37 +385,15 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
     b->hcases[c].vprev = d.vprev;
     for (int v = 0; v < lbm::BVAR; v++) {
       const int bx = lbm::BVAR_BX[v], npt = lbm::BVAR_NPT[v];
-      const int ntx = (P.n + bx - 1) / bx, nby = (P.m + npt - 1) / npt;
-      if (!b->bk->per_tile) {
-        for (int by = 0; by < nby; by++)
-          for (int tx = 0; tx < ntx; tx++) tiles[v].push_back(make_int4(c, tx, by, 0));
-        continue;
-      }
-      // per-tile kernels: each tile carries the range of its special nodes in
-      // the tile-ordered list (sorted by flags within the tile)
-      std::vector<std::vector<int>> bucket((size_t)ntx * nby);
-      for (size_t ri = 0; ri < P.rec.size(); ri++) {
-        const long long node = P.rec[ri].node;
-        const int x = (int)(node % P.pitch), y = (int)(node / P.pitch);
-        bucket[(size_t)(y / npt) * ntx + x / bx].push_back((int)ri);
-      }
-      for (int by = 0; by < nby; by++)
-        for (int tx = 0; tx < ntx; tx++) {
-          std::vector<int> &bk = bucket[(size_t)by * ntx + tx];
-          std::stable_sort(bk.begin(), bk.end(),
-                           [&](int i, int j) { return P.rec[i].flags < P.rec[j].flags; });
-          if (tx > 0xffff || bk.size() > 0xffff || tspec[v].size() > (size_t)INT32_MAX)
-            return bail(fail(LBM_INVALID, "batch: tile list too large"));
-          const int begin = (int)tspec[v].size();
-          for (int ri : bk)
-            tspec[v].push_back(make_int4(c, (int)P.rec[ri].node, ri, (int)P.rec[ri].flags));
-          tiles[v].push_back(make_int4(c, (int)((unsigned)tx | ((unsigned)bk.size() << 16)), by, begin));
-        }
+      for (int by = 0; by < (P.m + npt - 1) / npt; by++)
+        for (int tx = 0; tx < (P.n + bx - 1) / bx; tx++) tiles[v].push_back(make_int4(c, tx, by, 0));
     }
     for (int y = 0; y < P.m; y++)
       for (int tx = 0; tx < (P.n + 127) / 128; tx++) rows.push_back(make_int4(c, tx, y, 0));
     for (size_t ri = 0; ri < P.rec.size(); ri++) {
       const lbm::BRec &r = P.rec[ri];
+      // per-tile kernels treat wall, curved-wall and lid nodes in the tiles
+      if (b->bk->per_tile && !(r.flags & (lbm::FL_WEST | lbm::FL_EAST))) continue;
       specials.push_back(make_int4(c, (int)r.node, (int)ri, (int)r.flags));
       special_key.push_back(r.flags);
     }
@@ -446,6 +442,7 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
       lbm::SpecExtra &x = extra[c];
       std::memset(&x, 0, sizeof x);
       x.rec = a.rec;
+      x.wrec = b->cases[c].wrec;
       x.aux = a.aux;
       x.nanflag = a.nanflag;
       x.curved = a.curved;
@@ -454,11 +451,6 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
     }
     if ((st = balloc(b, &b->d_extra, extra.size())) != LBM_OK) return bail(st);
     cudaMemcpy(b->d_extra, extra.data(), extra.size() * sizeof(lbm::SpecExtra), cudaMemcpyHostToDevice);
-  }
-  for (int v = 0; v < lbm::BVAR; v++) {
-    if ((st = balloc(b, &b->d_tspec[v], tspec[v].size())) != LBM_OK) return bail(st);
-    if (!tspec[v].empty())
-      cudaMemcpy(b->d_tspec[v], tspec[v].data(), tspec[v].size() * sizeof(int4), cudaMemcpyHostToDevice);
   }
   for (int v = 0; v < lbm::BVAR; v++) {
     b->ntiles[v] = (int)tiles[v].size();

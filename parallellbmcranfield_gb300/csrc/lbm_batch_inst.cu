@@ -45,7 +45,11 @@ const BatchKernels &LBM_BATCH_FN(LBM_PREC)() {
     fill_batch_steps<LBM_ST, 1>(k.step[1]);
     fill_batch_steps<LBM_ST, 2>(k.step[2]);
     fill_batch_steps<LBM_ST, 3>(k.step[3]);
-    if (!k.per_tile) {
+    if (k.per_tile) {
+      k.special[1] = (const void *)k_batch_special_c<LBM_ST, 1>;
+      k.special[2] = (const void *)k_batch_special_c<LBM_ST, 2>;
+      k.special[3] = (const void *)k_batch_special_c<LBM_ST, 3>;
+    } else {
       k.special[1] = (const void *)k_batch_special<LBM_ST, 1>;
       k.special[2] = (const void *)k_batch_special<LBM_ST, 2>;
       k.special[3] = (const void *)k_batch_special<LBM_ST, 3>;

@@ -67,14 +67,14 @@ __global__ void __launch_bounds__(BX) k_batch_step(const BatchCase *cases, const
 // One special node whose boundary record is known: the special branch of
 // step_one (the same treatment and collision) without the class, index and
 // record lookups that find it.
-template <class ST, int MODEL, bool EXTRAP = true, class REC = BRec>
+template <class ST, int MODEL, bool EXTRAP = true>
 __device__ __forceinline__ void step_special_rec(const StepArgs &a, long long node,
-                                                 const REC &r) {
+                                                 const BRec &r) {
   using R = typename ST::R;
   constexpr bool SH = ST::SHIFT;
   R F[9], mac[3];
-  special_node_rec<R, AccMain<ST, PH_AB, SH>, EXTRAP, REC>(a, AccMain<ST, PH_AB, SH>(a, a.src), node,
-                                                           r, F, mac);
+  special_node_rec<R, AccMain<ST, PH_AB, SH>, EXTRAP>(a, AccMain<ST, PH_AB, SH>(a, a.src), node, r,
+                                                      F, mac);
   if constexpr (SH) {
     R M[9];
     collide_dev<MODEL>(F, mac[0], mac[1], mac[2], a, M);
@@ -119,76 +119,10 @@ struct BulkArgs {
 };
 static_assert(sizeof(BulkArgs) == 128, "BulkArgs layout");
 
-// Boundary record of the per-tile batches: the fields of BRec the treatment
-// reads, in the arithmetic type of those batches (the single-domain FP32 and
-// FP16-dev paths convert the same doubles to FP32).  FL_SIMPLE marks the
-// nodes the bulk kernel treats itself (no inlet or outlet: walls, curved
-// walls, the lid); the others go to the boundary-node pass.
-struct WRec {
-  uint32_t flags;
-  float uo;
-  float q[9];
-  uint32_t pad;
-};
-static_assert(sizeof(WRec) == 48, "WRec layout");
-constexpr uint32_t FL_SIMPLE = 1u << 30;
-
-// Per-case fields the boundary treatment needs beyond BulkArgs.
-struct SpecExtra {
-  const BRec *rec;
-  const uint32_t *aux;
-  const WRec *wrec;
-  int *nanflag;
-  int curved, outlet;
-  double rho_out;
-};
-
-// A case's arguments for the boundary treatment, in registers: the 128-byte
-// BulkArgs of its parity and its SpecExtra.
-__device__ __forceinline__ void spec_args(const BulkArgs &b, const SpecExtra &x, StepArgs &a) {
-  a.src = const_cast<void *>(b.src);
-  a.dst = b.dst;
-  a.cls = b.cls;
-  a.plane = b.plane;
-  a.pitch = b.pitch;
-  a.n = b.n;
-  a.m = b.m;
-  a.omega = b.omega;
-  a.omegaA = b.omegaA;
-  a.rho0 = b.rho0;
-  a.rec = x.rec;
-  a.aux = x.aux;
-  a.nanflag = x.nanflag;
-  a.curved = x.curved;
-  a.outlet = x.outlet;
-  a.rho_out = x.rho_out;
-#pragma unroll
-  for (int k = 0; k < 9; k++) {
-    a.scale[k] = b.scale[k];
-    a.inv_scale[k] = b.inv_scale[k];
-  }
-}
-
-// A special node met by the bulk kernel, out of line so that its registers
-// and its copy of the case arguments stay out of the bulk path: the
-// single-domain treatment and collision of a wall, curved-wall or lid node.
-// Its populations lie in the sectors the warp's bulk lanes have just read
-// (L1 hits), and its stores complete the sectors they write.
-template <class ST, int MODEL>
-__device__ __noinline__ void batch_simple_special(const BulkArgs *b, const SpecExtra *x,
-                                                  long long node) {
-  const WRec &w = x->wrec[__ldg(&x->aux[node])];
-  if (!(w.flags & FL_SIMPLE)) return;  // inlet / outlet: the boundary-node pass
-  StepArgs a;
-  spec_args(*b, *x, a);
-  step_special_rec<ST, MODEL, false, WRec>(a, node, w);
-}
-
-// One column of NPT rows: bulk nodes (class 1) with all their loads issued
-// first, then the column's simple special nodes (class 3).
+// Bulk nodes (class 1) of one column of NPT rows; every other class is left
+// to the boundary-node pass.  The loads of all NPT nodes go out first.
 template <class ST, int MODEL, int NPT>
-__device__ __forceinline__ void bulk_column(const StepArgs &a, int x, int y0, const BulkArgs *bp,
-                                            const SpecExtra *xp) {
+__device__ __forceinline__ void bulk_column(const StepArgs &a, int x, int y0) {
   using R = typename ST::R;
   using T = typename ST::T;
   if (x >= a.n) return;
@@ -209,45 +143,24 @@ __device__ __forceinline__ void bulk_column(const StepArgs &a, int x, int y0, co
   for (int j = 0; j < NPT; j++)
     if (c[j] == CLS_BULK)
       bulk_store<ST, MODEL, PH_AB>(a, (long long)(y0 + j) * a.pitch + x, c[j], F[j]);
-#pragma unroll
-  for (int j = 0; j < NPT; j++)
-    if (c[j] == CLS_SPECIAL)
-      batch_simple_special<ST, MODEL>(bp, xp, (long long)(y0 + j) * a.pitch + x);
 }
 
-// A node of an extrapolating outlet: the full treatment with the case's
-// arguments in global memory (it treats the two nodes upstream as well).
-template <class ST, int MODEL>
-__device__ __noinline__ void batch_special_full(const StepArgs &a, long long node, int rec) {
-  step_special_rec<ST, MODEL>(a, node, a.rec[rec]);
-}
-
-// Batched step with one block per live (case, tile): no persistent loop and
-// no shared-memory copy of the case arguments, so a block's loads go out as
-// soon as it starts and the hardware keeps every SM filled with blocks.  The
-// tiles update their bulk nodes and their simple special nodes (walls,
-// curved walls, lid); inlet and outlet nodes go to k_batch_special_c.
+// Batched bulk pass with one block per live (case, tile): no persistent loop
+// and no shared-memory copy of the case arguments, so a block's loads go out
+// as soon as it starts and the hardware keeps every SM filled with blocks.
 // Blocks past the live count (the grid is sized for all tiles when the
 // graph is captured) return at once.
-// Register budget of the bulk path per rows-per-thread: the out-of-line
-// special-node treatment is held to it (it may spill) so that it does not
-// cost the bulk warps occupancy.
-constexpr int bulk_regs(int npt) { return npt <= 1 ? 48 : (npt == 2 ? 56 : 72); }
-
 template <class ST, int MODEL, int BX, int NPT>
-__global__ void __launch_bounds__(BX, 65536 / (BX * bulk_regs(NPT))) k_batch_bulk(
-    const BulkArgs *__restrict__ args,
+__global__ void __launch_bounds__(BX) k_batch_bulk(const BulkArgs *__restrict__ args,
                                                    const int4 *__restrict__ tiles,
                                                    const int *__restrict__ ntiles_live,
                                                    const int *__restrict__ active,
-                                                   const int *__restrict__ gpar,
-                                                   const SpecExtra *__restrict__ extra) {
+                                                   const int *__restrict__ gpar) {
   const int t = blockIdx.x;
   if (t >= __ldg(ntiles_live)) return;
   const int4 tl = __ldg(&tiles[t]);
   if (!__ldg(&active[tl.x])) return;
-  const BulkArgs *bp = &args[2 * tl.x + (__ldg(&gpar[tl.x]) & 1)];
-  const BulkArgs &b = *bp;
+  const BulkArgs &b = args[2 * tl.x + (__ldg(&gpar[tl.x]) & 1)];
   StepArgs a;
   a.src = const_cast<void *>(b.src);
   a.dst = b.dst;
@@ -267,14 +180,32 @@ __global__ void __launch_bounds__(BX, 65536 / (BX * bulk_regs(NPT))) k_batch_bul
       a.inv_scale[k] = b.inv_scale[k];
     }
   }
-  bulk_column<ST, MODEL, NPT>(a, tl.y * BX + threadIdx.x, tl.z * NPT, bp, &extra[tl.x]);
+  bulk_column<ST, MODEL, NPT>(a, tl.y * BX + threadIdx.x, tl.z * NPT);
 }
 
-// Boundary-node pass of the per-tile batches (FP32, FP16-dev) over the inlet
-// and outlet nodes: one thread per entry of the (case, node, record, flags)
-// list.  The case arguments are assembled in registers from the BulkArgs of
-// the case's parity and its SpecExtra.  Nodes of an extrapolating outlet
-// take the full path with the arguments in global memory.
+// Per-case fields the boundary-node pass needs beyond BulkArgs.
+struct SpecExtra {
+  const BRec *rec;
+  const uint32_t *aux;
+  int *nanflag;
+  int curved, outlet;
+  double rho_out;
+};
+
+// A node of an extrapolating outlet: the full treatment with the case's
+// arguments in global memory (it treats the two nodes upstream as well).
+template <class ST, int MODEL>
+__device__ __noinline__ void batch_special_full(const StepArgs &a, long long node, int rec) {
+  step_special_rec<ST, MODEL>(a, node, a.rec[rec]);
+}
+
+// Boundary-node pass of the per-tile batches (FP32, FP16-dev): one thread per
+// entry of the (case, node, record, flags) list.  The case arguments are
+// assembled in registers from the 128-byte BulkArgs of the case's parity and
+// its SpecExtra, both read once, so the chain of dependent loads per node is
+// entry -> (parity, arguments, record) -> populations, and no argument is
+// reloaded after the node's stores.  Nodes of an extrapolating outlet take
+// the full path with the arguments in global memory.
 template <class ST, int MODEL>
 __global__ void __launch_bounds__(128) k_batch_special_c(const BulkArgs *__restrict__ args,
                                                          const SpecExtra *__restrict__ extra,
@@ -294,8 +225,31 @@ __global__ void __launch_bounds__(128) k_batch_special_c(const BulkArgs *__restr
     batch_special_full<ST, MODEL>(cases[e.x].args[par], (long long)e.y, e.z);
     return;
   }
+  const BulkArgs &b = args[2 * e.x + par];
   StepArgs a;
-  spec_args(args[2 * e.x + par], x, a);
+  a.src = const_cast<void *>(b.src);
+  a.dst = b.dst;
+  a.cls = b.cls;
+  a.plane = b.plane;
+  a.pitch = b.pitch;
+  a.n = b.n;
+  a.m = b.m;
+  a.omega = b.omega;
+  a.omegaA = b.omegaA;
+  a.rho0 = b.rho0;
+  a.rec = x.rec;
+  a.aux = x.aux;
+  a.nanflag = x.nanflag;
+  a.curved = x.curved;
+  a.outlet = x.outlet;
+  a.rho_out = x.rho_out;
+  if constexpr (sizeof(typename ST::T) == 2) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      a.scale[k] = b.scale[k];
+      a.inv_scale[k] = b.inv_scale[k];
+    }
+  }
   step_special_rec<ST, MODEL, false>(a, (long long)e.y, x.rec[e.z]);
 }
 
@@ -390,7 +344,7 @@ struct BatchKernels {
   int per_tile;               // 1: step kernels take BulkArgs and one block per tile
                               // (k_batch_bulk); 0: BatchCase and a persistent grid
   const void *special[4];     // [model 1..3]: k_batch_special (persistent kinds) or
-                              // k_batch_special_c (per-tile kinds: inlet / outlet nodes)
+                              // k_batch_special_c (per-tile kinds)
   const void *du;
   const void *advance;
   const void *converge;

@@ -38,7 +38,6 @@ struct CaseDev {
   uint8_t *cls = nullptr;
   uint32_t *aux = nullptr;
   lbm::BRec *rec = nullptr;
-  lbm::WRec *wrec = nullptr;  // FP32 copies of rec (per-tile kernels)
   float *uprev = nullptr, *vprev = nullptr;
   int n = 0, m = 0;
   long long fluid = 0;
@@ -195,19 +194,16 @@ lbm_status launch_steps(lbm_batch *b, int k) {
     // the boundary-node pass writes other nodes than the bulk pass and both
     // only read the source state, so it runs on a second stream alongside
     // (fork and join by events: two parallel branches when captured)
-    // (per-tile kernels: only the inlet / outlet nodes are in the list; the
-    // tiles update their wall and lid nodes themselves)
-    const bool side = b->nspecial > 0;
-    if (side) {
+    if (b->nspecial > 0) {
       LBM_BCK(cudaEventRecord(b->ev_fork, b->stream));
       LBM_BCK(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
     }
-    void *args[] = {&step_args0, &b->d_live_tiles, &cnt_t, &b->s.active, &b->s.gpar, &b->d_extra};
+    void *args[] = {&step_args0, &b->d_live_tiles, &cnt_t, &b->s.active, &b->s.gpar};
     cudaError_t e = cudaLaunchKernel(fn, dim3(grid), dim3(bx), args, 0, b->stream);
     if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
-    if (side) {
+    if (b->nspecial > 0) {
       void *sargs[] = {&b->d_cases, &b->d_special, &b->d_nspecial, &b->s.active, &b->s.gpar};
-      void *cargs[] = {&b->d_bulk,     &b->d_extra,  &b->d_cases, &b->d_special,
+      void *cargs[] = {&b->d_bulk,     &b->d_extra,    &b->d_cases, &b->d_special,
                        &b->d_nspecial, &b->s.active, &b->s.gpar};
       // k_batch_special_c: one thread per entry; k_batch_special: grid-stride
       const int sg = b->bk->per_tile ? (b->nspecial + 127) / 128
@@ -337,21 +333,6 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
     cudaMemcpy(d.aux, P.aux.data(), P.aux.size() * 4, cudaMemcpyHostToDevice);
     if (!P.rec.empty())
       cudaMemcpy(d.rec, P.rec.data(), P.rec.size() * sizeof(lbm::BRec), cudaMemcpyHostToDevice);
-    {
-      // FP32 copies of the records for the per-tile kernels' wall treatment
-      std::vector<lbm::WRec> wr(P.rec.size());
-      for (size_t ri = 0; ri < P.rec.size(); ri++) {
-        const lbm::BRec &r = P.rec[ri];
-        lbm::WRec &w = wr[ri];
-        std::memset(&w, 0, sizeof w);
-        w.flags = r.flags | ((r.flags & (lbm::FL_WEST | lbm::FL_EAST)) ? 0u : lbm::FL_SIMPLE);
-        w.uo = (float)r.uo;
-        for (int k = 0; k < 9; k++) w.q[k] = (float)r.q[k];
-      }
-      if ((st = balloc(b, &d.wrec, wr.size())) != LBM_OK) return bail(st);
-      if (!wr.empty())
-        cudaMemcpy(d.wrec, wr.data(), wr.size() * sizeof(lbm::WRec), cudaMemcpyHostToDevice);
-    }
     lbm::StepArgs a;
     std::memset(&a, 0, sizeof a);
     a.n = P.n;
@@ -392,8 +373,6 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
       for (int tx = 0; tx < (P.n + 127) / 128; tx++) rows.push_back(make_int4(c, tx, y, 0));
     for (size_t ri = 0; ri < P.rec.size(); ri++) {
       const lbm::BRec &r = P.rec[ri];
-      // per-tile kernels treat wall, curved-wall and lid nodes in the tiles
-      if (b->bk->per_tile && !(r.flags & (lbm::FL_WEST | lbm::FL_EAST))) continue;
       specials.push_back(make_int4(c, (int)r.node, (int)ri, (int)r.flags));
       special_key.push_back(r.flags);
     }
@@ -442,7 +421,6 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
       lbm::SpecExtra &x = extra[c];
       std::memset(&x, 0, sizeof x);
       x.rec = a.rec;
-      x.wrec = b->cases[c].wrec;
       x.aux = a.aux;
       x.nanflag = a.nanflag;
       x.curved = a.curved;

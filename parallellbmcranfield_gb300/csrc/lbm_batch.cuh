@@ -67,14 +67,14 @@ __global__ void __launch_bounds__(BX) k_batch_step(const BatchCase *cases, const
 // One special node whose boundary record is known: the special branch of
 // step_one (the same treatment and collision) without the class, index and
 // record lookups that find it.
-template <class ST, int MODEL, bool EXTRAP = true>
+template <class ST, int MODEL, bool EXTRAP = true, class REC = BRec,
+          class ACC = AccMain<ST, PH_AB, ST::SHIFT>>
 __device__ __forceinline__ void step_special_rec(const StepArgs &a, long long node,
-                                                 const BRec &r) {
+                                                 const REC &r) {
   using R = typename ST::R;
   constexpr bool SH = ST::SHIFT;
   R F[9], mac[3];
-  special_node_rec<R, AccMain<ST, PH_AB, SH>, EXTRAP>(a, AccMain<ST, PH_AB, SH>(a, a.src), node, r,
-                                                      F, mac);
+  special_node_rec<R, ACC, EXTRAP, REC>(a, ACC(a, a.src), node, r, F, mac);
   if constexpr (SH) {
     R M[9];
     collide_dev<MODEL>(F, mac[0], mac[1], mac[2], a, M);
@@ -183,9 +183,40 @@ __global__ void __launch_bounds__(BX) k_batch_bulk(const BulkArgs *__restrict__ 
   bulk_column<ST, MODEL, NPT>(a, tl.y * BX + threadIdx.x, tl.z * NPT);
 }
 
+// Boundary record of the per-tile batches: the fields of BRec the treatment
+// reads, in FP32 (the single-domain FP32 and FP16-dev paths convert the same
+// doubles to FP32), 48 bytes instead of 112.
+struct WRec {
+  uint32_t flags;
+  float uo;
+  float q[9];
+  uint32_t pad;
+};
+static_assert(sizeof(WRec) == 48, "WRec layout");
+
+// METAF of an unshifted (FP32) batch without the class check of AccMain:
+// solid and padding nodes hold 0 in both buffers (zeroed at allocation,
+// written as 0 by the first collision, never written again), the value
+// AccMain returns for them, so every read gives the same result with one
+// load instead of two (the class byte of a wall's neighbour is a sector of
+// its own).
+template <class ST>
+struct AccRaw {
+  using R = typename ST::R;
+  static constexpr bool dev = false;
+  const StepArgs &a;
+  const typename ST::T *s;
+  __device__ AccRaw(const StepArgs &a_, const void *src)
+      : a(a_), s((const typename ST::T *)src) {}
+  __device__ __forceinline__ R meta(long long z, int k) const {
+    return ST::ld(s + slot_of<PH_AB>(k, z, a), k, a);
+  }
+};
+
 // Per-case fields the boundary-node pass needs beyond BulkArgs.
 struct SpecExtra {
   const BRec *rec;
+  const WRec *wrec;
   const uint32_t *aux;
   int *nanflag;
   int curved, outlet;
@@ -250,7 +281,10 @@ __global__ void __launch_bounds__(128) k_batch_special_c(const BulkArgs *__restr
       a.inv_scale[k] = b.inv_scale[k];
     }
   }
-  step_special_rec<ST, MODEL, false>(a, (long long)e.y, x.rec[e.z]);
+  if constexpr (ST::SHIFT)
+    step_special_rec<ST, MODEL, false, WRec>(a, (long long)e.y, x.wrec[e.z]);
+  else
+    step_special_rec<ST, MODEL, false, WRec, AccRaw<ST>>(a, (long long)e.y, x.wrec[e.z]);
 }
 
 // After a step: active cases advance their parity and counters.

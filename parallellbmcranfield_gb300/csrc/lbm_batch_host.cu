@@ -38,6 +38,7 @@ struct CaseDev {
   uint8_t *cls = nullptr;
   uint32_t *aux = nullptr;
   lbm::BRec *rec = nullptr;
+  lbm::WRec *wrec = nullptr;  // FP32 copies of rec (boundary-node pass of per-tile batches)
   float *uprev = nullptr, *vprev = nullptr;
   int n = 0, m = 0;
   long long fluid = 0;
@@ -333,6 +334,19 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
     cudaMemcpy(d.aux, P.aux.data(), P.aux.size() * 4, cudaMemcpyHostToDevice);
     if (!P.rec.empty())
       cudaMemcpy(d.rec, P.rec.data(), P.rec.size() * sizeof(lbm::BRec), cudaMemcpyHostToDevice);
+    {
+      std::vector<lbm::WRec> wr(P.rec.size());
+      for (size_t ri = 0; ri < P.rec.size(); ri++) {
+        lbm::WRec &w = wr[ri];
+        std::memset(&w, 0, sizeof w);
+        w.flags = P.rec[ri].flags;
+        w.uo = (float)P.rec[ri].uo;
+        for (int k = 0; k < 9; k++) w.q[k] = (float)P.rec[ri].q[k];
+      }
+      if ((st = balloc(b, &d.wrec, wr.size())) != LBM_OK) return bail(st);
+      if (!wr.empty())
+        cudaMemcpy(d.wrec, wr.data(), wr.size() * sizeof(lbm::WRec), cudaMemcpyHostToDevice);
+    }
     lbm::StepArgs a;
     std::memset(&a, 0, sizeof a);
     a.n = P.n;
@@ -421,6 +435,7 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
       lbm::SpecExtra &x = extra[c];
       std::memset(&x, 0, sizeof x);
       x.rec = a.rec;
+      x.wrec = b->cases[c].wrec;
       x.aux = a.aux;
       x.nanflag = a.nanflag;
       x.curved = a.curved;

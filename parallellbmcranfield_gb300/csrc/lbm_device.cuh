@@ -594,9 +594,9 @@ __device__ __noinline__ void boundary_F_noout(const StepArgs &a, const ACC &acc,
 // EXTRAP the extrapolating outlet (outlet 2, which treats the two nodes
 // upstream through an out-of-line call) is left out, so that `a` need not
 // live in memory; the caller routes those nodes elsewhere.
-template <bool OUTLET, class R, class ACC, bool EXTRAP = true>
+template <bool OUTLET, class R, class ACC, bool EXTRAP = true, class REC = BRec>
 __device__ __forceinline__ void boundary_F_rec(const StepArgs &a, const ACC &acc, long long node,
-                                               const BRec &r, R F[9]);
+                                               const REC &r, R F[9]);
 
 template <bool OUTLET, class R, class ACC>
 __device__ void boundary_F(const StepArgs &a, const ACC &acc, long long node, R F[9]) {
@@ -616,9 +616,10 @@ __device__ void boundary_F(const StepArgs &a, const ACC &acc, long long node, R 
   boundary_F_rec<OUTLET, R, ACC>(a, acc, node, a.rec[a.aux[node]], F);
 }
 
-template <bool OUTLET, class R, class ACC, bool EXTRAP>
+// REC: BRec, or a record with the same members (flags, uo, q) in FP32.
+template <bool OUTLET, class R, class ACC, bool EXTRAP, class REC>
 __device__ __forceinline__ void boundary_F_rec(const StepArgs &a, const ACC &acc, long long node,
-                                               const BRec &r, R F[9]) {
+                                               const REC &r, R F[9]) {
   constexpr bool DEV = ACC::dev;
   const R rho0 = DEV ? (R)a.rho0 : R(0);
   const uint32_t fl = r.flags;
@@ -704,10 +705,10 @@ __device__ __forceinline__ void boundary_F_rec(const StepArgs &a, const ACC &acc
 // path's register budget small).  Returns F (in the accessor's form) and the
 // macroscopic fields (V = 0 on east-outlet cells,
 // serial/CellFunctions.c:483-486).
-template <class R, class ACC, bool EXTRAP = true>
+template <class R, class ACC, bool EXTRAP = true, class REC = BRec>
 __device__ __forceinline__ void special_node_rec(const StepArgs &a, const ACC &acc, long long node,
-                                                 const BRec &r, R F[9], R *mac) {
-  boundary_F_rec<true, R, ACC, EXTRAP>(a, acc, node, r, F);
+                                                 const REC &r, R F[9], R *mac) {
+  boundary_F_rec<true, R, ACC, EXTRAP, REC>(a, acc, node, r, F);
   R rho, u, v;
   if constexpr (ACC::dev) {
     R rt = ((F[0] + F[1]) + (F[2] + F[3])) + ((F[4] + F[5]) + (F[6] + F[7])) + F[8];

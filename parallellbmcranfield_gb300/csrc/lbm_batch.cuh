@@ -186,30 +186,52 @@ __global__ void __launch_bounds__(BX) k_batch_bulk(const BulkArgs *__restrict__ 
 // Boundary record of the per-tile batches: the fields of BRec the treatment
 // reads, in FP32 (the single-domain FP32 and FP16-dev paths convert the same
 // doubles to FP32), 48 bytes instead of 112.
+// nrec[k]: the record of the node the link k is pulled from (node - c_k)
+// when that node's METAF is kept in the side arrays, else -1.
 struct WRec {
   uint32_t flags;
   float uo;
   float q[9];
+  int32_t nrec[9];
   uint32_t pad;
 };
-static_assert(sizeof(WRec) == 48, "WRec layout");
+static_assert(sizeof(WRec) == 84, "WRec layout");
 
-// METAF of an unshifted (FP32) batch without the class check of AccMain:
-// solid and padding nodes hold 0 in both buffers (zeroed at allocation,
-// written as 0 by the first collision, never written again), the value
-// AccMain returns for them, so every read gives the same result with one
-// load instead of two (the class byte of a wall's neighbour is a sector of
-// its own).
+// METAF of a special node's own links and of its special neighbours from
+// the node-major side array of the current parity (9 values per record,
+// written by the boundary-node pass next to the planes, equal to what a
+// plane read returns: FP16-dev values pass through the storage's rounding),
+// every other read from the planes.  A wall node's own values and its
+// neighbours along the wall then come from a few contiguous sectors instead
+// of one sector per value and row.  In FP32 the plane reads skip AccMain's
+// class check: solid and padding nodes hold 0 in both buffers (zeroed at
+// allocation, written as 0 by the first collision, never written again),
+// the value AccMain returns for them.
 template <class ST>
-struct AccRaw {
+struct AccSideB {
   using R = typename ST::R;
-  static constexpr bool dev = false;
+  static constexpr bool dev = ST::SHIFT;
   const StepArgs &a;
   const typename ST::T *s;
-  __device__ AccRaw(const StepArgs &a_, const void *src)
-      : a(a_), s((const typename ST::T *)src) {}
+  const float *side;
+  long long node;
+  int ri;
+  const int32_t *nrec;
+  __device__ AccSideB(const StepArgs &a_, const float *side_, long long node_, int ri_,
+                      const int32_t *nrec_)
+      : a(a_), s((const typename ST::T *)a_.src), side(side_), node(node_), ri(ri_), nrec(nrec_) {}
   __device__ __forceinline__ R meta(long long z, int k) const {
-    return ST::ld(s + slot_of<PH_AB>(k, z, a), k, a);
+    if (z == node) return side[(size_t)ri * 9 + k];
+    if (z == node - nb(k, a.pitch)) {
+      const int r = nrec[k];
+      if (r >= 0) return side[(size_t)r * 9 + k];
+    }
+    if constexpr (ST::SHIFT) {
+      if (a.cls[z] == CLS_SOLID) return -wgt<R>(k) * (R)a.rho0;
+      return ST::cvt_dev(__ldg(s + slot_of<PH_AB>(k, z, a)), k, a);
+    } else {
+      return ST::ld(s + slot_of<PH_AB>(k, z, a), k, a);
+    }
   }
 };
 
@@ -217,6 +239,7 @@ struct AccRaw {
 struct SpecExtra {
   const BRec *rec;
   const WRec *wrec;
+  float *side[2];  // side arrays of buffer 0 / 1 (9 values per record)
   const uint32_t *aux;
   int *nanflag;
   int curved, outlet;
@@ -281,10 +304,37 @@ __global__ void __launch_bounds__(128) k_batch_special_c(const BulkArgs *__restr
       a.inv_scale[k] = b.inv_scale[k];
     }
   }
-  if constexpr (ST::SHIFT)
-    step_special_rec<ST, MODEL, false, WRec>(a, (long long)e.y, x.wrec[e.z]);
-  else
-    step_special_rec<ST, MODEL, false, WRec, AccRaw<ST>>(a, (long long)e.y, x.wrec[e.z]);
+  using R = typename ST::R;
+  const long long node = e.y;
+  const WRec &w = x.wrec[e.z];
+  const AccSideB<ST> acc(a, x.side[par], node, e.z, w.nrec);
+  R F[9], mac[3], M[9];
+  special_node_rec<R, AccSideB<ST>, false, WRec>(a, acc, node, w, F, mac);
+  float *out = x.side[par ^ 1] + (size_t)e.z * 9;
+  if constexpr (ST::SHIFT) {
+    collide_dev<MODEL>(F, mac[0], mac[1], mac[2], a, M);
+    store_node_dev<ST, PH_AB>(a, node, (uint8_t)CLS_SPECIAL, M);
+#pragma unroll
+    for (int k = 0; k < 9; k++) out[k] = ST::cvt_dev(ST::pack_dev(M[k], k, a), k, a);
+  } else {
+    collide<MODEL, R>(F, mac[0], mac[1], mac[2], a, M);
+    store_node<ST, PH_AB>(a, node, (uint8_t)CLS_SPECIAL, M);
+#pragma unroll
+    for (int k = 0; k < 9; k++) out[k] = M[k];
+  }
+}
+
+// Side arrays of buffer 0 after a (re)initialisation of one case: every
+// record's nine METAF as the planes hold them.
+template <class ST>
+__global__ void __launch_bounds__(128) k_batch_side_fill(const StepArgs a, const BRec *rec,
+                                                         int nrec, float *side0) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrec) return;
+  const AccMain<ST, PH_AB, ST::SHIFT> acc(a, a.src);
+  const long long node = rec[i].node;
+#pragma unroll
+  for (int k = 0; k < 9; k++) side0[(size_t)i * 9 + k] = acc.meta(node, k);
 }
 
 // After a step: active cases advance their parity and counters.
@@ -379,6 +429,7 @@ struct BatchKernels {
                               // (k_batch_bulk); 0: BatchCase and a persistent grid
   const void *special[4];     // [model 1..3]: k_batch_special (persistent kinds) or
                               // k_batch_special_c (per-tile kinds)
+  const void *side_fill;      // k_batch_side_fill (per-tile kinds)
   const void *du;
   const void *advance;
   const void *converge;

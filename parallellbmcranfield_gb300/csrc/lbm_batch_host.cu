@@ -39,6 +39,8 @@ struct CaseDev {
   uint32_t *aux = nullptr;
   lbm::BRec *rec = nullptr;
   lbm::WRec *wrec = nullptr;  // FP32 copies of rec (boundary-node pass of per-tile batches)
+  float *side[2] = {nullptr, nullptr};  // per-tile batches: METAF of the records, per buffer
+  int nrec = 0;
   float *uprev = nullptr, *vprev = nullptr;
   int n = 0, m = 0;
   long long fluid = 0;
@@ -138,6 +140,21 @@ lbm_status reset_state(lbm_batch *b) {
   return LBM_OK;
 }
 
+// Side arrays of buffer 0 from the planes, after case c was (re)initialised.
+lbm_status fill_side(lbm_batch *b, int c) {
+  const CaseDev &d = b->cases[c];
+  if (!b->bk->per_tile || d.nrec == 0) return LBM_OK;
+  lbm::StepArgs a = b->hcases[c].args[0];  // reads buffer 0
+  const lbm::BRec *rec = d.rec;
+  int nrec = d.nrec;
+  float *side0 = d.side[0];
+  void *args[] = {&a, (void *)&rec, &nrec, &side0};
+  cudaError_t e = cudaLaunchKernel(b->bk->side_fill, dim3((unsigned)((nrec + 127) / 128)), dim3(128),
+                                   args, 0, b->stream);
+  if (e != cudaSuccess) return fail(LBM_CUDA, std::string("side fill: ") + cudaGetErrorString(e));
+  return LBM_OK;
+}
+
 // f = f_eq(rho_ini, 0, 0) and its first collision, for every case.
 lbm_status set_rest(lbm_batch *b) {
   for (int c = 0; c < b->nc; c++) {
@@ -158,6 +175,8 @@ lbm_status set_rest(lbm_batch *b) {
     cudaFreeAsync(dr, b->stream);
     cudaFreeAsync(dz, b->stream);
     if (e != cudaSuccess) return fail(LBM_CUDA, std::string("init launch: ") + cudaGetErrorString(e));
+    lbm_status fs = fill_side(b, c);
+    if (fs != LBM_OK) return fs;
     LBM_BCK(cudaStreamSynchronize(b->stream));  // host vectors go out of scope
   }
   lbm_status s = reset_state(b);
@@ -335,17 +354,38 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
     if (!P.rec.empty())
       cudaMemcpy(d.rec, P.rec.data(), P.rec.size() * sizeof(lbm::BRec), cudaMemcpyHostToDevice);
     {
+      // FP32 records and, per link, the record of the node it is pulled from
+      // when that node's METAF is in the side arrays (every special node but
+      // the outlet ones, which take the full treatment from the planes)
       std::vector<lbm::WRec> wr(P.rec.size());
+      const int D[9][2] = {{0, 0}, {1, 0}, {0, 1}, {-1, 0}, {0, -1}, {1, 1}, {-1, 1}, {-1, -1}, {1, -1}};
       for (size_t ri = 0; ri < P.rec.size(); ri++) {
         lbm::WRec &w = wr[ri];
         std::memset(&w, 0, sizeof w);
         w.flags = P.rec[ri].flags;
         w.uo = (float)P.rec[ri].uo;
-        for (int k = 0; k < 9; k++) w.q[k] = (float)P.rec[ri].q[k];
+        const long long node = P.rec[ri].node;
+        const int x = (int)(node % P.pitch), y = (int)(node / P.pitch);
+        for (int k = 0; k < 9; k++) {
+          w.q[k] = (float)P.rec[ri].q[k];
+          w.nrec[k] = -1;
+          const int xs = x - D[k][0], ys = y - D[k][1];
+          if (xs < 0 || xs >= P.n || ys < 0 || ys >= P.m) continue;
+          const long long z = (long long)ys * P.pitch + xs;
+          if (P.cls[z] != lbm::CLS_SPECIAL) continue;
+          const uint32_t rj = P.aux[z];
+          if (P.rec[rj].flags & lbm::FL_EAST) continue;
+          w.nrec[k] = (int32_t)rj;
+        }
       }
       if ((st = balloc(b, &d.wrec, wr.size())) != LBM_OK) return bail(st);
       if (!wr.empty())
         cudaMemcpy(d.wrec, wr.data(), wr.size() * sizeof(lbm::WRec), cudaMemcpyHostToDevice);
+      d.nrec = (int)P.rec.size();
+      for (int i = 0; i < 2; i++) {
+        if ((st = balloc(b, &d.side[i], P.rec.size() * 9)) != LBM_OK) return bail(st);
+        cudaMemset(d.side[i], 0, std::max<size_t>(P.rec.size() * 9 * sizeof(float), 16));
+      }
     }
     lbm::StepArgs a;
     std::memset(&a, 0, sizeof a);
@@ -436,6 +476,8 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
       std::memset(&x, 0, sizeof x);
       x.rec = a.rec;
       x.wrec = b->cases[c].wrec;
+      x.side[0] = b->cases[c].side[0];
+      x.side[1] = b->cases[c].side[1];
       x.aux = a.aux;
       x.nanflag = a.nanflag;
       x.curved = a.curved;
@@ -529,6 +571,8 @@ lbm_status lbm_batch_set_state(lbm_batch *b, int32_t c, const double *rho, const
   cudaError_t e = cudaLaunchKernel(b->ks->init[b->model][0], grid, dim3(128), args, 0, b->stream);
   cudaFreeAsync(dm, b->stream);
   if (e != cudaSuccess) return fail(LBM_CUDA, std::string("init launch: ") + cudaGetErrorString(e));
+  lbm_status fs = fill_side(b, c);
+  if (fs != LBM_OK) return fs;
   const int one = 1, zero = 0;
   const long long zl = 0, neg = -1;
   LBM_BCK(cudaMemcpyAsync(b->s.active + c, &one, sizeof one, cudaMemcpyHostToDevice, b->stream));

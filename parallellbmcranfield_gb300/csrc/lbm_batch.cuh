@@ -187,13 +187,17 @@ __global__ void __launch_bounds__(BX) k_batch_bulk(const BulkArgs *__restrict__ 
 // reads, in FP32 (the single-domain FP32 and FP16-dev paths convert the same
 // doubles to FP32), 48 bytes instead of 112.
 // nrec[k]: the record of the node the link k is pulled from (node - c_k)
-// when that node's METAF is kept in the side arrays, else -1.
+// when that node's METAF is kept in the side arrays, else -1.  exported:
+// the planes k another update reads from the planes at this node (a bulk
+// neighbour at node + c_k, or one that reads it without the side arrays);
+// the boundary-node pass writes only those planes, k_batch_side_sync the
+// others before anything else reads the whole state.
 struct WRec {
   uint32_t flags;
   float uo;
   float q[9];
   int32_t nrec[9];
-  uint32_t pad;
+  uint32_t exported;
 };
 static_assert(sizeof(WRec) == 84, "WRec layout");
 
@@ -246,6 +250,35 @@ struct SpecExtra {
   double rho_out;
 };
 
+// A case's arguments for the boundary treatment, in registers: the 128-byte
+// BulkArgs of its parity and its SpecExtra.
+template <class ST>
+__device__ __forceinline__ void spec_args(const BulkArgs &b, const SpecExtra &x, StepArgs &a) {
+  a.src = const_cast<void *>(b.src);
+  a.dst = b.dst;
+  a.cls = b.cls;
+  a.plane = b.plane;
+  a.pitch = b.pitch;
+  a.n = b.n;
+  a.m = b.m;
+  a.omega = b.omega;
+  a.omegaA = b.omegaA;
+  a.rho0 = b.rho0;
+  a.rec = x.rec;
+  a.aux = x.aux;
+  a.nanflag = x.nanflag;
+  a.curved = x.curved;
+  a.outlet = x.outlet;
+  a.rho_out = x.rho_out;
+  if constexpr (sizeof(typename ST::T) == 2) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      a.scale[k] = b.scale[k];
+      a.inv_scale[k] = b.inv_scale[k];
+    }
+  }
+}
+
 // A node of an extrapolating outlet: the full treatment with the case's
 // arguments in global memory (it treats the two nodes upstream as well).
 template <class ST, int MODEL>
@@ -279,31 +312,8 @@ __global__ void __launch_bounds__(128) k_batch_special_c(const BulkArgs *__restr
     batch_special_full<ST, MODEL>(cases[e.x].args[par], (long long)e.y, e.z);
     return;
   }
-  const BulkArgs &b = args[2 * e.x + par];
   StepArgs a;
-  a.src = const_cast<void *>(b.src);
-  a.dst = b.dst;
-  a.cls = b.cls;
-  a.plane = b.plane;
-  a.pitch = b.pitch;
-  a.n = b.n;
-  a.m = b.m;
-  a.omega = b.omega;
-  a.omegaA = b.omegaA;
-  a.rho0 = b.rho0;
-  a.rec = x.rec;
-  a.aux = x.aux;
-  a.nanflag = x.nanflag;
-  a.curved = x.curved;
-  a.outlet = x.outlet;
-  a.rho_out = x.rho_out;
-  if constexpr (sizeof(typename ST::T) == 2) {
-#pragma unroll
-    for (int k = 0; k < 9; k++) {
-      a.scale[k] = b.scale[k];
-      a.inv_scale[k] = b.inv_scale[k];
-    }
-  }
+  spec_args<ST>(args[2 * e.x + par], x, a);
   using R = typename ST::R;
   const long long node = e.y;
   const WRec &w = x.wrec[e.z];
@@ -311,16 +321,51 @@ __global__ void __launch_bounds__(128) k_batch_special_c(const BulkArgs *__restr
   R F[9], mac[3], M[9];
   special_node_rec<R, AccSideB<ST>, false, WRec>(a, acc, node, w, F, mac);
   float *out = x.side[par ^ 1] + (size_t)e.z * 9;
+  typename ST::T *d = (typename ST::T *)a.dst;
   if constexpr (ST::SHIFT) {
     collide_dev<MODEL>(F, mac[0], mac[1], mac[2], a, M);
-    store_node_dev<ST, PH_AB>(a, node, (uint8_t)CLS_SPECIAL, M);
 #pragma unroll
-    for (int k = 0; k < 9; k++) out[k] = ST::cvt_dev(ST::pack_dev(M[k], k, a), k, a);
+    for (int k = 0; k < 9; k++) {
+      if ((w.exported >> k) & 1u) st_dev<ST>(d + slot_of<PH_AB>(k, node, a), k, M[k], a);
+      out[k] = ST::cvt_dev(ST::pack_dev(M[k], k, a), k, a);
+    }
   } else {
     collide<MODEL, R>(F, mac[0], mac[1], mac[2], a, M);
-    store_node<ST, PH_AB>(a, node, (uint8_t)CLS_SPECIAL, M);
 #pragma unroll
-    for (int k = 0; k < 9; k++) out[k] = M[k];
+    for (int k = 0; k < 9; k++) {
+      if ((w.exported >> k) & 1u) ST::st(d + slot_of<PH_AB>(k, node, a), k, M[k], a);
+      out[k] = M[k];
+    }
+  }
+}
+
+// The planes the boundary-node pass did not write (WRec::exported clear),
+// from the side arrays of the current parity, for every record of every
+// case: run before the du check and the read-back, which read whole states
+// from the planes.  One thread per (case, record) entry.
+template <class ST>
+__global__ void __launch_bounds__(128) k_batch_side_sync(const BulkArgs *__restrict__ args,
+                                                         const SpecExtra *__restrict__ extra,
+                                                         const int2 *__restrict__ recs, int n,
+                                                         const int *__restrict__ gpar) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int2 e = __ldg(&recs[i]);
+  const int par = __ldg(&gpar[e.x]) & 1;
+  const SpecExtra &x = extra[e.x];
+  const WRec &w = x.wrec[e.y];
+  const uint32_t todo = ~w.exported & 0x1FFu;
+  if (!todo) return;
+  StepArgs a;
+  spec_args<ST>(args[2 * e.x + par], x, a);
+  const long long node = x.rec[e.y].node;
+  typename ST::T *p = (typename ST::T *)a.src;  // the state the next step reads
+  const float *v = x.side[par] + (size_t)e.y * 9;
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    if (!((todo >> k) & 1u)) continue;
+    if constexpr (ST::SHIFT) st_dev<ST>(p + slot_of<PH_AB>(k, node, a), k, v[k], a);
+    else ST::st(p + slot_of<PH_AB>(k, node, a), k, v[k], a);
   }
 }
 
@@ -430,6 +475,7 @@ struct BatchKernels {
   const void *special[4];     // [model 1..3]: k_batch_special (persistent kinds) or
                               // k_batch_special_c (per-tile kinds)
   const void *side_fill;      // k_batch_side_fill (per-tile kinds)
+  const void *side_sync;      // k_batch_side_sync (per-tile kinds)
   const void *du;
   const void *advance;
   const void *converge;

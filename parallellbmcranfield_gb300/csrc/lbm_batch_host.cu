@@ -65,6 +65,8 @@ struct lbm_batch {
   int nrows = 0;
   int4 *d_special = nullptr;  // (case, node, record, flags) of every node with boundary work, sorted by kind
   int nspecial = 0;
+  int2 *d_allrec = nullptr;  // per-tile kinds: (case, record) of every record (side-array sync)
+  int nallrec = 0;
   int *d_nspecial = nullptr;  // nspecial on the device (the boundary-node kernel's count)
   int4 *d_live_tiles = nullptr;   // compacted work lists of the cases still stepping
   int *d_live_n = nullptr;        // [0]: live tiles
@@ -241,7 +243,20 @@ lbm_status launch_steps(lbm_batch *b, int k) {
   return LBM_OK;
 }
 
+// Planes of the boundary records the boundary-node pass left to the side
+// arrays, before anything reads whole states (per-tile kinds).
+lbm_status launch_side_sync(lbm_batch *b) {
+  if (!b->bk->per_tile || b->nallrec == 0) return LBM_OK;
+  void *args[] = {&b->d_bulk, &b->d_extra, &b->d_allrec, &b->nallrec, &b->s.gpar};
+  cudaError_t e = cudaLaunchKernel(b->bk->side_sync, dim3((unsigned)((b->nallrec + 127) / 128)),
+                                   dim3(128), args, 0, b->stream);
+  if (e != cudaSuccess) return fail(LBM_CUDA, std::string("side sync: ") + cudaGetErrorString(e));
+  return LBM_OK;
+}
+
 lbm_status launch_check(lbm_batch *b, int k, double tol) {
+  lbm_status ss = launch_side_sync(b);
+  if (ss != LBM_OK) return ss;
   const int grid = std::min(b->nrows, persistent_blocks(b->bk->du, 128, b->device));
   void *args[] = {&b->d_cases, &b->d_rows, &b->nrows, &b->s};
   cudaError_t e = cudaLaunchKernel(b->bk->du, dim3(grid), dim3(128), args, 0, b->stream);
@@ -324,6 +339,7 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
   std::vector<std::vector<int4>> tiles(lbm::BVAR);
   std::vector<int4> rows;
   std::vector<int4> specials;
+  std::vector<int2> allrec;  // (case, record) of every boundary record (per-tile kinds)
   std::vector<uint32_t> special_key;
   const size_t es = (size_t)b->ks->elem_size;
   const double w[9] = {4. / 9., 1. / 9., 1. / 9., 1. / 9., 1. / 9., 1. / 36., 1. / 36., 1. / 36., 1. / 36.};
@@ -359,24 +375,37 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
       // the outlet ones, which take the full treatment from the planes)
       std::vector<lbm::WRec> wr(P.rec.size());
       const int D[9][2] = {{0, 0}, {1, 0}, {0, 1}, {-1, 0}, {0, -1}, {1, 1}, {-1, 1}, {-1, -1}, {1, -1}};
+      // an extrapolating outlet reads its neighbours' planes through the full
+      // treatment: such cases keep every plane of every record written
+      bool all_planes = false;
+      if (params[c].outlet_profile == 2)
+        for (const lbm::BRec &r : P.rec) all_planes = all_planes || (r.flags & lbm::FL_EAST);
       for (size_t ri = 0; ri < P.rec.size(); ri++) {
         lbm::WRec &w = wr[ri];
         std::memset(&w, 0, sizeof w);
         w.flags = P.rec[ri].flags;
         w.uo = (float)P.rec[ri].uo;
         const long long node = P.rec[ri].node;
+        const bool east = (P.rec[ri].flags & lbm::FL_EAST) != 0;
         const int x = (int)(node % P.pitch), y = (int)(node / P.pitch);
         for (int k = 0; k < 9; k++) {
           w.q[k] = (float)P.rec[ri].q[k];
           w.nrec[k] = -1;
+          // the source of link k: node - c_k
           const int xs = x - D[k][0], ys = y - D[k][1];
-          if (xs < 0 || xs >= P.n || ys < 0 || ys >= P.m) continue;
-          const long long z = (long long)ys * P.pitch + xs;
-          if (P.cls[z] != lbm::CLS_SPECIAL) continue;
-          const uint32_t rj = P.aux[z];
-          if (P.rec[rj].flags & lbm::FL_EAST) continue;
-          w.nrec[k] = (int32_t)rj;
+          if (xs >= 0 && xs < P.n && ys >= 0 && ys < P.m) {
+            const long long z = (long long)ys * P.pitch + xs;
+            if (P.cls[z] == lbm::CLS_SPECIAL && !(P.rec[P.aux[z]].flags & lbm::FL_EAST))
+              w.nrec[k] = (int32_t)P.aux[z];
+          }
+          // the reader of plane k at this node: node + c_k
+          const int xt = x + D[k][0], yt = y + D[k][1];
+          if (k == 0 || xt < 0 || xt >= P.n || yt < 0 || yt >= P.m) continue;
+          const uint8_t ct = P.cls[(long long)yt * P.pitch + xt];
+          if (ct == lbm::CLS_SOLID) continue;
+          if (ct != lbm::CLS_SPECIAL || east) w.exported |= 1u << k;
         }
+        if (all_planes) w.exported = 0x1FFu;
       }
       if ((st = balloc(b, &d.wrec, wr.size())) != LBM_OK) return bail(st);
       if (!wr.empty())
@@ -425,6 +454,8 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
     }
     for (int y = 0; y < P.m; y++)
       for (int tx = 0; tx < (P.n + 127) / 128; tx++) rows.push_back(make_int4(c, tx, y, 0));
+    if (b->bk->per_tile)
+      for (size_t ri = 0; ri < P.rec.size(); ri++) allrec.push_back(make_int2(c, (int)ri));
     for (size_t ri = 0; ri < P.rec.size(); ri++) {
       const lbm::BRec &r = P.rec[ri];
       specials.push_back(make_int4(c, (int)r.node, (int)ri, (int)r.flags));
@@ -497,6 +528,10 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
   if ((st = balloc(b, &b->d_live_tiles, max_tiles)) != LBM_OK ||
       (st = balloc(b, &b->d_live_n, 2)) != LBM_OK)
     return bail(st);
+  b->nallrec = (int)allrec.size();
+  if ((st = balloc(b, &b->d_allrec, allrec.size())) != LBM_OK) return bail(st);
+  if (!allrec.empty())
+    cudaMemcpy(b->d_allrec, allrec.data(), allrec.size() * sizeof(int2), cudaMemcpyHostToDevice);
   b->nspecial = (int)specials.size();
   if ((st = balloc(b, &b->d_special, specials.size())) != LBM_OK) return bail(st);
   if ((st = balloc(b, &b->d_nspecial, 1)) != LBM_OK) return bail(st);
@@ -692,6 +727,11 @@ lbm_status lbm_batch_get_fields(lbm_batch *b, int32_t c, double *rho, double *u,
   cudaMemcpy((void *)o.rho_solid, rho0.data(), N * 8, cudaMemcpyHostToDevice);
   cudaMemset((void *)o.u_solid, 0, 2 * N * 8);
   void *args[] = {&a, &o};
+  lbm_status ss = launch_side_sync(b);
+  if (ss != LBM_OK) {
+    cudaFree(tmp);
+    return ss;
+  }
   cudaError_t e = cudaLaunchKernel(b->ks->finish[lbm::PH_AB], grid, dim3(128), args, 0, b->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
   if (e == cudaSuccess && rho) e = cudaMemcpy(rho, o.rho, N * 8, cudaMemcpyDeviceToHost);

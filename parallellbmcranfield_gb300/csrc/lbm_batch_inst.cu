@@ -47,6 +47,7 @@ const BatchKernels &LBM_BATCH_FN(LBM_PREC)() {
     fill_batch_steps<LBM_ST, 3>(k.step[3]);
     if (k.per_tile) {
       k.side_fill = (const void *)k_batch_side_fill<LBM_ST>;
+      k.side_sync = (const void *)k_batch_side_sync<LBM_ST>;
       k.special[1] = (const void *)k_batch_special_c<LBM_ST, 1>;
       k.special[2] = (const void *)k_batch_special_c<LBM_ST, 2>;
       k.special[3] = (const void *)k_batch_special_c<LBM_ST, 3>;

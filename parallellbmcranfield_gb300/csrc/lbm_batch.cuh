@@ -205,12 +205,9 @@ static_assert(sizeof(WRec) == 84, "WRec layout");
 // the node-major side array of the current parity (9 values per record,
 // written by the boundary-node pass next to the planes, equal to what a
 // plane read returns: FP16-dev values pass through the storage's rounding),
-// every other read from the planes.  A wall node's own values and its
-// neighbours along the wall then come from a few contiguous sectors instead
-// of one sector per value and row.  In FP32 the plane reads skip AccMain's
-// class check: solid and padding nodes hold 0 in both buffers (zeroed at
-// allocation, written as 0 by the first collision, never written again),
-// the value AccMain returns for them.
+// every other read from the planes as AccMain reads it.  A wall node's own
+// values and its neighbours along the wall then come from a few contiguous
+// sectors instead of one sector per value and row.
 template <class ST>
 struct AccSideB {
   using R = typename ST::R;
@@ -230,12 +227,9 @@ struct AccSideB {
       const int r = nrec[k];
       if (r >= 0) return side[(size_t)r * 9 + k];
     }
-    if constexpr (ST::SHIFT) {
-      if (a.cls[z] == CLS_SOLID) return -wgt<R>(k) * (R)a.rho0;
-      return ST::cvt_dev(__ldg(s + slot_of<PH_AB>(k, z, a)), k, a);
-    } else {
-      return ST::ld(s + slot_of<PH_AB>(k, z, a), k, a);
-    }
+    if (a.cls[z] == CLS_SOLID) return dev ? -wgt<R>(k) * (R)a.rho0 : R(0);
+    const typename ST::T *p = s + slot_of<PH_AB>(k, z, a);
+    return dev ? ST::cvt_dev(__ldg(p), k, a) : ST::ld(p, k, a);
   }
 };
 
@@ -391,11 +385,21 @@ static __global__ void k_batch_advance(int ncases, BatchState s) {
   }
 }
 
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 // du_rel sums of every active case: tiles are 128 positions of one row.
+// Per node and warp the sums are in the storage's arithmetic type (FP32
+// outside FP64 batches: GB300's FP64 rate made FP64 per-node sums the
+// kernel's bound), per block in FP64.
 template <class ST>
 __global__ void __launch_bounds__(128) k_batch_du(const BatchCase *cases, const int4 *rows,
                                                   int nrows, BatchState s) {
   using R = typename ST::R;
+  using A = R;  // per-node and per-warp sums
   __shared__ double sh[2][4];
   for (int t = blockIdx.x; t < nrows; t += gridDim.x) {
     const int4 tl = rows[t];
@@ -404,7 +408,7 @@ __global__ void __launch_bounds__(128) k_batch_du(const BatchCase *cases, const 
     const BatchCase &bc = cases[c];
     const StepArgs &a = bc.args[s.gpar[c] & 1];
     const int x = tl.y * 128 + threadIdx.x, y = tl.z;
-    double du = 0.0, uu = 0.0;
+    A du = A(0), uu = A(0);
     int bad = 0;
     if (x < a.n) {
       const long long node = (long long)y * a.pitch + x;
@@ -412,7 +416,13 @@ __global__ void __launch_bounds__(128) k_batch_du(const BatchCase *cases, const 
       if (cl != CLS_SOLID) {
         AccMain<ST, PH_AB, ST::SHIFT> acc(a, a.src);  // deviations for shifted storage
         R F[9], rho, u, v;
-        if (cl != CLS_SPECIAL) {
+        if (cl == CLS_BULK) {
+          // no boundary links: every source is fluid, plain pulls
+          const typename ST::T *src = (const typename ST::T *)a.src;
+#pragma unroll
+          for (int k = 0; k < 9; k++) F[k] = ld_dev<ST>(src + pull_index<PH_AB>(k, node, a), k, a);
+          moments_form<ST>(F, a, rho, u, v);
+        } else if (cl != CLS_SPECIAL) {
           boundary_F<false, R>(a, acc, node, F);
           moments_form<ST>(F, a, rho, u, v);
         } else {
@@ -423,20 +433,25 @@ __global__ void __launch_bounds__(128) k_batch_du(const BatchCase *cases, const 
           v = mac[2];
         }
         const long long cell = (long long)y * a.n + x;
-        const double pu = bc.uprev[cell], pv = bc.vprev[cell];
-        du = ((double)u - pu) * ((double)u - pu) + ((double)v - pv) * ((double)v - pv);
-        uu = (double)u * u + (double)v * v;
+        const A pu = (A)bc.uprev[cell], pv = (A)bc.vprev[cell];
+        du = ((A)u - pu) * ((A)u - pu) + ((A)v - pv) * ((A)v - pv);
+        uu = (A)u * (A)u + (A)v * (A)v;
         bc.uprev[cell] = (float)u;
         bc.vprev[cell] = (float)v;
         bad = (rho != rho || u != u || v != v);
       }
     }
-    du = warp_sum(du);
-    uu = warp_sum(uu);
+    if constexpr (sizeof(A) == 8) {
+      du = warp_sum(du);
+      uu = warp_sum(uu);
+    } else {
+      du = warp_sum_f(du);
+      uu = warp_sum_f(uu);
+    }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0) {
-      sh[0][wid] = du;
-      sh[1][wid] = uu;
+      sh[0][wid] = (double)du;
+      sh[1][wid] = (double)uu;
     }
     const int anybad = __syncthreads_or(bad);
     if (threadIdx.x == 0) {

@@ -101,3 +101,28 @@ def test_batch_matches_single_contexts_reduced(precision):
         assert err <= 1e-5, (c, err)
         assert np.abs(got["rho"] - want["rho"]).max() <= 1e-6
     b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16dev"])
+def test_batch_outlet_kinds_match_single_contexts(precision):
+    """Channels with each outlet kind (velocity outlet, second-order
+    extrapolation, constant pressure) and a curved cylinder in one batch: the
+    boundary-node pass takes its neighbours from the side arrays or from the
+    planes by kind, the extrapolating outlet takes the full treatment, and
+    every plane another node reads is written; the fields match single
+    contexts as in the cavity batches."""
+    cs = [(G.Mesh.channel(60, 20, [(15.0, 10.4, 4.0)]),
+           dict(BASE, uavg=0.04, viscosity=0.04, inlet_profile=1, outlet_profile=o, rho_out=1.0,
+                collision_model=3))
+          for o in (1, 2, 4)]
+    b = G.Batch(cs, precision=precision)
+    b.set_rest()
+    b.run(60, check_every=20, tol=-1.0)
+    for c, (mesh, params) in enumerate(cs):
+        got = b.fields(c)
+        want = single(mesh, params, G.PRECISIONS[precision], 61)
+        speed = np.sqrt(want["u"] ** 2 + want["v"] ** 2).max()
+        err = np.sqrt((got["u"] - want["u"]) ** 2 + (got["v"] - want["v"]) ** 2).max() / speed
+        assert err <= 1e-5, (c, err)
+        assert np.abs(got["rho"] - want["rho"]).max() <= 1e-6
+    b.close()

@@ -751,7 +751,7 @@ lbm_status gemm(lbm_sg *s, int epi, const bf16 *A, const bf16 *Bt, int M, int N,
   g.bias = bias;
   g.out_bf16 = ob;
   g.out_f32 = of;
-  if (X && s->cfg.products == 0 && splits == 1 &&
+  if (X && s->cfg.products == 0 && splits == 1 && K % 8 == 0 && K <= sgtc::TC_KTAB * 8 &&
       (epi == EPI_BIAS_RELU_BF16 || epi == EPI_BIAS_BF16 || epi == EPI_BF16)) {
     // the implicit-GEMM convolution on tcgen05
     cudaError_t e;

@@ -141,15 +141,17 @@ __device__ __forceinline__ void tm_ld16(uint32_t taddr, float v[16]) {
 }
 
 // Dynamic shared memory of a block: the stages, then the mbarriers and the
-// tensor-memory address (1024-byte aligned base).
+// tensor-memory address (64 bytes), then the convolution's K table (one int
+// per 8 K values, TC_KTAB entries), from a 1024-byte aligned base.
 // Ring depth: 4 stages up to 64 columns (two blocks fit an SM), 3 at 128.
+constexpr int TC_KTAB = 1024;  // K up to 8192
 template <int BN>
 struct TcSmem {
   static constexpr int STAGES = BN >= 128 ? 3 : 4;
   static constexpr int A_BYTES = TC_BM * TC_BK * 2;
   static constexpr int B_BYTES = BN * TC_BK * 2;
   static constexpr int STAGE = A_BYTES + B_BYTES;
-  static constexpr int BYTES = STAGES * STAGE + 64;
+  static constexpr int BYTES = STAGES * STAGE + 64 + TC_KTAB * 4;
   static constexpr int ALLOC = BYTES + 1024;  // room to align the base
 };
 
@@ -268,6 +270,20 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_conv(const bf16 *__restrict__
     px[j] = pin[j] ? pp[j] % W : 0;
     py[j] = pin[j] ? (pp[j] / W) % H : 0;
   }
+  // K table: per 8 K values the tap offsets and the channel, or -1 past K
+  // (no integer divisions in the copy loop)
+  int *ktab = (int *)(sm + TcSmem<BN>::STAGES * TcSmem<BN>::STAGE + 64);
+  for (int j = tid; j < Kp / 8; j += TC_THREADS) {
+    const int k = j * 8;
+    int e = -1;
+    if (k < KC) {
+      const int r = k / C, c = k - r * C;
+      const int dy = taps == 9 ? r / 3 : 1, dx = taps == 9 ? r % 3 : 1;
+      e = (c << 4) | (dy << 2) | dx;
+    }
+    ktab[j] = e;
+  }
+  __syncthreads();
   auto load = [&](uint8_t *sa, uint8_t *sb, int kt) {
     const uint32_t a = saddr(sa), b = saddr(sb);
     const int k0 = kt * TC_BK;
@@ -275,10 +291,10 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_conv(const bf16 *__restrict__
     for (int i = 0; i < 8; i++) {
       const int j = i >> 1, kc = (i & 1) * 4 + l4;
       const int k = k0 + kc * 8;
-      const int r = k / C, c = k - r * C;
-      const int dy = taps == 9 ? r / 3 - 1 : 0, dx = taps == 9 ? r % 3 - 1 : 0;
+      const int e = k < Kp ? ktab[k >> 3] : -1;
+      const int dy = ((e >> 2) & 3) - 1, dx = (e & 3) - 1, c = e >> 4;
       const int yy = py[j] + dy, xx = px[j] + dx;
-      const bool ok = pin[j] && k < KC && yy >= 0 && yy < H && xx >= 0 && xx < W;
+      const bool ok = pin[j] && e >= 0 && yy >= 0 && yy < H && xx >= 0 && xx < W;
       const bf16 *src = ok ? X + ((size_t)(pp[j] + dy * W + dx) * C + c) : X;
       cp16(a + (j * 4 + warp) * 1024 + kc * 128 + r8 * 16, src, ok);
     }
@@ -348,27 +364,53 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_wgrad(const bf16 *__restrict_
   // pixel slots in shared memory).  This thread's pixels of a K tile:
   // (2 warp + h) * 8 + lane / 4 for h = 0, 1.
   const int lane = tid & 31, warp = tid >> 5, l4 = lane & 3, r8 = lane >> 2;
+  // This thread's four K chunks are the same in every K tile (the block's M
+  // rows): their tap offsets and channels once, here.
+  int kdy[4], kdx[4], kc0[4];
+  bool kin[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const int k = m0 + (q * 4 + l4) * 8;
+    const int r = k / C;
+    kin[q] = k < KC;
+    kc0[q] = k - r * C;
+    kdy[q] = taps == 9 ? r / 3 - 1 : 0;
+    kdx[q] = taps == 9 ? r % 3 - 1 : 0;
+  }
+  // pixel coordinates of the two pixels of this thread, advanced by one K
+  // tile (64 pixels) per call: the loads are issued for kt = 0, 1, 2, ...
+  int p[2], px[2], py[2];
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    p[h] = pbeg + (2 * warp + h) * 8 + r8;
+    px[h] = p[h] % W;
+    py[h] = (p[h] / W) % H;
+  }
+  int kt_at = 0;
   auto load = [&](uint8_t *sa, uint8_t *sb, int kt) {
     const uint32_t a = saddr(sa), b = saddr(sb);
-    int p[2], px[2], py[2];
+    while (kt_at < kt) {
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        p[h] += TC_BK;
+        px[h] += TC_BK;
+        while (px[h] >= W) {
+          px[h] -= W;
+          if (++py[h] == H) py[h] = 0;
+        }
+      }
+      kt_at++;
+    }
     bool pin[2];
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-      p[h] = pbeg + kt * TC_BK + (2 * warp + h) * 8 + r8;
-      pin[h] = p[h] < pend;
-      px[h] = pin[h] ? p[h] % W : 0;
-      py[h] = pin[h] ? (p[h] / W) % H : 0;
-    }
+    for (int h = 0; h < 2; h++) pin[h] = p[h] < pend;
     // A: 16 chunks of 8 k values per pixel
 #pragma unroll
     for (int i = 0; i < 8; i++) {
-      const int h = i & 1, kc = (i >> 1) * 4 + l4;
-      const int k = m0 + kc * 8;
-      const int r = k / C, c = k - r * C;
-      const int dy = taps == 9 ? r / 3 - 1 : 0, dx = taps == 9 ? r % 3 - 1 : 0;
-      const int yy = py[h] + dy, xx = px[h] + dx;
-      const bool ok = pin[h] && k < KC && yy >= 0 && yy < H && xx >= 0 && xx < W;
-      const bf16 *src = ok ? X + ((size_t)(p[h] + dy * W + dx) * C + c) : X;
+      const int h = i & 1, q = i >> 1, kc = q * 4 + l4;
+      const int yy = py[h] + kdy[q], xx = px[h] + kdx[q];
+      const bool ok = pin[h] && kin[q] && yy >= 0 && yy < H && xx >= 0 && xx < W;
+      const bf16 *src = ok ? X + ((size_t)(p[h] + kdy[q] * W + kdx[q]) * C + kc0[q]) : X;
       cp16(a + (2 * warp + h) * (TC_BM * 16) + kc * 128 + r8 * 16, src, ok);
     }
     // B: BN / 8 chunks of 8 output channels per pixel

@@ -391,20 +391,22 @@ __device__ __forceinline__ float warp_sum_f(float v) {
   return v;
 }
 
-// du_rel sums of every active case: tiles are 128 positions of one row.
-// Per node and warp the sums are in the storage's arithmetic type (FP32
-// outside FP64 batches: GB300's FP64 rate made FP64 per-node sums the
-// kernel's bound), per block in FP64.
+// du_rel sums of every active case: one block per tile of 128 positions of
+// one row (no persistent loop: the blocks' chains of dependent loads
+// overlap).  Per node and warp the sums are in the storage's arithmetic
+// type (FP32 outside FP64 batches), per block in FP64.
 template <class ST>
 __global__ void __launch_bounds__(128) k_batch_du(const BatchCase *cases, const int4 *rows,
                                                   int nrows, BatchState s) {
   using R = typename ST::R;
   using A = R;  // per-node and per-warp sums
   __shared__ double sh[2][4];
-  for (int t = blockIdx.x; t < nrows; t += gridDim.x) {
+  {
+    const int t = blockIdx.x;
+    if (t >= nrows) return;
     const int4 tl = rows[t];
     const int c = tl.x;
-    if (!s.active[c]) continue;  // uniform per block
+    if (!s.active[c]) return;  // uniform per block
     const BatchCase &bc = cases[c];
     const StepArgs &a = bc.args[s.gpar[c] & 1];
     const int x = tl.y * 128 + threadIdx.x, y = tl.z;

@@ -257,7 +257,7 @@ lbm_status launch_side_sync(lbm_batch *b) {
 lbm_status launch_check(lbm_batch *b, int k, double tol) {
   lbm_status ss = launch_side_sync(b);
   if (ss != LBM_OK) return ss;
-  const int grid = std::min(b->nrows, persistent_blocks(b->bk->du, 128, b->device));
+  const int grid = b->nrows;  // one block per row tile
   void *args[] = {&b->d_cases, &b->d_rows, &b->nrows, &b->s};
   cudaError_t e = cudaLaunchKernel(b->bk->du, dim3(grid), dim3(128), args, 0, b->stream);
   if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch du: ") + cudaGetErrorString(e));

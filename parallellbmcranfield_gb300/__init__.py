@@ -405,6 +405,10 @@ def _load_sg(L):
     return L
 
 
+# tensor-core paths of the network's products (lbm_sg_config.products)
+PRODUCTS = {"tcgen05": 0, "mma": 1, "tcgen05-gather": 2}
+
+
 class Surrogate:
     """The warm-start network (wraps lbm_sg): NHWC float32 arrays on the host."""
 
@@ -412,14 +416,16 @@ class Surrogate:
                  max_batch=8, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8, seed=0, device=0,
                  weight_decay=0.0, coarse_weight=0.0, coarse_block=8, products="tcgen05"):
         """products: "tcgen05" (the convolution products on the 5th-generation
-        tensor cores where the shapes allow) or "mma" (every product on the
-        mma.sync kernels)."""
+        tensor cores where the shapes allow, the TMA-fed halo-tile form for
+        3x3 layers with W a multiple of 128 and C a multiple of 32),
+        "tcgen05-gather" (tcgen05 with the im2col gather only) or "mma" (every
+        product on the mma.sync kernels)."""
         L = self.L = _load_sg(load())
-        if products not in ("tcgen05", "mma"):
-            raise ValueError("products must be 'tcgen05' or 'mma'")
+        if products not in PRODUCTS:
+            raise ValueError("products must be one of " + ", ".join(PRODUCTS))
         self.cfg = lbm_sg_config(height, width, in_channels, out_channels, base, max_batch, lr,
                                  beta1, beta2, eps, seed, device, weight_decay, coarse_weight,
-                                 coarse_block, 0 if products == "tcgen05" else 1)
+                                 coarse_block, PRODUCTS[products])
         self.h = C.c_void_p()
         _check(L.lbm_sg_create(C.byref(self.cfg), C.byref(self.h)), "lbm_sg_create")
         n = C.c_int64()

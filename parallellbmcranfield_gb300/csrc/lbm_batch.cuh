@@ -20,11 +20,16 @@ constexpr int BVAR = 4;
 constexpr int BVAR_BX[BVAR] = {128, 64, 128, 128};
 constexpr int BVAR_NPT[BVAR] = {1, 4, 2, 4};
 
+// Each case's du sums sit in a 128-byte line of their own: the blocks of
+// one check add into them with FP64 atomics, and cases sharing a line would
+// serialise each other's atomics in the L2.
+constexpr int ACC_STRIDE = 16;
+
 struct BatchState {
   int *active;        // 1 while the case still steps
   int *gpar;          // METAF generation parity of each case
   long long *steps;   // iterations completed by each case
-  double *acc;        // per case: sum |du|^2, sum |u|^2
+  double *acc;        // per case: sum |du|^2, sum |u|^2 at [ACC_STRIDE * case + 0, 1]
   int *bad;           // per case: NaN seen
   double *du_last;    // per case: du_rel of the last check
   int *have_prev;     // per case: reference fields valid
@@ -457,8 +462,8 @@ __global__ void __launch_bounds__(128) k_batch_du(const BatchCase *cases, const 
     }
     const int anybad = __syncthreads_or(bad);
     if (threadIdx.x == 0) {
-      atomicAdd(&s.acc[2 * c], sh[0][0] + sh[0][1] + sh[0][2] + sh[0][3]);
-      atomicAdd(&s.acc[2 * c + 1], sh[1][0] + sh[1][1] + sh[1][2] + sh[1][3]);
+      atomicAdd(&s.acc[ACC_STRIDE * c], sh[0][0] + sh[0][1] + sh[0][2] + sh[0][3]);
+      atomicAdd(&s.acc[ACC_STRIDE * c + 1], sh[1][0] + sh[1][1] + sh[1][2] + sh[1][3]);
       if (anybad) s.bad[c] = 1;
     }
     __syncthreads();
@@ -471,8 +476,8 @@ __global__ void __launch_bounds__(128) k_batch_du(const BatchCase *cases, const 
 static __global__ void k_batch_converge(int ncases, BatchState s, double tol, double inv_span) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncases || !s.active[c]) return;
-  const double uu = s.acc[2 * c + 1];
-  const double du = uu > 0 ? sqrt(s.acc[2 * c] / uu) * inv_span : INFINITY;
+  const double uu = s.acc[ACC_STRIDE * c + 1];
+  const double du = uu > 0 ? sqrt(s.acc[ACC_STRIDE * c] / uu) * inv_span : INFINITY;
   s.du_last[c] = s.have_prev[c] ? du : INFINITY;
   if (s.bad[c]) {
     s.active[c] = 0;  // diverged: frozen, reported by the host
@@ -481,8 +486,8 @@ static __global__ void k_batch_converge(int ncases, BatchState s, double tol, do
     s.conv_at[c] = s.steps[c];
   }
   s.have_prev[c] = 1;
-  s.acc[2 * c] = 0.0;
-  s.acc[2 * c + 1] = 0.0;
+  s.acc[ACC_STRIDE * c] = 0.0;
+  s.acc[ACC_STRIDE * c + 1] = 0.0;
 }
 
 struct BatchKernels {

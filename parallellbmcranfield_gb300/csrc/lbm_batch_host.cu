@@ -133,7 +133,7 @@ lbm_status reset_state(lbm_batch *b) {
   LBM_BCK(cudaMemcpyAsync(b->s.active, ones.data(), b->nc * sizeof(int), cudaMemcpyHostToDevice, b->stream));
   LBM_BCK(cudaMemsetAsync(b->s.gpar, 0, b->nc * sizeof(int), b->stream));
   LBM_BCK(cudaMemsetAsync(b->s.steps, 0, b->nc * sizeof(long long), b->stream));
-  LBM_BCK(cudaMemsetAsync(b->s.acc, 0, 2 * b->nc * sizeof(double), b->stream));
+  LBM_BCK(cudaMemsetAsync(b->s.acc, 0, (size_t)lbm::ACC_STRIDE * b->nc * sizeof(double), b->stream));
   LBM_BCK(cudaMemsetAsync(b->s.bad, 0, b->nc * sizeof(int), b->stream));
   LBM_BCK(cudaMemsetAsync(b->s.du_last, 0, b->nc * sizeof(double), b->stream));
   LBM_BCK(cudaMemsetAsync(b->s.have_prev, 0, b->nc * sizeof(int), b->stream));
@@ -543,7 +543,7 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
   cudaMemcpy(b->d_rows, rows.data(), rows.size() * sizeof(int4), cudaMemcpyHostToDevice);
   lbm::BatchState &s = b->s;
   if ((st = balloc(b, &s.active, ncases)) != LBM_OK || (st = balloc(b, &s.gpar, ncases)) != LBM_OK ||
-      (st = balloc(b, &s.steps, ncases)) != LBM_OK || (st = balloc(b, &s.acc, 2 * ncases)) != LBM_OK ||
+      (st = balloc(b, &s.steps, ncases)) != LBM_OK || (st = balloc(b, &s.acc, (size_t)lbm::ACC_STRIDE * ncases)) != LBM_OK ||
       (st = balloc(b, &s.bad, ncases)) != LBM_OK || (st = balloc(b, &s.du_last, ncases)) != LBM_OK ||
       (st = balloc(b, &s.have_prev, ncases)) != LBM_OK ||
       (st = balloc(b, &s.conv_at, ncases)) != LBM_OK)

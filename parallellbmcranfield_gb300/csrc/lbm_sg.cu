@@ -12,6 +12,7 @@
 //   input grad    dX[p][ci]  = sum_k A'[p][k] Wd[ci][k],  A' = im2col(dZ), Wd = flipped W
 //   weight grad   dW[co][k]  = sum_p dZ[p][co] A[p][k]   (split-K over p, FP32 atomics)
 // The GEMM kernel takes both operands K-contiguous (A[M][K], Bt[N][K]).
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -701,9 +702,75 @@ cudaError_t tc_conv_launch(lbm_sg *s, const bf16 *X, int P, int H, int W, int C,
   return cudaGetLastError();
 }
 
+// cuTensorMapEncodeTiled from the driver (resolved once; null if absent).
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return (EncodeTiledFn) nullptr;
+    return (EncodeTiledFn)p;
+  }();
+  return fn;
+}
+
+// The halo-tile tcgen05 convolution (k_tc_conv3h): 3x3, W a multiple of 128,
+// C a multiple of 32, N = BN.  Returns false (nothing launched) when the
+// tensor maps cannot be encoded, so the caller takes the gather kernel.
+template <int EPI, int BN>
+bool tc_conv3h(lbm_sg *s, const bf16 *X, int P, int H, int W, int C, const bf16 *Bt, int Kp,
+               const float *bias, bf16 *out, cudaError_t *err) {
+  using T = sgtc::TcHalo<BN>;
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc || ((uintptr_t)X & 15) || ((uintptr_t)Bt & 15)) return false;
+  const int imgs = P / (H * W);
+  CUtensorMap ma, mb;
+  const cuuint64_t da[5] = {8, (cuuint64_t)W, (cuuint64_t)(C / 8), (cuuint64_t)H, (cuuint64_t)imgs};
+  const cuuint64_t sa[4] = {(cuuint64_t)C * 2, 16, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+  const cuuint32_t ba[5] = {8, 130, 4, 3, 1}, ea[5] = {1, 1, 1, 1, 1};
+  const cuuint64_t db[4] = {8, (cuuint64_t)BN, (cuuint64_t)(C / 8), 9};
+  const cuuint64_t sb[3] = {(cuuint64_t)Kp * 2, 16, (cuuint64_t)C * 2};
+  const cuuint32_t bb[4] = {8, (cuuint32_t)BN, 4, 9}, eb[4] = {1, 1, 1, 1};
+  if (enc(&ma, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, (void *)X, da, sa, ba, ea,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS ||
+      enc(&mb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)Bt, db, sb, bb, eb,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  static bool attr = false;
+  if (!attr) {
+    *err = cudaFuncSetAttribute(sgtc::k_tc_conv3h<EPI, BN>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, T::bytes(2));
+    if (*err != cudaSuccess) return true;
+    attr = true;
+  }
+  const int S = C / 32 >= 2 ? 2 : 1;
+  dim3 grid((unsigned)(W / sgtc::TC_BM), (unsigned)H, (unsigned)imgs);
+  sgtc::k_tc_conv3h<EPI, BN><<<grid, sgtc::TC_THREADS, T::bytes(S), s->stream>>>(
+      ma, mb, H, W, C, BN, S, bias, out, s->d_err);
+  *err = cudaGetLastError();
+  return true;
+}
+
 template <int EPI>
 cudaError_t tc_conv(lbm_sg *s, const bf16 *X, int P, int H, int W, int C, int taps,
                     const bf16 *Bt, int N, int Kp, const float *bias, bf16 *out) {
+  if (taps == 9 && W % sgtc::TC_BM == 0 && C % 32 == 0 && Kp >= 9 * C && Kp % 8 == 0 &&
+      P % (H * W) == 0 && s->cfg.products == 0) {
+    cudaError_t e = cudaSuccess;
+    bool done = false;
+    if (N == 32) done = tc_conv3h<EPI, 32>(s, X, P, H, W, C, Bt, Kp, bias, out, &e);
+    else if (N == 64) done = tc_conv3h<EPI, 64>(s, X, P, H, W, C, Bt, Kp, bias, out, &e);
+    else if (N == 128) done = tc_conv3h<EPI, 128>(s, X, P, H, W, C, Bt, Kp, bias, out, &e);
+    if (done) return e;
+  }
   if (N <= 32) return tc_conv_launch<EPI, 32>(s, X, P, H, W, C, taps, Bt, N, Kp, bias, out);
   if (N <= 64) return tc_conv_launch<EPI, 64>(s, X, P, H, W, C, taps, Bt, N, Kp, bias, out);
   return tc_conv_launch<EPI, 128>(s, X, P, H, W, C, taps, Bt, N, Kp, bias, out);
@@ -751,7 +818,7 @@ lbm_status gemm(lbm_sg *s, int epi, const bf16 *A, const bf16 *Bt, int M, int N,
   g.bias = bias;
   g.out_bf16 = ob;
   g.out_f32 = of;
-  if (X && s->cfg.products == 0 && splits == 1 && K % 8 == 0 && K <= sgtc::TC_KTAB * 8 &&
+  if (X && s->cfg.products != 1 && splits == 1 && K % 8 == 0 && K <= sgtc::TC_KTAB * 8 &&
       (epi == EPI_BIAS_RELU_BF16 || epi == EPI_BIAS_BF16 || epi == EPI_BF16)) {
     // the implicit-GEMM convolution on tcgen05
     cudaError_t e;
@@ -832,7 +899,7 @@ lbm_status conv_bwd(lbm_sg *s, int li, int xi, int yi, int B, bool need_dx) {
     k_bias_grad<<<grid_for((size_t)M), 256, 0, s->stream>>>(Y.dx, s->g + c.boff, (size_t)M, c.cout);
   }
   lbm_status st = LBM_OK;
-  if (X.c % 8 == 0 && c.cout % 8 == 0 && s->cfg.products == 0) {
+  if (X.c % 8 == 0 && c.cout % 8 == 0 && s->cfg.products != 1) {
     cudaError_t e;
     if (c.cout <= 32)
       e = tc_wgrad_launch<32>(s, Y.dx, X.x, M, X.h, X.w, X.c, c.taps, c.cout, s->g + c.woff, c.Kp);
@@ -1074,8 +1141,9 @@ lbm_status lbm_sg_create(const lbm_sg_config *cfg, lbm_sg **out) {
       (st = salloc(s, &s->msk, P)) || (st = salloc(s, &s->xin, P * ci)) ||
       (st = salloc(s, &s->yout, P * co)) || (st = salloc(s, &s->loss, 3)))
     return bail(st);
-  if (cfg->products != 0 && cfg->products != 1)
-    return bail(fail(LBM_INVALID, "surrogate: products must be 0 (tcgen05) or 1 (mma.sync)"));
+  if (cfg->products < 0 || cfg->products > 2)
+    return bail(fail(LBM_INVALID,
+                     "surrogate: products must be 0 (tcgen05), 1 (mma.sync) or 2 (tcgen05, gather only)"));
   if ((st = salloc(s, &s->d_err, 1)) != LBM_OK) return bail(st);
   cudaMemset(s->d_err, 0, sizeof(int));
   if (cfg->coarse_weight > 0.f) {

@@ -30,6 +30,7 @@
 // (R = rows of the tile.)  Tensor memory holds D with row i of the tile in
 // lane i and column j in column j; warp w reads lanes 32w..32w+31.
 #pragma once
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -138,6 +139,30 @@ __device__ __forceinline__ void tm_ld16(uint32_t taddr, float v[16]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 #pragma unroll
   for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// TMA: the mbarrier expects `bytes` more (this thread's arrival included);
+// tiled tensor loads of 4 and 5 dimensions completing on that mbarrier.
+__device__ __forceinline__ void mb_expect_tx(uint64_t *b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(saddr(b)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, uint64_t *bar,
+                                            int c0, int c1, int c2, int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%3, %4, %5, %6}], [%2];\n" ::"r"(dst),
+      "l"((uint64_t)map), "r"(saddr(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap *map, uint64_t *bar,
+                                            int c0, int c1, int c2, int c3, int c4) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%3, %4, %5, %6, %7}], [%2];\n" ::"r"(dst),
+      "l"((uint64_t)map), "r"(saddr(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4)
+      : "memory");
 }
 
 // Dynamic shared memory of a block: the stages, then the mbarriers and the
@@ -443,6 +468,138 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_wgrad(const bf16 *__restrict_
     }
   }
   tc_teardown<BN>(tmem);
+}
+
+// 3x3 convolution (pad 1) of an NHWC tensor with W a multiple of 128 and C a
+// multiple of 32, N = BN outputs: the halo-tile form.  A block computes 128
+// consecutive pixels of one image row.  Per 32-channel chunk one TMA load
+// stages the halo -- rows y-1..y+1, pixels x0-1..x0+128, 4 groups of 8
+// channels, zero outside the image -- as [row][group][pixel][8 channels]
+// (16 bytes per pixel, so a one-pixel shift is a 16-byte shift of the
+// descriptor's start address), and one TMA load stages the weights of all
+// nine taps as [tap][group][output][8 channels].  The nine taps are then
+// MMAs on offsets of the same halo: every input pixel crosses from L2 once
+// per chunk instead of nine times.  Tensor maps (built by the host):
+//   mapA: dims (8, W, C/8, H, images), strides (C*2, 16, W*C*2, H*W*C*2),
+//         box (8, 130, 4, 3, 1)
+//   mapB: dims (8, N, C/8, 9), strides (Kp*2, 16, C*2), box (8, BN, 4, 9)
+// S stages (1 or 2) of TcHalo<BN>::STAGE bytes; thread 0 issues the loads
+// and the MMAs, every wait is bounded.
+constexpr int TH_A_BYTES = 8 * 130 * 4 * 3 * 2;  // 24960
+constexpr int TH_A_SLOT = 25600;                  // rounded up to 1024
+template <int BN>
+struct TcHalo {
+  static constexpr int B_BYTES = 8 * BN * 4 * 9 * 2;
+  static constexpr int STAGE = TH_A_SLOT + B_BYTES;
+  static constexpr int bytes(int stages) { return stages * STAGE + 64 + 1024; }
+};
+
+template <int EPI, int BN>
+__global__ void __launch_bounds__(TC_THREADS) k_tc_conv3h(const __grid_constant__ CUtensorMap mapA,
+                                                          const __grid_constant__ CUtensorMap mapB,
+                                                          int H, int W, int C, int N, int S,
+                                                          const float *__restrict__ bias,
+                                                          bf16 *__restrict__ out, int *err) {
+  using T = TcHalo<BN>;
+  uint8_t *sm = tc_smem_base();
+  uint64_t *bars = (uint64_t *)(sm + S * T::STAGE);  // full[2], empty[2], done
+  uint64_t *full = bars, *empty = bars + 2, *done = bars + 4;
+  uint32_t *slot = (uint32_t *)(bars + 5);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int x0 = blockIdx.x * TC_BM, y = blockIdx.y, img = blockIdx.z;
+  const int nch = C / 32;
+  if (tid == 0) {
+    for (int i = 0; i < 5; i++) mb_init(&bars[i], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    fence_async_smem();
+  }
+  __syncwarp();
+  if (tid < 32) tm_alloc(slot, BN < 32 ? 32 : BN);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *slot;
+  bool ok = true;
+  if (tid == 0) {
+    const uint32_t idesc = tc_idesc(BN, 0, 0);
+    int issued = 0, consumed = 0;  // chunks whose loads were issued / have landed
+    auto issue = [&](int kc, int st) {
+      const uint32_t a = saddr(sm + st * T::STAGE), b = a + TH_A_SLOT;
+      mb_expect_tx(&full[st], TH_A_BYTES + T::B_BYTES);
+      tma_load_5d(a, &mapA, &full[st], 0, x0 - 1, kc * 4, y - 1, img);
+      tma_load_4d(b, &mapB, &full[st], 0, 0, kc * 4, 0);
+      issued = kc + 1;
+    };
+    for (int i = 0; i < S && i < nch; i++) issue(i, i);
+    for (int kc = 0; kc < nch && ok; kc++) {
+      const int st = kc % S;
+      const uint32_t ph = (uint32_t)(kc / S) & 1u;
+      if (!mb_wait(&full[st], ph)) {
+        ok = false;
+        break;
+      }
+      consumed = kc + 1;
+      tc_fence_after();
+      const uint32_t a = saddr(sm + st * T::STAGE), b = a + TH_A_SLOT;
+#pragma unroll
+      for (int tap = 0; tap < 9; tap++) {
+        const int dy = tap / 3, dx = tap % 3;  // offsets + 1
+#pragma unroll
+        for (int k2 = 0; k2 < 2; k2++) {
+          const uint32_t ad = a + dy * (4 * 2080) + (2 * k2) * 2080 + dx * 16;
+          const uint32_t bd = b + tap * (4 * BN * 16) + (2 * k2) * (BN * 16);
+          tc_mma(tmem, tc_desc(ad, 2080, 128), tc_desc(bd, BN * 16, 128), idesc,
+                 (kc | tap | k2) != 0);
+        }
+      }
+      tc_commit(&empty[st]);
+      if (kc + S < nch) {
+        if (!mb_wait(&empty[st], ph)) {
+          ok = false;
+          break;
+        }
+        issue(kc + S, st);
+      }
+    }
+    tc_commit(done);  // arrives when every MMA issued above is complete
+    if (!ok) {
+      // loads still in flight land in this block's shared memory: wait for
+      // them (bounded) before the block may exit
+      for (int kc = consumed; kc < issued; kc++) mb_wait(&full[kc % S], (uint32_t)(kc / S) & 1u);
+    }
+  }
+  if (!mb_wait(done, 0)) ok = false;
+  ok = __syncthreads_and(ok) != 0;
+  __syncwarp();
+  tc_fence_after();
+  if (!ok) {
+    if (tid == 0) atomicExch(err, 1);
+  } else {
+    const long long p = ((long long)img * H + y) * W + x0 + warp * 32 + lane;
+#pragma unroll
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+      float v[16];
+      tm_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
+#pragma unroll
+      for (int j = 0; j < 16; j += 2) {
+        const int n = c0 + j;
+        float v0 = v[j], v1 = v[j + 1];
+        if (EPI != TC_PLAIN) {
+          v0 += bias[n];
+          v1 += bias[n + 1];
+        }
+        if (EPI == TC_BIAS_RELU) {
+          v0 = fmaxf(v0, 0.f);
+          v1 = fmaxf(v1, 0.f);
+        }
+        *(__nv_bfloat162 *)(out + p * N + n) = __floats2bfloat162_rn(v0, v1);
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  __syncwarp();
+  if (tid < 32) tm_free(tmem, BN < 32 ? 32 : BN);
 }
 
 }  // namespace sgtc

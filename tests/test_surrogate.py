@@ -279,21 +279,26 @@ def test_gap_flow_of_an_empty_channel_is_the_inlet_parabola():
 
 
 @pytest.mark.gpu
-def test_tcgen05_and_mma_products_agree():
-    """Both product paths on a 64 x 64 batch at base width 32 (every tile width
-    32, 64, 128 and several K tiles): forward outputs and gradients agree to
-    the BF16 rounding of the activations."""
+@pytest.mark.parametrize("tc", ["tcgen05", "tcgen05-gather"])
+@pytest.mark.parametrize("h,B", [(64, 2), (256, 1)])
+def test_tcgen05_and_mma_products_agree(tc, h, B):
+    """The tcgen05 product paths against mma.sync at base width 32: at 64 x 64
+    every layer takes the im2col gather (tile widths 32, 64, 128, several K
+    tiles); at 256 x 256 the 3x3 layers of levels 0 and 1 (W 256 and 128, C a
+    multiple of 32, N 32 or 64) take the TMA-fed halo-tile form with
+    "tcgen05", the gather with "tcgen05-gather".  Forward outputs and
+    gradients agree to the BF16 rounding of the activations."""
     import parallellbmcranfield_gb300 as G
 
-    x, t, m = sample(seed=9, B=2, h=64, cin=8)
+    x, t, m = sample(seed=9, B=B, h=h, cin=8)
     out = {}
-    for products in ("tcgen05", "mma"):
-        s = G.Surrogate(height=64, width=64, in_channels=8, out_channels=COUT, base=32,
-                        max_batch=2, seed=11, products=products)
+    for products in (tc, "mma"):
+        s = G.Surrogate(height=h, width=h, in_channels=8, out_channels=COUT, base=32,
+                        max_batch=B, seed=11, products=products)
         loss, g = s.loss_grads(x, t, m)
         out[products] = (s.forward(x), loss, g)
         s.close()
-    (ya, la, ga), (yb, lb, gb) = out["tcgen05"], out["mma"]
+    (ya, la, ga), (yb, lb, gb) = out[tc], out["mma"]
     assert np.abs(ya - yb).max() <= 1e-2 * np.abs(yb).max()
     assert abs(la - lb) <= 1e-2 * lb
     assert np.linalg.norm(ga - gb) <= 3e-2 * np.linalg.norm(gb)

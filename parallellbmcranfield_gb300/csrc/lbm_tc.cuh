@@ -265,6 +265,52 @@ __device__ __forceinline__ uint8_t *tc_smem_base() {
 
 enum TcEpi : int { TC_BIAS_RELU = 0, TC_BIAS = 1, TC_PLAIN = 2 };
 
+// Epilogue through shared memory: each warp's 32 rows of the accumulator tile
+// (tcgen05.ld), bias / ReLU, BF16, into `tile` (rows of BN * 2 + 16 bytes,
+// freed stage memory), then 16-byte copies of whole row segments to
+// out[row][n0 .. n0 + BN) (row length N): consecutive threads write
+// consecutive 16 bytes instead of each thread writing 4 bytes of its own row.
+// Needs N and n0 multiples of 8 and a 16-byte aligned `out`.
+template <int EPI, int BN>
+__device__ __forceinline__ void tc_epilogue_tile(uint32_t tmem, uint8_t *tile, long long row0,
+                                                 int rows, int N, int n0,
+                                                 const float *__restrict__ bias,
+                                                 bf16 *__restrict__ out) {
+  constexpr int RS = BN * 2 + 16;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  uint8_t *mine = tile + (warp * 32 + lane) * RS;
+#pragma unroll
+  for (int c0 = 0; c0 < BN; c0 += 16) {
+    float v[16];
+    tm_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
+    uint32_t w[8];
+#pragma unroll
+    for (int j = 0; j < 16; j += 2) {
+      const int n = n0 + c0 + j;
+      float v0 = v[j], v1 = v[j + 1];
+      if (EPI != TC_PLAIN) {
+        if (n < N) v0 += bias[n];
+        if (n + 1 < N) v1 += bias[n + 1];
+      }
+      if (EPI == TC_BIAS_RELU) {
+        v0 = fmaxf(v0, 0.f);
+        v1 = fmaxf(v1, 0.f);
+      }
+      const __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
+      memcpy(&w[j / 2], &h, 4);
+    }
+    *(uint4 *)(mine + c0 * 2) = make_uint4(w[0], w[1], w[2], w[3]);
+    *(uint4 *)(mine + c0 * 2 + 16) = make_uint4(w[4], w[5], w[6], w[7]);
+  }
+  __syncthreads();
+  constexpr int CPR = BN * 2 / 16;  // 16-byte chunks per row
+  for (int i = tid; i < TC_BM * CPR; i += TC_THREADS) {
+    const int r = i / CPR, ch = i - r * CPR;
+    if (r < rows && n0 + ch * 8 < N)
+      *(uint4 *)(out + (row0 + r) * N + n0 + ch * 8) = *(const uint4 *)(tile + r * RS + ch * 16);
+  }
+}
+
 // Convolution as C[p][n] = im2col(X)[p][k] Bt[n][k]: X is [P][H][W][C] BF16
 // (C a multiple of 8: a 16-byte chunk never straddles two taps), taps 9
 // (3x3, pad 1) or 1, k = tap*C + c < taps*C, Bt is [N][Kp] (rows of Kp
@@ -335,7 +381,10 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_conv(const bf16 *__restrict__
   };
   const bool ok = tc_mainloop<BN>(sm, tmem, nk, tc_idesc(BN, 0, 0), 128, 1024, 256, 128, 1024, 256,
                                   load, err);
-  if (ok) {
+  if (ok && (N & 7) == 0 && ((uintptr_t)out & 15) == 0) {
+    // the stages are free: the main loop waited for every copy and MMA
+    tc_epilogue_tile<EPI, BN>(tmem, sm, m0, min(TC_BM, P - m0), N, n0, bias, out);
+  } else if (ok) {
     const int row = m0 + warp * 32 + lane;
 #pragma unroll
     for (int c0 = 0; c0 < BN; c0 += 16) {
@@ -575,26 +624,8 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_conv3h(const __grid_constant_
   if (!ok) {
     if (tid == 0) atomicExch(err, 1);
   } else {
-    const long long p = ((long long)img * H + y) * W + x0 + warp * 32 + lane;
-#pragma unroll
-    for (int c0 = 0; c0 < BN; c0 += 16) {
-      float v[16];
-      tm_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
-#pragma unroll
-      for (int j = 0; j < 16; j += 2) {
-        const int n = c0 + j;
-        float v0 = v[j], v1 = v[j + 1];
-        if (EPI != TC_PLAIN) {
-          v0 += bias[n];
-          v1 += bias[n + 1];
-        }
-        if (EPI == TC_BIAS_RELU) {
-          v0 = fmaxf(v0, 0.f);
-          v1 = fmaxf(v1, 0.f);
-        }
-        *(__nv_bfloat162 *)(out + p * N + n) = __floats2bfloat162_rn(v0, v1);
-      }
-    }
+    // the stages are free: every MMA has completed and every load landed
+    tc_epilogue_tile<EPI, BN>(tmem, sm, ((long long)img * H + y) * W + x0, TC_BM, N, 0, bias, out);
   }
   tc_fence_before();
   __syncthreads();

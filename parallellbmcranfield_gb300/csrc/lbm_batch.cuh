@@ -20,16 +20,12 @@ constexpr int BVAR = 4;
 constexpr int BVAR_BX[BVAR] = {128, 64, 128, 128};
 constexpr int BVAR_NPT[BVAR] = {1, 4, 2, 4};
 
-// Each case's du sums sit in a 128-byte line of their own: the blocks of
-// one check add into them with FP64 atomics, and cases sharing a line would
-// serialise each other's atomics in the L2.
-constexpr int ACC_STRIDE = 16;
-
 struct BatchState {
   int *active;        // 1 while the case still steps
   int *gpar;          // METAF generation parity of each case
   long long *steps;   // iterations completed by each case
-  double *acc;        // per case: sum |du|^2, sum |u|^2 at [ACC_STRIDE * case + 0, 1]
+  double2 *part;      // per row tile of the last check: sum |du|^2, sum |u|^2
+  const int *rbeg;    // row tiles of case c: [rbeg[c], rbeg[c + 1])
   int *bad;           // per case: NaN seen
   double *du_last;    // per case: du_rel of the last check
   int *have_prev;     // per case: reference fields valid
@@ -462,22 +458,32 @@ __global__ void __launch_bounds__(128) k_batch_du(const BatchCase *cases, const 
     }
     const int anybad = __syncthreads_or(bad);
     if (threadIdx.x == 0) {
-      atomicAdd(&s.acc[ACC_STRIDE * c], sh[0][0] + sh[0][1] + sh[0][2] + sh[0][3]);
-      atomicAdd(&s.acc[ACC_STRIDE * c + 1], sh[1][0] + sh[1][1] + sh[1][2] + sh[1][3]);
+      s.part[t] = make_double2(sh[0][0] + sh[0][1] + sh[0][2] + sh[0][3],
+                               sh[1][0] + sh[1][1] + sh[1][2] + sh[1][3]);
       if (anybad) s.bad[c] = 1;
     }
     __syncthreads();
   }
 }
 
-// Per-case convergence decision after k_batch_du.  du_rel is the relative
-// change per step: ||(u,v) - (u,v)_prev|| / ||(u,v)|| over the check interval,
-// times inv_span = 1 / (steps in the interval).
+// Per-case convergence decision after k_batch_du, one warp per case summing
+// its row tiles' partial sums in a fixed order (the result does not depend on
+// block scheduling).  du_rel is the relative change per step:
+// ||(u,v) - (u,v)_prev|| / ||(u,v)|| over the check interval, times
+// inv_span = 1 / (steps in the interval).
 static __global__ void k_batch_converge(int ncases, BatchState s, double tol, double inv_span) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncases || !s.active[c]) return;
-  const double uu = s.acc[ACC_STRIDE * c + 1];
-  const double du = uu > 0 ? sqrt(s.acc[ACC_STRIDE * c] / uu) * inv_span : INFINITY;
+  const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (c >= ncases || !s.active[c]) return;  // uniform per warp
+  double a0 = 0.0, a1 = 0.0;
+  for (int r = s.rbeg[c] + lane; r < s.rbeg[c + 1]; r += 32) {
+    const double2 q = s.part[r];
+    a0 += q.x;
+    a1 += q.y;
+  }
+  a0 = warp_sum(a0);
+  a1 = warp_sum(a1);
+  if (lane != 0) return;
+  const double du = a1 > 0 ? sqrt(a0 / a1) * inv_span : INFINITY;
   s.du_last[c] = s.have_prev[c] ? du : INFINITY;
   if (s.bad[c]) {
     s.active[c] = 0;  // diverged: frozen, reported by the host
@@ -486,8 +492,6 @@ static __global__ void k_batch_converge(int ncases, BatchState s, double tol, do
     s.conv_at[c] = s.steps[c];
   }
   s.have_prev[c] = 1;
-  s.acc[ACC_STRIDE * c] = 0.0;
-  s.acc[ACC_STRIDE * c + 1] = 0.0;
 }
 
 struct BatchKernels {

@@ -133,7 +133,6 @@ lbm_status reset_state(lbm_batch *b) {
   LBM_BCK(cudaMemcpyAsync(b->s.active, ones.data(), b->nc * sizeof(int), cudaMemcpyHostToDevice, b->stream));
   LBM_BCK(cudaMemsetAsync(b->s.gpar, 0, b->nc * sizeof(int), b->stream));
   LBM_BCK(cudaMemsetAsync(b->s.steps, 0, b->nc * sizeof(long long), b->stream));
-  LBM_BCK(cudaMemsetAsync(b->s.acc, 0, (size_t)lbm::ACC_STRIDE * b->nc * sizeof(double), b->stream));
   LBM_BCK(cudaMemsetAsync(b->s.bad, 0, b->nc * sizeof(int), b->stream));
   LBM_BCK(cudaMemsetAsync(b->s.du_last, 0, b->nc * sizeof(double), b->stream));
   LBM_BCK(cudaMemsetAsync(b->s.have_prev, 0, b->nc * sizeof(int), b->stream));
@@ -263,7 +262,8 @@ lbm_status launch_check(lbm_batch *b, int k, double tol) {
   if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch du: ") + cudaGetErrorString(e));
   double inv_span = 1.0 / k;
   void *cargs[] = {&b->nc, &b->s, &tol, &inv_span};
-  e = cudaLaunchKernel(b->bk->converge, dim3((b->nc + 255) / 256), dim3(256), cargs, 0, b->stream);
+  e = cudaLaunchKernel(b->bk->converge, dim3((unsigned)((b->nc * 32 + 255) / 256)), dim3(256), cargs,
+                       0, b->stream);
   if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch converge: ") + cudaGetErrorString(e));
   return LBM_OK;
 }
@@ -339,6 +339,7 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
   std::vector<std::vector<int4>> tiles(lbm::BVAR);
   std::vector<int4> rows;
   std::vector<int4> specials;
+  std::vector<int> rbeg;  // first row tile of each case (then the total)
   std::vector<int2> allrec;  // (case, record) of every boundary record (per-tile kinds)
   std::vector<uint32_t> special_key;
   const size_t es = (size_t)b->ks->elem_size;
@@ -452,6 +453,7 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
       for (int by = 0; by < (P.m + npt - 1) / npt; by++)
         for (int tx = 0; tx < (P.n + bx - 1) / bx; tx++) tiles[v].push_back(make_int4(c, tx, by, 0));
     }
+    rbeg.push_back((int)rows.size());
     for (int y = 0; y < P.m; y++)
       for (int tx = 0; tx < (P.n + 127) / 128; tx++) rows.push_back(make_int4(c, tx, y, 0));
     if (b->bk->per_tile)
@@ -541,9 +543,18 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
   b->nrows = (int)rows.size();
   if ((st = balloc(b, &b->d_rows, rows.size())) != LBM_OK) return bail(st);
   cudaMemcpy(b->d_rows, rows.data(), rows.size() * sizeof(int4), cudaMemcpyHostToDevice);
+  rbeg.push_back((int)rows.size());
+  {
+    int *d_rbeg = nullptr;
+    if ((st = balloc(b, &d_rbeg, rbeg.size())) != LBM_OK ||
+        (st = balloc(b, &b->s.part, rows.size())) != LBM_OK)
+      return bail(st);
+    cudaMemcpy(d_rbeg, rbeg.data(), rbeg.size() * sizeof(int), cudaMemcpyHostToDevice);
+    b->s.rbeg = d_rbeg;
+  }
   lbm::BatchState &s = b->s;
   if ((st = balloc(b, &s.active, ncases)) != LBM_OK || (st = balloc(b, &s.gpar, ncases)) != LBM_OK ||
-      (st = balloc(b, &s.steps, ncases)) != LBM_OK || (st = balloc(b, &s.acc, (size_t)lbm::ACC_STRIDE * ncases)) != LBM_OK ||
+      (st = balloc(b, &s.steps, ncases)) != LBM_OK ||
       (st = balloc(b, &s.bad, ncases)) != LBM_OK || (st = balloc(b, &s.du_last, ncases)) != LBM_OK ||
       (st = balloc(b, &s.have_prev, ncases)) != LBM_OK ||
       (st = balloc(b, &s.conv_at, ncases)) != LBM_OK)

@@ -393,9 +393,10 @@ __device__ __forceinline__ float warp_sum_f(float v) {
 }
 
 // du_rel sums of every active case: one block per tile of 128 positions of
-// one row (no persistent loop: the blocks' chains of dependent loads
-// overlap).  Per node and warp the sums are in the storage's arithmetic
-// type (FP32 outside FP64 batches), per block in FP64.
+// one row.  The velocity of a node is that of its post-collision METAF (the
+// state the next step streams).  Per node and warp the sums are in the
+// storage's arithmetic type (FP32 outside FP64 batches), per block in FP64,
+// per case in k_batch_converge.
 template <class ST>
 __global__ void __launch_bounds__(128) k_batch_du(const BatchCase *cases, const int4 *rows,
                                                   int nrows, BatchState s) {
@@ -417,24 +418,15 @@ __global__ void __launch_bounds__(128) k_batch_du(const BatchCase *cases, const 
       const long long node = (long long)y * a.pitch + x;
       const uint8_t cl = a.cls[node];
       if (cl != CLS_SOLID) {
-        AccMain<ST, PH_AB, ST::SHIFT> acc(a, a.src);  // deviations for shifted storage
+        // The node's own post-collision METAF: the collision conserves rho
+        // and j, so their moments are the macroscopic fields of the step
+        // just taken, read without streaming or boundary treatment (nine
+        // coalesced loads; the planes are complete after k_batch_side_sync).
+        const typename ST::T *src = (const typename ST::T *)a.src;
         R F[9], rho, u, v;
-        if (cl == CLS_BULK) {
-          // no boundary links: every source is fluid, plain pulls
-          const typename ST::T *src = (const typename ST::T *)a.src;
 #pragma unroll
-          for (int k = 0; k < 9; k++) F[k] = ld_dev<ST>(src + pull_index<PH_AB>(k, node, a), k, a);
-          moments_form<ST>(F, a, rho, u, v);
-        } else if (cl != CLS_SPECIAL) {
-          boundary_F<false, R>(a, acc, node, F);
-          moments_form<ST>(F, a, rho, u, v);
-        } else {
-          R mac[3];
-          special_node<R>(a, acc, node, F, mac);
-          rho = mac[0];
-          u = mac[1];
-          v = mac[2];
-        }
+        for (int k = 0; k < 9; k++) F[k] = ld_dev<ST>(src + slot_of<PH_AB>(k, node, a), k, a);
+        moments_form<ST>(F, a, rho, u, v);
         const long long cell = (long long)y * a.n + x;
         const A pu = (A)bc.uprev[cell], pv = (A)bc.vprev[cell];
         du = ((A)u - pu) * ((A)u - pu) + ((A)v - pv) * ((A)v - pv);

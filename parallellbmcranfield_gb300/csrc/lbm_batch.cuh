@@ -20,6 +20,8 @@ constexpr int BVAR = 4;
 constexpr int BVAR_BX[BVAR] = {128, 64, 128, 128};
 constexpr int BVAR_NPT[BVAR] = {1, 4, 2, 4};
 
+constexpr int DU_NPT = 4;  // rows per thread of the du check
+
 struct BatchState {
   int *active;        // 1 while the case still steps
   int *gpar;          // METAF generation parity of each case
@@ -393,7 +395,7 @@ __device__ __forceinline__ float warp_sum_f(float v) {
 }
 
 // du_rel sums of every active case: one block per tile of 128 positions of
-// one row.  The velocity of a node is that of its post-collision METAF (the
+// DU_NPT rows.  The velocity of a node is that of its post-collision METAF (the
 // state the next step streams).  Per node and warp the sums are in the
 // storage's arithmetic type (FP32 outside FP64 batches), per block in FP64,
 // per case in k_batch_converge.
@@ -401,60 +403,69 @@ template <class ST>
 __global__ void __launch_bounds__(128) k_batch_du(const BatchCase *cases, const int4 *rows,
                                                   int nrows, BatchState s) {
   using R = typename ST::R;
+  using T = typename ST::T;
   using A = R;  // per-node and per-warp sums
   __shared__ double sh[2][4];
-  {
-    const int t = blockIdx.x;
-    if (t >= nrows) return;
-    const int4 tl = rows[t];
-    const int c = tl.x;
-    if (!s.active[c]) return;  // uniform per block
-    const BatchCase &bc = cases[c];
-    const StepArgs &a = bc.args[s.gpar[c] & 1];
-    const int x = tl.y * 128 + threadIdx.x, y = tl.z;
-    A du = A(0), uu = A(0);
-    int bad = 0;
-    if (x < a.n) {
-      const long long node = (long long)y * a.pitch + x;
-      const uint8_t cl = a.cls[node];
-      if (cl != CLS_SOLID) {
-        // The node's own post-collision METAF: the collision conserves rho
-        // and j, so their moments are the macroscopic fields of the step
-        // just taken, read without streaming or boundary treatment (nine
-        // coalesced loads; the planes are complete after k_batch_side_sync).
-        const typename ST::T *src = (const typename ST::T *)a.src;
-        R F[9], rho, u, v;
+  const int t = blockIdx.x;
+  if (t >= nrows) return;
+  const int4 tl = rows[t];
+  const int c = tl.x;
+  if (!s.active[c]) return;  // uniform per block
+  const BatchCase &bc = cases[c];
+  const StepArgs &a = bc.args[s.gpar[c] & 1];
+  const int x = tl.y * 128 + threadIdx.x, y0 = tl.z * DU_NPT;
+  const int n = a.n, m = a.m, pitch = a.pitch;
+  const T *src = (const T *)a.src;
+  float *up = bc.uprev, *vp = bc.vprev;
+  // every load of the DU_NPT rows first (more bytes in flight per thread)
+  uint8_t cl[DU_NPT];
+  R F[DU_NPT][9];
+  float pu[DU_NPT], pv[DU_NPT];
 #pragma unroll
-        for (int k = 0; k < 9; k++) F[k] = ld_dev<ST>(src + slot_of<PH_AB>(k, node, a), k, a);
-        moments_form<ST>(F, a, rho, u, v);
-        const long long cell = (long long)y * a.n + x;
-        const A pu = (A)bc.uprev[cell], pv = (A)bc.vprev[cell];
-        du = ((A)u - pu) * ((A)u - pu) + ((A)v - pv) * ((A)v - pv);
-        uu = (A)u * (A)u + (A)v * (A)v;
-        bc.uprev[cell] = (float)u;
-        bc.vprev[cell] = (float)v;
-        bad = (rho != rho || u != u || v != v);
-      }
-    }
-    if constexpr (sizeof(A) == 8) {
-      du = warp_sum(du);
-      uu = warp_sum(uu);
-    } else {
-      du = warp_sum_f(du);
-      uu = warp_sum_f(uu);
-    }
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) {
-      sh[0][wid] = (double)du;
-      sh[1][wid] = (double)uu;
-    }
-    const int anybad = __syncthreads_or(bad);
-    if (threadIdx.x == 0) {
-      s.part[t] = make_double2(sh[0][0] + sh[0][1] + sh[0][2] + sh[0][3],
-                               sh[1][0] + sh[1][1] + sh[1][2] + sh[1][3]);
-      if (anybad) s.bad[c] = 1;
-    }
-    __syncthreads();
+  for (int j = 0; j < DU_NPT; j++) {
+    const bool in = x < n && y0 + j < m;
+    const long long node = (long long)(y0 + j) * pitch + x;
+    cl[j] = in ? a.cls[node] : (uint8_t)CLS_SOLID;
+    const bool fl = cl[j] != CLS_SOLID;
+#pragma unroll
+    for (int k = 0; k < 9; k++) F[j][k] = fl ? ld_dev<ST>(src + slot_of<PH_AB>(k, node, a), k, a) : R(0);
+    const long long cell = (long long)(y0 + j) * n + x;
+    pu[j] = fl ? up[cell] : 0.f;
+    pv[j] = fl ? vp[cell] : 0.f;
+  }
+  A du = A(0), uu = A(0);
+  int bad = 0;
+#pragma unroll
+  for (int j = 0; j < DU_NPT; j++) {
+    if (cl[j] == CLS_SOLID) continue;
+    // the node's own post-collision METAF: the collision conserves rho and
+    // j, so their moments are the macroscopic fields of the step just taken
+    R rho, u, v;
+    moments_form<ST>(F[j], a, rho, u, v);
+    du += ((A)u - (A)pu[j]) * ((A)u - (A)pu[j]) + ((A)v - (A)pv[j]) * ((A)v - (A)pv[j]);
+    uu += (A)u * (A)u + (A)v * (A)v;
+    const long long cell = (long long)(y0 + j) * n + x;
+    up[cell] = (float)u;
+    vp[cell] = (float)v;
+    bad |= (rho != rho || u != u || v != v);
+  }
+  if constexpr (sizeof(A) == 8) {
+    du = warp_sum(du);
+    uu = warp_sum(uu);
+  } else {
+    du = warp_sum_f(du);
+    uu = warp_sum_f(uu);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    sh[0][wid] = (double)du;
+    sh[1][wid] = (double)uu;
+  }
+  const int anybad = __syncthreads_or(bad);
+  if (threadIdx.x == 0) {
+    s.part[t] = make_double2(sh[0][0] + sh[0][1] + sh[0][2] + sh[0][3],
+                             sh[1][0] + sh[1][1] + sh[1][2] + sh[1][3]);
+    if (anybad) s.bad[c] = 1;
   }
 }
 

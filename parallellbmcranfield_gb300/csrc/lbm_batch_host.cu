@@ -454,8 +454,8 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
         for (int tx = 0; tx < (P.n + bx - 1) / bx; tx++) tiles[v].push_back(make_int4(c, tx, by, 0));
     }
     rbeg.push_back((int)rows.size());
-    for (int y = 0; y < P.m; y++)
-      for (int tx = 0; tx < (P.n + 127) / 128; tx++) rows.push_back(make_int4(c, tx, y, 0));
+    for (int yb = 0; yb < (P.m + lbm::DU_NPT - 1) / lbm::DU_NPT; yb++)
+      for (int tx = 0; tx < (P.n + 127) / 128; tx++) rows.push_back(make_int4(c, tx, yb, 0));
     if (b->bk->per_tile)
       for (size_t ri = 0; ri < P.rec.size(); ri++) allrec.push_back(make_int2(c, (int)ri));
     for (size_t ri = 0; ri < P.rec.size(); ri++) {

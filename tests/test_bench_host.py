@@ -27,7 +27,9 @@ def test_workload_config_and_traffic():
     a.precision = "fp16dev"
     assert "9.66 GB" in bench.workload_config(a, 16382)["l2_flush"]
     t = bench.load_traffic("fp32", "ab", 3)
-    assert 0.95 < t / (72 * 16384 * 16385) < 1.0  # measured bytes per launch vs algorithmic
+    # measured DRAM bytes of one full-size launch: the algorithmic 72 B/node plus
+    # the class byte (1.4 %), no re-reads
+    assert 1.0 < t / (72 * 16384 * 16385) < 1.03
     assert bench.load_traffic("fp64", "aa", 1) is None
 
 

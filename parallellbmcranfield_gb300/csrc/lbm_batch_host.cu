@@ -211,42 +211,30 @@ lbm_status launch_steps(lbm_batch *b, int k) {
   lbm_status st = launch_compact(b);
   if (st != LBM_OK) return st;
   int *cnt_t = b->d_live_n;
-  int prio_lo = 0, prio_hi = 0;
-  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
   for (int i = 0; i < k; i++) {
     // the boundary-node pass writes other nodes than the bulk pass and both
     // only read the source state, so it runs on a second stream alongside
-    // (fork and join by events: two parallel branches when captured).  It is
-    // launched first and at the highest priority: its few latency-bound
-    // blocks take SM slots as they free up and overlap the bulk pass instead
-    // of waiting for the bulk pass's last wave.
-    cudaError_t e = cudaSuccess;
+    // (fork and join by events: two parallel branches when captured)
     if (b->nspecial > 0) {
       LBM_BCK(cudaEventRecord(b->ev_fork, b->stream));
       LBM_BCK(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
+    }
+    void *args[] = {&step_args0, &b->d_live_tiles, &cnt_t, &b->s.active, &b->s.gpar};
+    cudaError_t e = cudaLaunchKernel(fn, dim3(grid), dim3(bx), args, 0, b->stream);
+    if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
+    if (b->nspecial > 0) {
       void *sargs[] = {&b->d_cases, &b->d_special, &b->d_nspecial, &b->s.active, &b->s.gpar};
       void *cargs[] = {&b->d_bulk,     &b->d_extra,    &b->d_cases, &b->d_special,
                        &b->d_nspecial, &b->s.active, &b->s.gpar};
       // k_batch_special_c: one thread per entry; k_batch_special: grid-stride
       const int sg = b->bk->per_tile ? (b->nspecial + 127) / 128
                                      : std::min((b->nspecial + 127) / 128, 152 * 16);
-      cudaLaunchAttribute attr;
-      attr.id = cudaLaunchAttributePriority;
-      attr.val.priority = prio_hi;
-      cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3(sg);
-      cfg.blockDim = dim3(128);
-      cfg.stream = b->side;
-      cfg.attrs = &attr;
-      cfg.numAttrs = 1;
-      e = cudaLaunchKernelExC(&cfg, b->bk->special[b->model], b->bk->per_tile ? cargs : sargs);
+      e = cudaLaunchKernel(b->bk->special[b->model], dim3(sg), dim3(128),
+                           b->bk->per_tile ? cargs : sargs, 0, b->side);
       if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch special: ") + cudaGetErrorString(e));
       LBM_BCK(cudaEventRecord(b->ev_join, b->side));
+      LBM_BCK(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
     }
-    void *args[] = {&step_args0, &b->d_live_tiles, &cnt_t, &b->s.active, &b->s.gpar};
-    e = cudaLaunchKernel(fn, dim3(grid), dim3(bx), args, 0, b->stream);
-    if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
-    if (b->nspecial > 0) LBM_BCK(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
     void *aargs[] = {&b->nc, &b->s};
     e = cudaLaunchKernel(b->bk->advance, dim3((b->nc + 255) / 256), dim3(256), aargs, 0, b->stream);
     if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch advance: ") + cudaGetErrorString(e));

@@ -776,6 +776,48 @@ cudaError_t tc_conv(lbm_sg *s, const bf16 *X, int P, int H, int W, int C, int ta
   return tc_conv_launch<EPI, 128>(s, X, P, H, W, C, taps, Bt, N, Kp, bias, out);
 }
 
+// The halo-tile tcgen05 weight gradient (k_tc_wgrad3h): 3x3, W a multiple
+// of 128, C a multiple of 32, N a multiple of 8; one block per SM in all (the
+// row segments split over blocks).  Returns false (nothing launched) when the
+// tensor maps cannot be encoded.
+bool tc_wgrad3h(lbm_sg *s, const bf16 *dZ, const bf16 *X, int P, int H, int W, int C, int N,
+                float *dW, int ldw, cudaError_t *err) {
+  using T = sgtc::TcHaloW;
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc || ((uintptr_t)X & 15) || ((uintptr_t)dZ & 15)) return false;
+  const int imgs = P / (H * W);
+  CUtensorMap mx, mz;
+  const cuuint64_t dx[5] = {8, (cuuint64_t)W, (cuuint64_t)(C / 8), (cuuint64_t)H, (cuuint64_t)imgs};
+  const cuuint64_t sx[4] = {(cuuint64_t)C * 2, 16, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+  const cuuint32_t bx[5] = {8, 130, 4, 3, 1}, e5[5] = {1, 1, 1, 1, 1};
+  const cuuint64_t dz[5] = {8, (cuuint64_t)W, (cuuint64_t)(N / 8), (cuuint64_t)H, (cuuint64_t)imgs};
+  const cuuint64_t sz[4] = {(cuuint64_t)N * 2, 16, (cuuint64_t)W * N * 2, (cuuint64_t)H * W * N * 2};
+  const cuuint32_t bz[5] = {8, 128, (cuuint32_t)std::min(16, N / 8), 1, 1};
+  if (enc(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, (void *)X, dx, sx, bx, e5,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS ||
+      enc(&mz, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, (void *)dZ, dz, sz, bz, e5,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  static bool attr = false;
+  if (!attr) {
+    *err = cudaFuncSetAttribute(sgtc::k_tc_wgrad3h, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                T::BYTES);
+    if (*err != cudaSuccess) return true;
+    attr = true;
+  }
+  const int nseg = imgs * H * (W / sgtc::TC_BM);
+  const int bx_ = C / 32, by_ = (N + 127) / 128;
+  const int splits = std::max(1, std::min(nseg, (152 + bx_ * by_ - 1) / (bx_ * by_)));
+  const int spb = (nseg + splits - 1) / splits;
+  dim3 grid((unsigned)bx_, (unsigned)by_, (unsigned)((nseg + spb - 1) / spb));
+  sgtc::k_tc_wgrad3h<<<grid, sgtc::TC_THREADS, T::BYTES, s->stream>>>(mx, mz, H, W, C, N, nseg, spb,
+                                                                      dW, ldw, s->d_err);
+  *err = cudaGetLastError();
+  return true;
+}
+
 // tcgen05 weight gradient (lbm_tc.cuh), pixels split so that about four
 // blocks per SM run in all, at least 256 pixels each.
 template <int BN>
@@ -899,7 +941,16 @@ lbm_status conv_bwd(lbm_sg *s, int li, int xi, int yi, int B, bool need_dx) {
     k_bias_grad<<<grid_for((size_t)M), 256, 0, s->stream>>>(Y.dx, s->g + c.boff, (size_t)M, c.cout);
   }
   lbm_status st = LBM_OK;
-  if (X.c % 8 == 0 && c.cout % 8 == 0 && s->cfg.products != 1) {
+  bool halo_done = false;
+  if (s->cfg.products == 0 && c.taps == 9 && X.w % sgtc::TC_BM == 0 && X.c % 32 == 0 &&
+      c.cout % 8 == 0 && c.Kp >= 9 * X.c && M % (X.h * X.w) == 0) {
+    cudaError_t e = cudaSuccess;
+    halo_done = tc_wgrad3h(s, Y.dx, X.x, M, X.h, X.w, X.c, c.cout, s->g + c.woff, c.Kp, &e);
+    if (halo_done && e != cudaSuccess)
+      return fail(LBM_CUDA, std::string("surrogate tcgen05 wgrad: ") + cudaGetErrorString(e));
+  }
+  if (halo_done) {
+  } else if (X.c % 8 == 0 && c.cout % 8 == 0 && s->cfg.products != 1) {
     cudaError_t e;
     if (c.cout <= 32)
       e = tc_wgrad_launch<32>(s, Y.dx, X.x, M, X.h, X.w, X.c, c.taps, c.cout, s->g + c.woff, c.Kp);

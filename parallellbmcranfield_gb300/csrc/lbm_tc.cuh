@@ -554,7 +554,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_conv3h(const __grid_constant_
   uint64_t *bars = (uint64_t *)(sm + S * T::STAGE);  // full[2], empty[2], done
   uint64_t *full = bars, *empty = bars + 2, *done = bars + 4;
   uint32_t *slot = (uint32_t *)(bars + 5);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x;
   const int x0 = blockIdx.x * TC_BM, y = blockIdx.y, img = blockIdx.z;
   const int nch = C / 32;
   if (tid == 0) {
@@ -631,6 +631,134 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_conv3h(const __grid_constant_
   __syncthreads();
   __syncwarp();
   if (tid < 32) tm_free(tmem, BN < 32 ? 32 : BN);
+}
+
+// Weight gradient of a 3x3 convolution (pad 1, W a multiple of 128, C a
+// multiple of 32) in the halo-tile form: dW[n][tap][c] = sum over pixels p of
+// dZ[p][n] X[p + offset(tap)][c], as nine products D_tap[n][c] (M = 128
+// output channels, N = 32 input channels of one chunk, K = pixels) that stay
+// in tensor memory (9 x 32 columns) while the block walks its range of
+// 128-pixel row segments.  Per segment one TMA load stages the X halo exactly
+// as k_tc_conv3h does (its rows are the B operand, MN-major: pixels 16 bytes
+// apart, so tap (dy, dx) is a start-address offset), and one TMA load stages
+// dZ as [output group][pixel][8 outputs] (the A operand, MN-major).  FP32
+// atomics add the block's nine tiles into dW at the end.
+//   mapX:  as k_tc_conv3h's mapA
+//   mapDZ: dims (8, W, N/8, H, images), strides (N*2, 16, W*N*2, H*W*N*2),
+//          box (8, 128, min(16, N/8), 1, 1)
+// Stages: TH_WS of TcHaloW::STAGE bytes (one block per SM: the nine tiles
+// take 512 tensor-memory columns).
+constexpr int TH_WS = 3;
+struct TcHaloW {
+  static constexpr int DZ_SLOT = 128 * 128 * 2;  // 16 groups x 128 pixels x 16 bytes
+  static constexpr int STAGE = TH_A_SLOT + DZ_SLOT;
+  static constexpr int BYTES = TH_WS * STAGE + 64 + 1024;
+};
+
+__global__ void __launch_bounds__(TC_THREADS) k_tc_wgrad3h(const __grid_constant__ CUtensorMap mapX,
+                                                           const __grid_constant__ CUtensorMap mapDZ,
+                                                           int H, int W, int C, int N, int nseg,
+                                                           int seg_per_block, float *__restrict__ dW,
+                                                           int ldw, int *err) {
+  using T = TcHaloW;
+  constexpr int S = TH_WS;
+  uint8_t *sm = tc_smem_base();
+  uint64_t *bars = (uint64_t *)(sm + S * T::STAGE);  // full[S], empty[S], done
+  uint64_t *full = bars, *empty = bars + S, *done = bars + 2 * S;
+  uint32_t *slot = (uint32_t *)(bars + 2 * S + 1);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int c0 = blockIdx.x * 32, n0 = blockIdx.y * 128;
+  const int sbeg = blockIdx.z * seg_per_block, send = min(nseg, sbeg + seg_per_block);
+  const int ns = send > sbeg ? send - sbeg : 0;
+  const int groups = min(16, (N - n0) / 8);
+  const uint32_t tx_bytes = TH_A_BYTES + 8 * 128 * groups * 2;
+  const int segs_per_row = W / TC_BM;
+  if (tid == 0) {
+    for (int i = 0; i < 2 * S + 1; i++) mb_init(&bars[i], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    fence_async_smem();
+  }
+  __syncwarp();
+  if (tid < 32) tm_alloc(slot, 512);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *slot;
+  bool ok = true;
+  if (tid == 0) {
+    const uint32_t idesc = tc_idesc(32, 1, 1);
+    int issued = 0, consumed = 0;
+    auto issue = [&](int i, int st) {
+      const int sg = sbeg + i;
+      const int xs = sg % segs_per_row, row = sg / segs_per_row;
+      const int y = row % H, img = row / H, x0 = xs * TC_BM;
+      const uint32_t a = saddr(sm + st * T::STAGE), d = a + TH_A_SLOT;
+      mb_expect_tx(&full[st], tx_bytes);
+      tma_load_5d(a, &mapX, &full[st], 0, x0 - 1, c0 / 8, y - 1, img);
+      tma_load_5d(d, &mapDZ, &full[st], 0, x0, n0 / 8, y, img);
+      issued = i + 1;
+    };
+    for (int i = 0; i < S && i < ns; i++) issue(i, i);
+    for (int i = 0; i < ns && ok; i++) {
+      const int st = i % S;
+      const uint32_t ph = (uint32_t)(i / S) & 1u;
+      if (!mb_wait(&full[st], ph)) {
+        ok = false;
+        break;
+      }
+      consumed = i + 1;
+      tc_fence_after();
+      const uint32_t xa = saddr(sm + st * T::STAGE), za = xa + TH_A_SLOT;
+#pragma unroll 1
+      for (int tap = 0; tap < 9; tap++) {
+        const int dy = tap / 3, dx = tap % 3;  // offsets + 1
+#pragma unroll
+        for (int kk = 0; kk < 8; kk++) {
+          const uint32_t ad = za + kk * 256;
+          const uint32_t bd = xa + dy * (4 * 2080) + (16 * kk + dx) * 16;
+          tc_mma(tmem + tap * 32, tc_desc(ad, 128, 2048), tc_desc(bd, 128, 2080), idesc,
+                 (i | kk) != 0);
+        }
+      }
+      tc_commit(&empty[st]);
+      if (i + S < ns) {
+        if (!mb_wait(&empty[st], ph)) {
+          ok = false;
+          break;
+        }
+        issue(i + S, st);
+      }
+    }
+    tc_commit(done);
+    if (!ok)
+      for (int i = consumed; i < issued; i++) mb_wait(&full[i % S], (uint32_t)(i / S) & 1u);
+  }
+  if (!mb_wait(done, 0)) ok = false;
+  ok = __syncthreads_and(ok) != 0;
+  __syncwarp();
+  tc_fence_after();
+  if (!ok) {
+    if (tid == 0) atomicExch(err, 1);
+  } else if (ns > 0) {
+    const int n = n0 + warp * 32 + lane;  // this thread's tensor-memory lane
+#pragma unroll 1
+    for (int tap = 0; tap < 9; tap++) {
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        float v[16];
+        tm_ld16(tmem + ((uint32_t)(warp * 32) << 16) + tap * 32 + h * 16, v);
+        if (n < N) {
+          float *row = dW + (size_t)n * ldw + tap * C + c0 + h * 16;
+#pragma unroll
+          for (int j = 0; j < 16; j++) atomicAdd(row + j, v[j]);
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  __syncwarp();
+  if (tid < 32) tm_free(tmem, 512);
 }
 
 }  // namespace sgtc

@@ -602,12 +602,15 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_conv3h(const __grid_constant_
         }
       }
       tc_commit(&empty[st]);
-      if (kc + S < nch) {
-        if (!mb_wait(&empty[st], ph)) {
+      // refill the stage the previous chunk used: its MMAs complete ahead of
+      // the ones just issued, which keep the tensor pipe busy meanwhile
+      if (kc >= 1 && kc - 1 + S < nch) {
+        const int pst = (kc - 1) % S;
+        if (!mb_wait(&empty[pst], (uint32_t)((kc - 1) / S) & 1u)) {
           ok = false;
           break;
         }
-        issue(kc + S, st);
+        issue(kc - 1 + S, pst);
       }
     }
     tc_commit(done);  // arrives when every MMA issued above is complete
@@ -721,12 +724,14 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_wgrad3h(const __grid_constant
         }
       }
       tc_commit(&empty[st]);
-      if (i + S < ns) {
-        if (!mb_wait(&empty[st], ph)) {
+      // refill the stage the previous segment used (see k_tc_conv3h)
+      if (i >= 1 && i - 1 + S < ns) {
+        const int pst = (i - 1) % S;
+        if (!mb_wait(&empty[pst], (uint32_t)((i - 1) / S) & 1u)) {
           ok = false;
           break;
         }
-        issue(i + S, st);
+        issue(i - 1 + S, pst);
       }
     }
     tc_commit(done);

@@ -569,56 +569,61 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_conv3h(const __grid_constant_
   tc_fence_after();
   const uint32_t tmem = *slot;
   bool ok = true;
-  if (tid == 0) {
-    const uint32_t idesc = tc_idesc(BN, 0, 0);
-    int issued = 0, consumed = 0;  // chunks whose loads were issued / have landed
-    auto issue = [&](int kc, int st) {
-      const uint32_t a = saddr(sm + st * T::STAGE), b = a + TH_A_SLOT;
-      mb_expect_tx(&full[st], TH_A_BYTES + T::B_BYTES);
-      tma_load_5d(a, &mapA, &full[st], 0, x0 - 1, kc * 4, y - 1, img);
-      tma_load_4d(b, &mapB, &full[st], 0, 0, kc * 4, 0);
-      issued = kc + 1;
-    };
-    for (int i = 0; i < S && i < nch; i++) issue(i, i);
-    for (int kc = 0; kc < nch && ok; kc++) {
-      const int st = kc % S;
-      const uint32_t ph = (uint32_t)(kc / S) & 1u;
-      if (!mb_wait(&full[st], ph)) {
-        ok = false;
-        break;
-      }
-      consumed = kc + 1;
-      tc_fence_after();
-      const uint32_t a = saddr(sm + st * T::STAGE), b = a + TH_A_SLOT;
-#pragma unroll
-      for (int tap = 0; tap < 9; tap++) {
-        const int dy = tap / 3, dx = tap % 3;  // offsets + 1
-#pragma unroll
-        for (int k2 = 0; k2 < 2; k2++) {
-          const uint32_t ad = a + dy * (4 * 2080) + (2 * k2) * 2080 + dx * 16;
-          const uint32_t bd = b + tap * (4 * BN * 16) + (2 * k2) * (BN * 16);
-          tc_mma(tmem, tc_desc(ad, 2080, 128), tc_desc(bd, BN * 16, 128), idesc,
-                 (kc | tap | k2) != 0);
-        }
-      }
-      tc_commit(&empty[st]);
-      // refill the stage the previous chunk used: its MMAs complete ahead of
-      // the ones just issued, which keep the tensor pipe busy meanwhile
-      if (kc >= 1 && kc - 1 + S < nch) {
-        const int pst = (kc - 1) % S;
-        if (!mb_wait(&empty[pst], (uint32_t)((kc - 1) / S) & 1u)) {
+  // warp 0 issues, lane 0 alone; its other lanes wait at __syncwarp
+  // instead of polling the mbarrier beside it
+  if (tid < 32) {
+    if (tid == 0) {
+      const uint32_t idesc = tc_idesc(BN, 0, 0);
+      int issued = 0, consumed = 0;  // chunks whose loads were issued / have landed
+      auto issue = [&](int kc, int st) {
+        const uint32_t a = saddr(sm + st * T::STAGE), b = a + TH_A_SLOT;
+        mb_expect_tx(&full[st], TH_A_BYTES + T::B_BYTES);
+        tma_load_5d(a, &mapA, &full[st], 0, x0 - 1, kc * 4, y - 1, img);
+        tma_load_4d(b, &mapB, &full[st], 0, 0, kc * 4, 0);
+        issued = kc + 1;
+      };
+      for (int i = 0; i < S && i < nch; i++) issue(i, i);
+      for (int kc = 0; kc < nch && ok; kc++) {
+        const int st = kc % S;
+        const uint32_t ph = (uint32_t)(kc / S) & 1u;
+        if (!mb_wait(&full[st], ph)) {
           ok = false;
           break;
         }
-        issue(kc - 1 + S, pst);
+        consumed = kc + 1;
+        tc_fence_after();
+        const uint32_t a = saddr(sm + st * T::STAGE), b = a + TH_A_SLOT;
+  #pragma unroll
+        for (int tap = 0; tap < 9; tap++) {
+          const int dy = tap / 3, dx = tap % 3;  // offsets + 1
+  #pragma unroll
+          for (int k2 = 0; k2 < 2; k2++) {
+            const uint32_t ad = a + dy * (4 * 2080) + (2 * k2) * 2080 + dx * 16;
+            const uint32_t bd = b + tap * (4 * BN * 16) + (2 * k2) * (BN * 16);
+            tc_mma(tmem, tc_desc(ad, 2080, 128), tc_desc(bd, BN * 16, 128), idesc,
+                   (kc | tap | k2) != 0);
+          }
+        }
+        tc_commit(&empty[st]);
+        // refill the stage the previous chunk used: its MMAs complete ahead of
+        // the ones just issued, which keep the tensor pipe busy meanwhile
+        if (kc >= 1 && kc - 1 + S < nch) {
+          const int pst = (kc - 1) % S;
+          if (!mb_wait(&empty[pst], (uint32_t)((kc - 1) / S) & 1u)) {
+            ok = false;
+            break;
+          }
+          issue(kc - 1 + S, pst);
+        }
+      }
+      tc_commit(done);  // arrives when every MMA issued above is complete
+      if (!ok) {
+        // loads still in flight land in this block's shared memory: wait for
+        // them (bounded) before the block may exit
+        for (int kc = consumed; kc < issued; kc++) mb_wait(&full[kc % S], (uint32_t)(kc / S) & 1u);
       }
     }
-    tc_commit(done);  // arrives when every MMA issued above is complete
-    if (!ok) {
-      // loads still in flight land in this block's shared memory: wait for
-      // them (bounded) before the block may exit
-      for (int kc = consumed; kc < issued; kc++) mb_wait(&full[kc % S], (uint32_t)(kc / S) & 1u);
-    }
+    __syncwarp();
   }
   if (!mb_wait(done, 0)) ok = false;
   ok = __syncthreads_and(ok) != 0;
@@ -688,55 +693,60 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_wgrad3h(const __grid_constant
   tc_fence_after();
   const uint32_t tmem = *slot;
   bool ok = true;
-  if (tid == 0) {
-    const uint32_t idesc = tc_idesc(32, 1, 1);
-    int issued = 0, consumed = 0;
-    auto issue = [&](int i, int st) {
-      const int sg = sbeg + i;
-      const int xs = sg % segs_per_row, row = sg / segs_per_row;
-      const int y = row % H, img = row / H, x0 = xs * TC_BM;
-      const uint32_t a = saddr(sm + st * T::STAGE), d = a + TH_A_SLOT;
-      mb_expect_tx(&full[st], tx_bytes);
-      tma_load_5d(a, &mapX, &full[st], 0, x0 - 1, c0 / 8, y - 1, img);
-      tma_load_5d(d, &mapDZ, &full[st], 0, x0, n0 / 8, y, img);
-      issued = i + 1;
-    };
-    for (int i = 0; i < S && i < ns; i++) issue(i, i);
-    for (int i = 0; i < ns && ok; i++) {
-      const int st = i % S;
-      const uint32_t ph = (uint32_t)(i / S) & 1u;
-      if (!mb_wait(&full[st], ph)) {
-        ok = false;
-        break;
-      }
-      consumed = i + 1;
-      tc_fence_after();
-      const uint32_t xa = saddr(sm + st * T::STAGE), za = xa + TH_A_SLOT;
-#pragma unroll 1
-      for (int tap = 0; tap < 9; tap++) {
-        const int dy = tap / 3, dx = tap % 3;  // offsets + 1
-#pragma unroll
-        for (int kk = 0; kk < 8; kk++) {
-          const uint32_t ad = za + kk * 256;
-          const uint32_t bd = xa + dy * (4 * 2080) + (16 * kk + dx) * 16;
-          tc_mma(tmem + tap * 32, tc_desc(ad, 128, 2048), tc_desc(bd, 128, 2080), idesc,
-                 (i | kk) != 0);
-        }
-      }
-      tc_commit(&empty[st]);
-      // refill the stage the previous segment used (see k_tc_conv3h)
-      if (i >= 1 && i - 1 + S < ns) {
-        const int pst = (i - 1) % S;
-        if (!mb_wait(&empty[pst], (uint32_t)((i - 1) / S) & 1u)) {
+  // warp 0 issues, lane 0 alone; its other lanes wait at __syncwarp
+  // instead of polling the mbarrier beside it
+  if (tid < 32) {
+    if (tid == 0) {
+      const uint32_t idesc = tc_idesc(32, 1, 1);
+      int issued = 0, consumed = 0;
+      auto issue = [&](int i, int st) {
+        const int sg = sbeg + i;
+        const int xs = sg % segs_per_row, row = sg / segs_per_row;
+        const int y = row % H, img = row / H, x0 = xs * TC_BM;
+        const uint32_t a = saddr(sm + st * T::STAGE), d = a + TH_A_SLOT;
+        mb_expect_tx(&full[st], tx_bytes);
+        tma_load_5d(a, &mapX, &full[st], 0, x0 - 1, c0 / 8, y - 1, img);
+        tma_load_5d(d, &mapDZ, &full[st], 0, x0, n0 / 8, y, img);
+        issued = i + 1;
+      };
+      for (int i = 0; i < S && i < ns; i++) issue(i, i);
+      for (int i = 0; i < ns && ok; i++) {
+        const int st = i % S;
+        const uint32_t ph = (uint32_t)(i / S) & 1u;
+        if (!mb_wait(&full[st], ph)) {
           ok = false;
           break;
         }
-        issue(i - 1 + S, pst);
+        consumed = i + 1;
+        tc_fence_after();
+        const uint32_t xa = saddr(sm + st * T::STAGE), za = xa + TH_A_SLOT;
+  #pragma unroll 1
+        for (int tap = 0; tap < 9; tap++) {
+          const int dy = tap / 3, dx = tap % 3;  // offsets + 1
+  #pragma unroll
+          for (int kk = 0; kk < 8; kk++) {
+            const uint32_t ad = za + kk * 256;
+            const uint32_t bd = xa + dy * (4 * 2080) + (16 * kk + dx) * 16;
+            tc_mma(tmem + tap * 32, tc_desc(ad, 128, 2048), tc_desc(bd, 128, 2080), idesc,
+                   (i | kk) != 0);
+          }
+        }
+        tc_commit(&empty[st]);
+        // refill the stage the previous segment used (see k_tc_conv3h)
+        if (i >= 1 && i - 1 + S < ns) {
+          const int pst = (i - 1) % S;
+          if (!mb_wait(&empty[pst], (uint32_t)((i - 1) / S) & 1u)) {
+            ok = false;
+            break;
+          }
+          issue(i - 1 + S, pst);
+        }
       }
+      tc_commit(done);
+      if (!ok)
+        for (int i = consumed; i < issued; i++) mb_wait(&full[i % S], (uint32_t)(i / S) & 1u);
     }
-    tc_commit(done);
-    if (!ok)
-      for (int i = consumed; i < issued; i++) mb_wait(&full[i % S], (uint32_t)(i / S) & 1u);
+    __syncwarp();
   }
   if (!mb_wait(done, 0)) ok = false;
   ok = __syncthreads_and(ok) != 0;

@@ -721,10 +721,10 @@ EncodeTiledFn encode_tiled() {
 }
 
 // The halo-tile tcgen05 convolution (k_tc_conv3h): 3x3, W a multiple of 128,
-// C a multiple of 32, N = BN.  Returns false (nothing launched) when the
+// C a multiple of 32, N a multiple of BN (N / BN output tiles).  Returns false (nothing launched) when the
 // tensor maps cannot be encoded, so the caller takes the gather kernel.
 template <int EPI, int BN>
-bool tc_conv3h(lbm_sg *s, const bf16 *X, int P, int H, int W, int C, const bf16 *Bt, int Kp,
+bool tc_conv3h(lbm_sg *s, const bf16 *X, int P, int H, int W, int C, const bf16 *Bt, int N, int Kp,
                const float *bias, bf16 *out, cudaError_t *err) {
   using T = sgtc::TcHalo<BN>;
   EncodeTiledFn enc = encode_tiled();
@@ -734,7 +734,7 @@ bool tc_conv3h(lbm_sg *s, const bf16 *X, int P, int H, int W, int C, const bf16 
   const cuuint64_t da[5] = {8, (cuuint64_t)W, (cuuint64_t)(C / 8), (cuuint64_t)H, (cuuint64_t)imgs};
   const cuuint64_t sa[4] = {(cuuint64_t)C * 2, 16, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
   const cuuint32_t ba[5] = {8, 130, 4, 3, 1}, ea[5] = {1, 1, 1, 1, 1};
-  const cuuint64_t db[4] = {8, (cuuint64_t)BN, (cuuint64_t)(C / 8), 9};
+  const cuuint64_t db[4] = {8, (cuuint64_t)N, (cuuint64_t)(C / 8), 9};
   const cuuint64_t sb[3] = {(cuuint64_t)Kp * 2, 16, (cuuint64_t)C * 2};
   const cuuint32_t bb[4] = {8, (cuuint32_t)BN, 4, 9}, eb[4] = {1, 1, 1, 1};
   if (enc(&ma, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, (void *)X, da, sa, ba, ea,
@@ -752,9 +752,9 @@ bool tc_conv3h(lbm_sg *s, const bf16 *X, int P, int H, int W, int C, const bf16 
     attr = true;
   }
   const int S = C / 32 >= 2 ? 2 : 1;
-  dim3 grid((unsigned)(W / sgtc::TC_BM), (unsigned)H, (unsigned)imgs);
+  dim3 grid((unsigned)(W / sgtc::TC_BM * (N / BN)), (unsigned)H, (unsigned)imgs);
   sgtc::k_tc_conv3h<EPI, BN><<<grid, sgtc::TC_THREADS, T::bytes(S), s->stream>>>(
-      ma, mb, H, W, C, BN, S, bias, out, s->d_err);
+      ma, mb, H, W, C, N, S, bias, out, s->d_err);
   *err = cudaGetLastError();
   return true;
 }
@@ -766,9 +766,9 @@ cudaError_t tc_conv(lbm_sg *s, const bf16 *X, int P, int H, int W, int C, int ta
       P % (H * W) == 0 && s->cfg.products == 0) {
     cudaError_t e = cudaSuccess;
     bool done = false;
-    if (N == 32) done = tc_conv3h<EPI, 32>(s, X, P, H, W, C, Bt, Kp, bias, out, &e);
-    else if (N == 64) done = tc_conv3h<EPI, 64>(s, X, P, H, W, C, Bt, Kp, bias, out, &e);
-    else if (N == 128) done = tc_conv3h<EPI, 128>(s, X, P, H, W, C, Bt, Kp, bias, out, &e);
+    if (N % 128 == 0) done = tc_conv3h<EPI, 128>(s, X, P, H, W, C, Bt, N, Kp, bias, out, &e);
+    else if (N % 64 == 0) done = tc_conv3h<EPI, 64>(s, X, P, H, W, C, Bt, N, Kp, bias, out, &e);
+    else if (N % 32 == 0) done = tc_conv3h<EPI, 32>(s, X, P, H, W, C, Bt, N, Kp, bias, out, &e);
     if (done) return e;
   }
   if (N <= 32) return tc_conv_launch<EPI, 32>(s, X, P, H, W, C, taps, Bt, N, Kp, bias, out);

@@ -520,7 +520,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_wgrad(const bf16 *__restrict_
 }
 
 // 3x3 convolution (pad 1) of an NHWC tensor with W a multiple of 128 and C a
-// multiple of 32, N = BN outputs: the halo-tile form.  A block computes 128
+// multiple of 32, N a multiple of BN outputs: the halo-tile form.  A block computes 128
 // consecutive pixels of one image row.  Per 32-channel chunk one TMA load
 // stages the halo -- rows y-1..y+1, pixels x0-1..x0+128, 4 groups of 8
 // channels, zero outside the image -- as [row][group][pixel][8 channels]
@@ -531,7 +531,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_wgrad(const bf16 *__restrict_
 // per chunk instead of nine times.  Tensor maps (built by the host):
 //   mapA: dims (8, W, C/8, H, images), strides (C*2, 16, W*C*2, H*W*C*2),
 //         box (8, 130, 4, 3, 1)
-//   mapB: dims (8, N, C/8, 9), strides (Kp*2, 16, C*2), box (8, BN, 4, 9)
+//   mapB: dims (8, N, C/8, 9), strides (Kp*2, 16, C*2), box (8, BN, 4, 9) at n0
 // S stages (1 or 2) of TcHalo<BN>::STAGE bytes; thread 0 issues the loads
 // and the MMAs, every wait is bounded.
 constexpr int TH_A_BYTES = 8 * 130 * 4 * 3 * 2;  // 24960
@@ -555,7 +555,10 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_conv3h(const __grid_constant_
   uint64_t *full = bars, *empty = bars + 2, *done = bars + 4;
   uint32_t *slot = (uint32_t *)(bars + 5);
   const int tid = threadIdx.x;
-  const int x0 = blockIdx.x * TC_BM, y = blockIdx.y, img = blockIdx.z;
+  // blockIdx.x: row segment (W / 128 of them) and output tile n0 = BN * tile
+  const int segs = W / TC_BM;
+  const int x0 = (blockIdx.x % segs) * TC_BM, n0 = (blockIdx.x / segs) * BN;
+  const int y = blockIdx.y, img = blockIdx.z;
   const int nch = C / 32;
   if (tid == 0) {
     for (int i = 0; i < 5; i++) mb_init(&bars[i], 1);
@@ -579,7 +582,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_conv3h(const __grid_constant_
         const uint32_t a = saddr(sm + st * T::STAGE), b = a + TH_A_SLOT;
         mb_expect_tx(&full[st], TH_A_BYTES + T::B_BYTES);
         tma_load_5d(a, &mapA, &full[st], 0, x0 - 1, kc * 4, y - 1, img);
-        tma_load_4d(b, &mapB, &full[st], 0, 0, kc * 4, 0);
+        tma_load_4d(b, &mapB, &full[st], 0, n0, kc * 4, 0);
         issued = kc + 1;
       };
       for (int i = 0; i < S && i < nch; i++) issue(i, i);
@@ -633,7 +636,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_conv3h(const __grid_constant_
     if (tid == 0) atomicExch(err, 1);
   } else {
     // the stages are free: every MMA has completed and every load landed
-    tc_epilogue_tile<EPI, BN>(tmem, sm, ((long long)img * H + y) * W + x0, TC_BM, N, 0, bias, out);
+    tc_epilogue_tile<EPI, BN>(tmem, sm, ((long long)img * H + y) * W + x0, TC_BM, N, n0, bias, out);
   }
   tc_fence_before();
   __syncthreads();

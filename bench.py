@@ -388,19 +388,25 @@ def run_gpu(args):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         solver.set_state(None, rho_h.numpy(), u_h.numpy(), v_h.numpy())
+        t1 = time.perf_counter()
         for i in range(args.steps):
             res_h[i] = solver.step(1, 1)[0]
+        t2 = time.perf_counter()
         out = solver.L.lbm_get_fields(solver.h, rho_o.ctypes.data, u_o.ctypes.data,
                                       v_o.ctypes.data, None, None)
         torch.cuda.synchronize(dev)
-        el = time.perf_counter() - t0
+        t3 = time.perf_counter()
+        el = t3 - t0
         assert out == 0
         el = max_over_ranks(ws, el, dev)
         e2e = {"value": round(ws * N * args.steps / el / 1e6, 1), "unit": "MLUPS",
                "h2d_bytes_per_step": int(3 * 8 * N / args.steps),
                "d2h_bytes_per_step": int(32 + 3 * 8 * N / args.steps),
                "what": "lbm_set_state(host rho,u,v) + steps x lbm_step(1, residual line) + "
-                       "lbm_get_fields(host rho,u,v), wall clock"}
+                       "lbm_get_fields(host rho,u,v), wall clock",
+               "phases_ms": {"set_state": round((t1 - t0) * 1e3, 2),
+                             "steps": round((t2 - t1) * 1e3, 2),
+                             "get_fields": round((t3 - t2) * 1e3, 2)}}
     solver.close()
 
     variants = {}

@@ -422,8 +422,53 @@ __global__ void k_bias_grad(const bf16 *dZ, float *db, size_t P, int C) {
   }
 }
 
-// 2x2 average pool (NHWC) and its gradient.
+// The channel-layout kernels below move 8 channels (16 bytes) per thread when
+// every channel count and offset is a multiple of 8 (all feature maps of the
+// network), with 32-bit index arithmetic; the sums and roundings are those of
+// one channel at a time.  The scalar loops remain for other shapes.
+__device__ __forceinline__ void ld8(const bf16 *p, float v[8]) {
+  const uint4 u = *(const uint4 *)p;
+  const __nv_bfloat162 *h = (const __nv_bfloat162 *)&u;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const float2 f = __bfloat1622float2(h[i]);
+    v[2 * i] = f.x;
+    v[2 * i + 1] = f.y;
+  }
+}
+__device__ __forceinline__ void st8(bf16 *p, const float v[8]) {
+  uint4 u;
+  __nv_bfloat162 *h = (__nv_bfloat162 *)&u;
+#pragma unroll
+  for (int i = 0; i < 4; i++) h[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+  *(uint4 *)p = u;
+}
+__host__ __device__ __forceinline__ bool vec8(int C, int Ctot, int coff, const void *a,
+                                              const void *b) {
+  return (C % 8) == 0 && (Ctot % 8) == 0 && (coff % 8) == 0 && ((uintptr_t)a & 15) == 0 &&
+         ((uintptr_t)b & 15) == 0;
+}
+
+// 2x2 average pool of X [B][H][W][C] into Y [B][H/2][W/2][C].
 __global__ void k_pool(const bf16 *X, bf16 *Y, int B, int H, int W, int C) {
+  if (vec8(C, C, 0, X, Y) && (size_t)B * H * W * C < (1u << 31)) {
+    const int C8 = C / 8, W2 = W / 2, H2 = H / 2;
+    const int total = B * H2 * W2 * C8;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+      const int c = (i % C8) * 8, q = i / C8;
+      const int x = q % W2, y = (q / W2) % H2, b = q / (W2 * H2);
+      const size_t base = (((size_t)b * H + 2 * y) * W + 2 * x) * C + c;
+      float a[8], e[8], f[8], g[8], o[8];
+      ld8(X + base, a);
+      ld8(X + base + C, e);
+      ld8(X + base + (size_t)W * C, f);
+      ld8(X + base + (size_t)W * C + C, g);
+#pragma unroll
+      for (int k = 0; k < 8; k++) o[k] = 0.25f * (a[k] + e[k] + f[k] + g[k]);
+      st8(Y + (size_t)q * C + c, o);
+    }
+    return;
+  }
   const size_t total = (size_t)B * (H / 2) * (W / 2) * C;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
     const int c = (int)(i % C);
@@ -436,6 +481,22 @@ __global__ void k_pool(const bf16 *X, bf16 *Y, int B, int H, int W, int C) {
 }
 // Gradient of the pool, written into channels [coff, coff+C) of a [.., Ctot] tensor (adds when acc).
 __global__ void k_pool_back(const bf16 *dY, bf16 *dX, int B, int H, int W, int C, int Ctot, int coff, int accum) {
+  if (vec8(C, Ctot, coff, dY, dX) && (size_t)B * H * W * Ctot < (1u << 31)) {
+    const int C8 = C / 8;
+    const int total = B * H * W * C8;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+      const int c = (i % C8) * 8, q = i / C8;
+      const int x = q % W, y = (q / W) % H, b = q / (W * H);
+      float g[8], o[8];
+      ld8(dY + (((size_t)b * (H / 2) + y / 2) * (W / 2) + x / 2) * C + c, g);
+      bf16 *po = dX + (size_t)q * Ctot + coff + c;
+      if (accum) ld8(po, o);
+#pragma unroll
+      for (int k = 0; k < 8; k++) o[k] = accum ? o[k] + 0.25f * g[k] : 0.25f * g[k];
+      st8(po, o);
+    }
+    return;
+  }
   const size_t total = (size_t)B * H * W * C;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
     const int c = (int)(i % C);
@@ -449,6 +510,17 @@ __global__ void k_pool_back(const bf16 *dY, bf16 *dX, int B, int H, int W, int C
 
 // Nearest 2x upsample of X [B][h][w][C] into channels [0, C) of Y [B][2h][2w][Ctot].
 __global__ void k_upsample(const bf16 *X, bf16 *Y, int B, int h, int w, int C, int Ctot) {
+  if (vec8(C, Ctot, 0, X, Y) && (size_t)B * 4 * h * w * Ctot < (1u << 31)) {
+    const int C8 = C / 8, W2 = 2 * w, H2 = 2 * h;
+    const int total = B * H2 * W2 * C8;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+      const int c = (i % C8) * 8, q = i / C8;
+      const int x = q % W2, y = (q / W2) % H2, b = q / (W2 * H2);
+      *(uint4 *)(Y + (size_t)q * Ctot + c) =
+          *(const uint4 *)(X + (((size_t)b * h + y / 2) * w + x / 2) * C + c);
+    }
+    return;
+  }
   const size_t total = (size_t)B * 2 * h * 2 * w * C;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
     const int c = (int)(i % C);
@@ -459,6 +531,25 @@ __global__ void k_upsample(const bf16 *X, bf16 *Y, int B, int h, int w, int C, i
 }
 // Gradient of the upsample: dX[b][y][x][c] = sum of the 4 children in channels [0, C) of dY.
 __global__ void k_upsample_back(const bf16 *dY, bf16 *dX, int B, int h, int w, int C, int Ctot) {
+  if (vec8(C, Ctot, 0, dY, dX) && (size_t)B * 4 * h * w * Ctot < (1u << 31)) {
+    const int C8 = C / 8;
+    const int total = B * h * w * C8;
+    const size_t W2 = 2 * w;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+      const int c = (i % C8) * 8, q = i / C8;
+      const int x = q % w, y = (q / w) % h, b = q / (w * h);
+      const size_t base = (((size_t)b * 2 * h + 2 * y) * W2 + 2 * x) * Ctot + c;
+      float a[8], e[8], f[8], g[8], o[8];
+      ld8(dY + base, a);
+      ld8(dY + base + Ctot, e);
+      ld8(dY + base + W2 * Ctot, f);
+      ld8(dY + base + W2 * Ctot + Ctot, g);
+#pragma unroll
+      for (int k = 0; k < 8; k++) o[k] = a[k] + e[k] + f[k] + g[k];
+      st8(dX + (size_t)q * C + c, o);
+    }
+    return;
+  }
   const size_t total = (size_t)B * h * w * C;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
     const int c = (int)(i % C);
@@ -473,11 +564,32 @@ __global__ void k_upsample_back(const bf16 *dY, bf16 *dX, int B, int h, int w, i
 
 // Copy X [P][C] into channels [coff, coff+C) of Y [P][Ctot] (and the reverse).
 __global__ void k_copy_ch(const bf16 *X, bf16 *Y, size_t P, int C, int Ctot, int coff) {
+  if (vec8(C, Ctot, coff, X, Y) && P * Ctot < (1u << 31)) {
+    const int C8 = C / 8, total = (int)P * C8;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+      const int c = (i % C8) * 8, q = i / C8;
+      *(uint4 *)(Y + (size_t)q * Ctot + coff + c) = *(const uint4 *)(X + (size_t)q * C + c);
+    }
+    return;
+  }
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < P * C; i += (size_t)gridDim.x * blockDim.x)
     Y[(i / C) * Ctot + coff + i % C] = X[i];
 }
 // dX[p][c] += dY[p][coff + c] (gradient of a skip tensor used in a concat).
 __global__ void k_add_ch(const bf16 *dY, bf16 *dX, size_t P, int C, int Ctot, int coff) {
+  if (vec8(C, Ctot, coff, dY, dX) && P * Ctot < (1u << 31)) {
+    const int C8 = C / 8, total = (int)P * C8;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+      const int c = (i % C8) * 8, q = i / C8;
+      float a[8], d[8];
+      ld8(dX + (size_t)q * C + c, a);
+      ld8(dY + (size_t)q * Ctot + coff + c, d);
+#pragma unroll
+      for (int k = 0; k < 8; k++) a[k] = a[k] + d[k];
+      st8(dX + (size_t)q * C + c, a);
+    }
+    return;
+  }
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < P * C; i += (size_t)gridDim.x * blockDim.x)
     dX[i] = __float2bfloat16_rn(bf(dX[i]) + bf(dY[(i / C) * Ctot + coff + i % C]));
 }

@@ -376,6 +376,10 @@ lbm_status lbm_create(const lbm_mesh *mesh, const lbm_params *params, lbm_ctx **
     return fail(LBM_INVALID, "tile_variant must be 0 (default/tuned) or 1.." + std::to_string(lbm::NVAR));
   }
   c->variant = params->tile_variant > 0 ? params->tile_variant - 1 : 0;
+  if (mom && (long long)c->P.pitch * 21 > INT32_MAX) {
+    delete c;
+    return fail(LBM_INVALID, "moment storage: rows of more than 102 M nodes are not supported");
+  }
   if (c->P.m > 65535) {
     delete c;
     return fail(LBM_INVALID, "grid taller than 65535 rows");
@@ -507,8 +511,21 @@ lbm_status lbm_create(const lbm_mesh *mesh, const lbm_params *params, lbm_ctx **
     a.fx_j = (float)(0.25 * r0 / qmax);
     a.fx_ij = (float)(qmax / (0.25 * r0));
     a.fx_irho0 = (float)(1.0 / r0);
-    a.neq_s = 4096.f;
-    a.neq_is = 1.f / 4096.f;
+    a.neq_s = lbm::MOM_NEQ_S;
+    a.neq_is = 1.f / lbm::MOM_NEQ_S;
+    a.f_i4rho0 = (float)(0.25 / r0);
+    const double hr = 0.5 * r0 / qmax, hj = 0.25 * r0 / qmax, S = lbm::MOM_NEQ_S;
+    a.fx_enc[0] = (float)(64.0 / hr);
+    a.fx_enc[1] = (float)(32.0 / hj);
+    // two codes of margin: the rounding of v / step and the dither stay inside +-qmax
+    a.fx_rlim = (float)((qmax - 2.0) * hr);
+    a.fx_jlim = (float)((qmax - 2.0) * hj);
+    a.enc_c[0] = (float)(2.0 * S * hr);
+    a.enc_c[1] = (float)(-3.0 * S * hj * hj);
+    a.enc_c[2] = (float)(-S * hr);
+    a.enc_c[3] = (float)(3.0 * S * hj * hj);
+    a.enc_c[4] = (float)(S * hj);
+    a.enc_c[5] = (float)(-S * hj * hj / r0);
     a.f_rho0 = (float)a.rho0;
     a.f_om = (float)a.omega;
     a.f_omA = (float)a.omegaA;

@@ -13,6 +13,11 @@
 //   planes 0..2   int16  high 16 bits of Q(rho - rho0), Q(j_x), Q(j_y)
 //   planes 3..8   FP16   n_i = (m*_i - b_i) * neq_scale, i = 1, 2, 4, 6, 7, 8
 //   bytes  0..2   uint8  low 8 bits of the three fixed-point values
+// Layout: chunks of 64 consecutive nodes of a row (the pitch is a multiple
+// of 256), 1344 bytes each, in node order; inside a chunk the nine 16-bit
+// planes (128 bytes each) and then the three byte planes (64 bytes each).
+// A node's twelve values are then at fixed offsets from one pointer, so a
+// thread addresses a whole row with one pointer and immediate offsets.
 // Q(x) = floor(x / step + u) is a 24-bit signed fixed-point number with a
 // per-node, per-generation dither u in [0, 1) (unbiased rounding; steps from
 // the host: the density range +-0.5 rho0, the momentum range +-0.25 rho0); a value
@@ -37,15 +42,27 @@ namespace lbm {
 
 constexpr int MOM_QMAX = (1 << 23) - 1;     // largest fixed-point magnitude
 
-// Byte offsets of the planes in one moment buffer of `plane` nodes per plane.
-__device__ __forceinline__ const int16_t *mom_hi(const void *b, const StepArgs &a, int p) {
-  return (const int16_t *)b + (long long)p * a.plane;
+constexpr int MOM_CH = 64;                // nodes per chunk
+constexpr int MOM_CHB = 21 * MOM_CH;      // bytes per chunk
+constexpr int MOM_LO_OFF = 18 * MOM_CH;   // first byte plane inside a chunk
+
+// Byte offset of node z's 16-bit slot in plane 0 (the node's chunk plus
+// two bytes per node before it in the chunk); plane p lies 128 p bytes on.
+__device__ __forceinline__ long long mom_off(long long z) {
+  return 21LL * (z & ~(long long)(MOM_CH - 1)) + 2 * (z & (MOM_CH - 1));
 }
-__device__ __forceinline__ const __half *mom_n(const void *b, const StepArgs &a, int i) {
-  return (const __half *)b + (long long)(3 + i) * a.plane;
+// Byte offset of node z's slot in byte plane 0; byte plane p lies 64 p on.
+__device__ __forceinline__ long long mom_off_lo(long long z) {
+  return 21LL * (z & ~(long long)(MOM_CH - 1)) + MOM_LO_OFF + (z & (MOM_CH - 1));
 }
-__device__ __forceinline__ const uint8_t *mom_lo(const void *b, const StepArgs &a, int p) {
-  return (const uint8_t *)b + 18 * a.plane + (long long)p * a.plane;
+__device__ __forceinline__ const int16_t *mom_hi(const void *b, long long z, int p) {
+  return (const int16_t *)((const char *)b + mom_off(z) + 2 * MOM_CH * p);
+}
+__device__ __forceinline__ const __half *mom_n(const void *b, long long z, int i) {
+  return (const __half *)((const char *)b + mom_off(z) + 2 * MOM_CH * (3 + i));
+}
+__device__ __forceinline__ const uint8_t *mom_lo(const void *b, long long z, int p) {
+  return (const uint8_t *)b + mom_off_lo(z) + MOM_CH * p;
 }
 
 // The stored moment set of one node in deviation form: r = rho - rho0,
@@ -97,15 +114,15 @@ __device__ __forceinline__ MomSet mom_load(const StepArgs &a, const void *b, lon
   float q[3];
 #pragma unroll
   for (int p = 0; p < 3; p++) {
-    const int hi = __ldg(mom_hi(b, a, p) + z);
-    const int lo = __ldg(mom_lo(b, a, p) + z);
+    const int hi = __ldg(mom_hi(b, z, p));
+    const int lo = __ldg(mom_lo(b, z, p));
     q[p] = (float)(hi * 256 + lo) * fx_step(a, p);
   }
   s.r = q[0];
   s.x = q[1];
   s.y = q[2];
 #pragma unroll
-  for (int i = 0; i < 6; i++) s.n[i] = __half2float(__ldg(mom_n(b, a, i) + z)) * a.neq_is;
+  for (int i = 0; i < 6; i++) s.n[i] = __half2float(__ldg(mom_n(b, z, i))) * a.neq_is;
   return s;
 }
 
@@ -217,11 +234,11 @@ __device__ __forceinline__ void mom_store(const StepArgs &a, void *b, long long 
                                           const MomCode &c) {
 #pragma unroll
   for (int p = 0; p < 3; p++) {
-    ((int16_t *)mom_hi(b, a, p))[z] = (int16_t)(c.q[p] >> 8);
-    ((uint8_t *)mom_lo(b, a, p))[z] = (uint8_t)(c.q[p] & 0xff);
+    *(int16_t *)mom_hi(b, z, p) = (int16_t)(c.q[p] >> 8);
+    *(uint8_t *)mom_lo(b, z, p) = (uint8_t)(c.q[p] & 0xff);
   }
 #pragma unroll
-  for (int i = 0; i < 6; i++) ((__half *)mom_n(b, a, i))[z] = c.n[i];
+  for (int i = 0; i < 6; i++) *(__half *)mom_n(b, z, i) = c.n[i];
 }
 
 // Out-of-range or non-finite result: the step's flag (checked by the host).
@@ -279,15 +296,16 @@ struct MomRaw {
   uint32_t n[6];  // two FP16 non-equilibrium moments
 };
 
-__device__ __forceinline__ void mom_raw_load(const StepArgs &a, const void *b, long long z,
-                                             bool in, MomRaw &w) {
+// p16 / plo: the pair's slots in 16-bit plane 0 and byte plane 0 (mom_off,
+// mom_off_lo of its first node, which is even: both nodes share a chunk).
+__device__ __forceinline__ void mom_raw_load(const char *p16, const char *plo, MomRaw &w) {
 #pragma unroll
   for (int p = 0; p < 3; p++) {
-    w.h[p] = in ? __ldg((const unsigned *)(mom_hi(b, a, p) + z)) : 0u;
-    w.l[p] = in ? (uint32_t)__ldg((const unsigned short *)(mom_lo(b, a, p) + z)) : 0u;
+    w.h[p] = __ldg((const unsigned *)(p16 + 2 * MOM_CH * p));
+    w.l[p] = (uint32_t)__ldg((const unsigned short *)(plo + MOM_CH * p));
   }
 #pragma unroll
-  for (int i = 0; i < 6; i++) w.n[i] = in ? __ldg((const unsigned *)(mom_n(b, a, i) + z)) : 0u;
+  for (int i = 0; i < 6; i++) w.n[i] = __ldg((const unsigned *)(p16 + 2 * MOM_CH * (3 + i)));
 }
 
 // Byte permute with the PTX default mode: a selector nibble with bit 3 set
@@ -299,9 +317,15 @@ __device__ __forceinline__ int prmt_s(uint32_t a, uint32_t b, uint32_t sel) {
   return (int)d;
 }
 
-// Post-collision deviations of both nodes of a pair (the arithmetic of
-// mom_to_pops on FP32 pairs): each 24-bit code is the low byte, then the
-// int16 high part, then the high part's sign replicated, in one permute.
+// Post-collision deviations of both nodes of a pair (mom_to_pops on FP32
+// pairs): each 24-bit code is the low byte, then the int16 high part, then
+// the high part's sign replicated, in one permute.  The factor 1/36 of Minv
+// and the storage scale of the n_i are folded into the constants, so that
+// each diagonal population is two sums of terms formed by one multiply-add:
+//   36 d_5..8 = (r + 3|j|^2 + 2 N1 + N2) +- 3 (x + N4) +- 3 (y + N6) +- 9 (x y / rho0 + N8)
+//   36 (d_1 + d_3) / 2 = (4 r + 3|j|^2 - N1 - 2 N2) + 9 ((x^2 - y^2) / rho0 + N7)
+// (N_i = n_i / neq_s; the axis pairs and d_0 as in mom_to_pops, so that mass
+// and momentum are exact up to one rounding each).
 __device__ __forceinline__ void mom_decode2(const StepArgs &a, const MomRaw &w, float2 d[9]) {
   float2 q[3];
 #pragma unroll
@@ -310,43 +334,46 @@ __device__ __forceinline__ void mom_decode2(const StepArgs &a, const MomRaw &w, 
     const int q1 = prmt_s(w.l[p], w.h[p], 0xF761u);  // l.b1, h.b2, h.b3, sign(h.b3)
     q[p] = mul2(make_float2((float)q0, (float)q1), bc2(fx_step(a, p)));
   }
-  float2 n[6];  // stored units (n_i * neq_s); the inverse scale enters the FMAs below
+  float2 n[6];  // stored units (n_i * neq_s)
 #pragma unroll
   for (int i = 0; i < 6; i++) {
     __half2 h;
     memcpy(&h, &w.n[i], 4);
     n[i] = __half22float2(h);
   }
-  const float2 is = bc2(a.neq_is);
+  constexpr float is = 1.f / MOM_NEQ_S;
   const float2 r = q[0], x = q[1], y = q[2];
-  const float2 i0 = bc2(a.fx_irho0);
-  const float2 jj = fma2(x, x, mul2(y, y));
-  const float2 m1 = fma2(n[0], is, fma2(bc2(3.f), jj, mul2(bc2(-2.f), r)));
-  const float2 m2 = fma2(n[1], is, fma2(bc2(-3.f), jj, r));
-  const float2 m4 = fma2(n[2], is, mul2(bc2(-1.f), x)), m6 = fma2(n[3], is, mul2(bc2(-1.f), y));
-  const float2 m7 = fma2(n[4], is, mul2(mul2(sub2(x, y), add2(x, y)), i0));
-  const float2 m8 = fma2(n[5], is, mul2(mul2(x, y), i0));
-  const float2 ax = sub2(fma2(bc2(4.f), r, mul2(bc2(-2.f), m2)), m1);
-  const float2 dg = fma2(bc2(2.f), m1, fma2(bc2(4.f), r, m2));
-  const float2 P = mul2(bc2(9.f), m7), Q = mul2(bc2(9.f), m8);
-  const float2 Xd = fma2(bc2(3.f), m4, mul2(bc2(6.f), x));
-  const float2 Yd = fma2(bc2(3.f), m6, mul2(bc2(6.f), y));
-  const float2 c = bc2(1.f / 36.f);
+  const float2 yy = mul2(y, y);
+  const float2 jj = fma2(x, x, yy);
+  const float2 xmy = fma2(bc2(-2.f), yy, jj);  // x^2 - y^2
+  const float2 xy = mul2(x, y);
+  const float2 i4 = bc2(a.f_i4rho0);            // 1 / (4 rho0)
+  // the four diagonal populations, already divided by 36
+  const float2 dg = fma2(n[1], bc2(is / 36.f),
+                         fma2(n[0], bc2(2.f * is / 36.f),
+                              fma2(jj, bc2(1.f / 12.f), mul2(r, bc2(1.f / 36.f)))));
+  const float2 Q = fma2(n[5], bc2(is / 4.f), mul2(xy, i4));
+  const float2 Xd = fma2(n[2], bc2(is / 12.f), mul2(x, bc2(1.f / 12.f)));
+  const float2 Yd = fma2(n[3], bc2(is / 12.f), mul2(y, bc2(1.f / 12.f)));
   const float2 gp = add2(dg, Q), gm = sub2(dg, Q), sp = add2(Xd, Yd), sm = sub2(Xd, Yd);
-  d[5] = mul2(c, add2(gp, sp));
-  d[6] = mul2(c, sub2(gm, sm));
-  d[7] = mul2(c, sub2(gp, sp));
-  d[8] = mul2(c, add2(gm, sm));
-  // conserved moments exact by construction (see mom_to_pops)
-  const float2 s13 = mul2(bc2(2.f / 36.f), add2(ax, P)), s24 = mul2(bc2(2.f / 36.f), sub2(ax, P));
-  const float2 e57 = sub2(d[5], d[7]);
-  const float2 dx = sub2(x, add2(e57, sub2(d[8], d[6])));
-  const float2 dy = sub2(y, add2(e57, sub2(d[6], d[8])));
-  const float2 h = bc2(0.5f);
-  d[1] = mul2(h, add2(s13, dx));
-  d[3] = mul2(h, sub2(s13, dx));
-  d[2] = mul2(h, add2(s24, dy));
-  d[4] = mul2(h, sub2(s24, dy));
+  d[5] = add2(gp, sp);
+  d[6] = sub2(gm, sm);
+  d[7] = sub2(gp, sp);
+  d[8] = add2(gm, sm);
+  // half the axis pairs' sums, divided by 36
+  const float2 ax = fma2(n[1], bc2(-2.f * is / 36.f),
+                         fma2(n[0], bc2(-is / 36.f),
+                              fma2(jj, bc2(3.f / 36.f), mul2(r, bc2(4.f / 36.f)))));
+  const float2 P = fma2(n[4], bc2(is / 4.f), mul2(xmy, i4));
+  const float2 s13 = add2(ax, P), s24 = sub2(ax, P);
+  // the momentum the diagonals leave goes to the axis pairs (see mom_to_pops)
+  const float2 e57 = sub2(d[5], d[7]), e86 = sub2(d[8], d[6]);
+  const float2 dx = sub2(x, add2(e57, e86));
+  const float2 dy = sub2(y, sub2(e57, e86));
+  d[1] = fma2(dx, bc2(0.5f), s13);
+  d[3] = fma2(dx, bc2(-0.5f), s13);
+  d[2] = fma2(dy, bc2(0.5f), s24);
+  d[4] = fma2(dy, bc2(-0.5f), s24);
   d[0] = sub2(r, add2(add2(add2(d[1], d[3]), add2(d[2], d[4])),
                       add2(add2(d[5], d[7]), add2(d[6], d[8]))));
 }
@@ -394,72 +421,79 @@ __device__ __forceinline__ void collide_mom2(float2 r, float2 jx, float2 jy, flo
 }
 
 // Encodes the post-collision moments of a pair and stores the nodes whose
-// `own` flag is set (both: full words; one: its own elements).
-__device__ __forceinline__ void mom_encode_store2(const StepArgs &a, void *b, long long z,
-                                                  uint32_t hseed, float2 r, float2 jx, float2 jy,
-                                                  const float2 m[6], bool own0, bool own1,
-                                                  bool &ok) {
+// `own` flag is set (both: full words; one: its own elements).  The largest
+// |rho - rho0| and |j| of the stored nodes go to rmax / jmax: the caller
+// compares them with the fixed-point range once, at the end of its walk.
+__device__ __forceinline__ void mom_encode_store2(const StepArgs &a, char *p16, char *plo,
+                                                  long long z, uint32_t hseed, float2 r, float2 jx,
+                                                  float2 jy, const float2 m[6], bool own0,
+                                                  bool own1, float &rmax, float &jmax) {
   // Dithered codes in integers: R = round(2^D v / step), t = (R + u) >> D
   // with u uniform in 0 .. 2^D - 1, so that E[t] = R / 2^D, within 2^-(D+1)
   // of v / step.  The pair's dithers come from one hash: node 0 in bits
-  // 0..15, node 1 in 16..31; D = 6 for rho, 5 for each j.  Out of range
-  // (|t| > MOM_QMAX, or R saturated by the conversion) clears `ok`; a NaN
-  // converts to 0 and is caught by the caller's probe instead.
+  // 0..15, node 1 in 16..31; D = 6 for rho, 5 for each j.  Values beyond the
+  // range show in rmax / jmax; a NaN converts to 0 and is caught by the
+  // caller's probe instead.
   const uint32_t h = mix32((uint32_t)z ^ hseed);
   const float2 v[3] = {r, jx, jy};
   const int sh[3] = {0, 6, 11}, nb[3] = {6, 5, 5};
   int q0[3], q1[3];
-  bool bad = false;
+  float2 qf[3];
 #pragma unroll
   for (int p = 0; p < 3; p++) {
     const uint32_t mask = (1u << nb[p]) - 1u;
-    const float2 x = mul2(v[p], bc2(fx_istep(a, p) * (float)(1u << nb[p])));
+    const float2 x = mul2(v[p], bc2(a.fx_enc[p == 0 ? 0 : 1]));
     const uint32_t R0 = (uint32_t)__float2int_rn(x.x), R1 = (uint32_t)__float2int_rn(x.y);
     q0[p] = (int)(R0 + ((h >> sh[p]) & mask)) >> nb[p];
     q1[p] = (int)(R1 + ((h >> (16 + sh[p])) & mask)) >> nb[p];
-    const bool b0 = (uint32_t)(q0[p] + MOM_QMAX) > 2u * (uint32_t)MOM_QMAX;
-    const bool b1 = (uint32_t)(q1[p] + MOM_QMAX) > 2u * (uint32_t)MOM_QMAX;
-    bad = bad || (own0 && b0) || (own1 && b1);
+    qf[p] = make_float2((float)q0[p], (float)q1[p]);
   }
-  ok = ok && !bad;
+  if (own0) {
+    rmax = fmaxf(rmax, fabsf(r.x));
+    jmax = fmaxf(jmax, fmaxf(fabsf(jx.x), fabsf(jy.x)));
+  }
+  if (own1) {
+    rmax = fmaxf(rmax, fabsf(r.y));
+    jmax = fmaxf(jmax, fmaxf(fabsf(jx.y), fabsf(jy.y)));
+  }
   // minus the references b_i (times neq_s) of the stored conserved moments,
-  // so that each stored value is one multiply-add
-  const float ns = a.neq_s;
-  const float2 sr = mul2(make_float2((float)q0[0], (float)q1[0]), bc2(fx_step(a, 0)));
-  const float2 sx = mul2(make_float2((float)q0[1], (float)q1[1]), bc2(fx_step(a, 1)));
-  const float2 sy = mul2(make_float2((float)q0[2], (float)q1[2]), bc2(fx_step(a, 2)));
-  const float2 i0 = bc2(a.fx_irho0 * ns);
-  const float2 jj = fma2(sx, sx, mul2(sy, sy));
-  const float2 mref[6] = {fma2(bc2(-3.f * ns), jj, mul2(bc2(2.f * ns), sr)),
-                          fma2(bc2(3.f * ns), jj, mul2(bc2(-ns), sr)), mul2(bc2(ns), sx),
-                          mul2(bc2(ns), sy), mul2(mul2(sub2(sy, sx), add2(sx, sy)), i0),
-                          mul2(mul2(sx, sy), bc2(-a.fx_irho0 * ns))};
+  // from the codes with the fixed-point steps folded into the constants
+  // (enc_c), so that each stored value is one multiply-add
+  const float2 qr = qf[0], qx = qf[1], qy = qf[2];
+  const float2 qyy = mul2(qy, qy);
+  const float2 jj = fma2(qx, qx, qyy);
+  const float2 xmy = fma2(bc2(-2.f), qyy, jj);
+  const float2 c5 = bc2(a.enc_c[5]), c4 = bc2(a.enc_c[4]);
+  const float2 mref[6] = {fma2(jj, bc2(a.enc_c[1]), mul2(qr, bc2(a.enc_c[0]))),
+                          fma2(jj, bc2(a.enc_c[3]), mul2(qr, bc2(a.enc_c[2]))), mul2(qx, c4),
+                          mul2(qy, c4), mul2(xmy, c5), mul2(mul2(qx, qy), c5)};
   uint32_t nw[6];
 #pragma unroll
   for (int i = 0; i < 6; i++) {
-    const __half2 hh = __float22half2_rn(fma2(m[i], bc2(ns), mref[i]));
+    const __half2 hh = __float22half2_rn(fma2(m[i], bc2(MOM_NEQ_S), mref[i]));
     memcpy(&nw[i], &hh, 4);
   }
   if (own0 && own1) {
 #pragma unroll
     for (int p = 0; p < 3; p++) {
-      *(uint32_t *)(mom_hi(b, a, p) + z) = __byte_perm((uint32_t)q0[p], (uint32_t)q1[p], 0x6521);
-      *(unsigned short *)(mom_lo(b, a, p) + z) =
+      *(uint32_t *)(p16 + 2 * MOM_CH * p) = __byte_perm((uint32_t)q0[p], (uint32_t)q1[p], 0x6521);
+      *(unsigned short *)(plo + MOM_CH * p) =
           (unsigned short)__byte_perm((uint32_t)q0[p], (uint32_t)q1[p], 0x0040);
     }
 #pragma unroll
-    for (int i = 0; i < 6; i++) *(uint32_t *)(mom_n(b, a, i) + z) = nw[i];
+    for (int i = 0; i < 6; i++) *(uint32_t *)(p16 + 2 * MOM_CH * (3 + i)) = nw[i];
   } else if (own0 || own1) {
     const int e = own0 ? 0 : 1;
 #pragma unroll
     for (int p = 0; p < 3; p++) {
       const int q = e ? q1[p] : q0[p];
-      *(int16_t *)(mom_hi(b, a, p) + z + e) = (int16_t)(q >> 8);
-      *(uint8_t *)(mom_lo(b, a, p) + z + e) = (uint8_t)(q & 0xff);
+      *(int16_t *)(p16 + 2 * MOM_CH * p + 2 * e) = (int16_t)(q >> 8);
+      *(uint8_t *)(plo + MOM_CH * p + e) = (uint8_t)(q & 0xff);
     }
 #pragma unroll
     for (int i = 0; i < 6; i++)
-      *(unsigned short *)(mom_n(b, a, i) + z + e) = (unsigned short)(e ? nw[i] >> 16 : nw[i] & 0xffffu);
+      *(unsigned short *)(p16 + 2 * MOM_CH * (3 + i) + 2 * e) =
+          (unsigned short)(e ? nw[i] >> 16 : nw[i] & 0xffffu);
   }
 }
 
@@ -472,9 +506,11 @@ __device__ __forceinline__ void mom_encode_store2(const StepArgs &a, void *b, lo
 // destination row r+1, c_y = 0 to row r and c_y = -1 to row r-1, which is
 // then complete: it collides and stores (class-1 nodes only; class 2 and 3
 // belong to k_special_mom, solid nodes are never written).  The raw words of
-// source rows are loaded two rows ahead into a ring of three, and lanes 0..11
+// source rows are loaded two rows ahead into a ring of three, and lanes 0..21
 // prefetch the warp's span of row r + MOM_PF into L2 (a hint: nothing waits
-// for it, every prefetched byte lies inside the buffer and its guard bytes).
+// for it, every prefetched address lies inside the row).  Rows are addressed
+// by one pointer per thread and row (the chunked layout), each value at an
+// immediate offset from it.
 // The row walk is a loop over groups of three rows, the period of the ring
 // and of the three population rows, so that the code stays small.
 constexpr int MOM_PF = 6;
@@ -482,33 +518,44 @@ constexpr int MOM_PF = 6;
 struct MomWalk {
   MomRaw raw[3];
   float2 Fa[9], Fb[9], Fc[9];
-  bool ok;
+  float rmax, jmax;        // largest |rho - rho0|, |j| stored (range check at the end)
   float probe;
+  int rowb;                // bytes per row of a moment buffer (21 x pitch)
+  int o16, olo;            // the pair's slot offsets within a row (mom_off, mom_off_lo of x0)
+  int pf0, pf1;            // the warp's span of a row, [pf0, pf1) bytes within the row
 };
 
 // Row j of the walk (source row y0 + j); PH = (j + 1) mod 3 selects the ring
-// slots: row j decodes slot PH and loads row j + 2 into slot (PH + 2) mod 3.
-template <int MODEL, int NPT, bool PF, int PH>
+// slots: row j decodes slot PH and loads row j + LD into slot (PH + LD) mod 3
+// (LD = 1 or 2 rows ahead: 12 or 24 registers of loads in flight).
+template <int MODEL, int NPT, bool PF, int LD, int PH>
 __device__ __forceinline__ void mom_walk_row(const StepArgs &a, MomWalk &w, int j, int y0, int wx,
-                                             int x0, int lane, bool inx, bool owner,
+                                             int x0, int lane, bool owner,
                                              uint32_t hseed) {
   const unsigned FULL = 0xffffffffu;
   const int r = y0 + j;
-  if (j + 2 <= NPT) {
-    const int r2 = r + 2;
-    mom_raw_load(a, a.src, (long long)r2 * a.pitch + x0, inx && r2 < a.m, w.raw[(PH + 2) % 3]);
+  const char *src = (const char *)a.src;
+  if (j + LD <= NPT) {
+    const long long rb = (long long)min(r + LD, a.m - 1) * w.rowb;
+    mom_raw_load(src + rb + w.o16, src + rb + w.olo, w.raw[(PH + LD) % 3]);
   }
+  // class word of this row's destination row r - 1, loaded before the
+  // decode so that the arithmetic covers its latency
+  const int y = r - 1;
+  const uint32_t cw = j >= 1 && owner && y < a.m
+                          ? __ldg((const unsigned short *)(a.cls + (long long)y * a.pitch + x0))
+                          : 0u;
   if (PF && lane < 24) {
-    // one 128-byte line per lane: the warp's span of row r + MOM_PF covers at
-    // most two lines of each of the nine 16-bit planes (lanes 0..17) and of
-    // the three byte planes (lanes 18..23); every address lies in the span
+    // one 128-byte line per lane: the warp's span of a row is one or two
+    // whole chunks (at most 2688 bytes, 22 lines at a 64-byte offset) for
+    // lanes 0..21, the span's class bytes (64 bytes, at most two lines) for
+    // lanes 22 and 23; the last address of each is clamped into the span
     const int rp = r + MOM_PF;
     if (rp < a.m && j + MOM_PF <= NPT) {
-      const long long e = (long long)rp * a.pitch + wx - 2;
-      const int pl = lane >> 1, hi = lane & 1;
-      const char *base = (const char *)a.src;
-      const char *p = pl < 9 ? base + (long long)pl * 2 * a.plane + 2 * e + hi * 127
-                             : base + (long long)(9 + pl) * a.plane + e + hi * 63;
+      const char *p =
+          lane < 22 ? src + (long long)rp * w.rowb + min(w.pf0 + 128 * lane, w.pf1 - 1)
+                    : (const char *)a.cls + (long long)rp * a.pitch +
+                          (lane == 22 ? max(wx - 2, 0) : min(wx + 61, a.pitch - 1));
       asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
     }
   }
@@ -529,22 +576,18 @@ __device__ __forceinline__ void mom_walk_row(const StepArgs &a, MomWalk &w, int 
     else w.Fa[k] = v;
   }
   if (j >= 1) {  // destination row r - 1 is complete
-    const int y = r - 1;
-    bool own0 = false, own1 = false;
-    if (owner && y < a.m) {
-      const uint32_t cw = __ldg((const unsigned short *)(a.cls + (long long)y * a.pitch + x0));
-      own0 = (cw & 0xffu) == CLS_BULK;
-      own1 = (cw >> 8) == CLS_BULK && x0 + 1 < a.n;
-    }
-    if (own0 || own1) {
-      float2 rr, jx, jy, m[6];
-      pops_to_mom2(w.Fa, rr, jx, jy, m);
-      collide_mom2<MODEL>(rr, jx, jy, m, a);
-      if (own0) w.probe += rr.x + m[4].x;
-      if (own1) w.probe += rr.y + m[4].y;
-      mom_encode_store2(a, a.dst, (long long)y * a.pitch + x0, hseed, rr, jx, jy, m, own0, own1,
-                        w.ok);
-    }
+    const bool own0 = (cw & 0xffu) == CLS_BULK;
+    const bool own1 = (cw >> 8) == CLS_BULK && x0 + 1 < a.n;
+    // every lane runs the arithmetic (no divergent branch around it); only
+    // the nodes a lane owns are stored and counted
+    float2 rr, jx, jy, m[6];
+    pops_to_mom2(w.Fa, rr, jx, jy, m);
+    collide_mom2<MODEL>(rr, jx, jy, m, a);
+    if (own0) w.probe += rr.x + m[4].x;
+    if (own1) w.probe += rr.y + m[4].y;
+    char *dst = (char *)a.dst + (long long)y * w.rowb;
+    mom_encode_store2(a, dst + w.o16, dst + w.olo, (long long)y * a.pitch + x0, hseed, rr, jx, jy,
+                      m, own0, own1, w.rmax, w.jmax);
   }
 #pragma unroll
   for (int k = 0; k < 9; k++) {
@@ -553,35 +596,51 @@ __device__ __forceinline__ void mom_walk_row(const StepArgs &a, MomWalk &w, int 
   }
 }
 
-template <int MODEL, int NPT, int MINB, bool PF>
+template <int MODEL, int NPT, int MINB, bool PF, int LD>
 __global__ void __launch_bounds__(128, MINB) k_step_mom(const __grid_constant__ StepArgs a) {
   static_assert((NPT + 2) % 3 == 0, "the row walk runs in groups of three rows");
+  static_assert(LD == 1 || LD == 2, "source rows are loaded one or two rows ahead");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int wx = (blockIdx.x * 4 + warp) * 60;
   if (wx >= a.n) return;  // the whole warp lies past the row
   const int x0 = wx - 2 + 2 * lane;
-  const bool inx = x0 >= 0 && x0 < a.pitch;  // the pitch is even, so x0 + 1 < pitch too
   const bool owner = lane >= 1 && lane <= 30 && x0 < a.n;
   const int y0 = blockIdx.y * NPT;
   if (y0 - 1 >= a.m) return;
   const uint32_t hseed = mix32(a.gen * 0x9e3779b9u + 0x632be5abu);
   MomWalk w;
-  mom_raw_load(a, a.src, (long long)(y0 - 1) * a.pitch + x0, inx && y0 >= 1 && y0 - 1 < a.m,
-               w.raw[0]);
-  mom_raw_load(a, a.src, (long long)y0 * a.pitch + x0, inx && y0 < a.m, w.raw[1]);
+  w.rowb = 21 * a.pitch;  // the host keeps 21 x pitch below 2^31
+  // Loads are unconditional: a pair left or right of the row (x0 = -2, or
+  // x0 >= pitch) reads the row's first or last pair, a row above or below
+  // the domain its first or last row.  Those values reach only nodes that
+  // are not bulk nodes (the domain's edge columns and rows are never class
+  // 1), which this kernel does not store.
+  const int x0c = min(max(x0, 0), a.pitch - 2);
+  w.o16 = (int)mom_off(x0c);
+  w.olo = (int)mom_off_lo(x0c);
+  // chunks met by the warp's columns wx - 2 .. wx + 61 (clamped to the row)
+  w.pf0 = MOM_CHB * (max(wx - 2, 0) / MOM_CH);
+  w.pf1 = MOM_CHB * (min(wx + 61, a.pitch - 1) / MOM_CH + 1);
+  {
+    const char *src = (const char *)a.src;
+    const long long rm = (long long)min(max(y0 - 1, 0), a.m - 1) * w.rowb;
+    const long long r0 = (long long)min(y0, a.m - 1) * w.rowb;
+    mom_raw_load(src + rm + w.o16, src + rm + w.olo, w.raw[0]);
+    if (LD == 2) mom_raw_load(src + r0 + w.o16, src + r0 + w.olo, w.raw[1]);
+  }
 #pragma unroll
   for (int k = 0; k < 9; k++) w.Fa[k] = w.Fb[k] = w.Fc[k] = make_float2(0.f, 0.f);
-  w.ok = true;
+  w.rmax = w.jmax = 0.f;
   w.probe = 0.f;
   // the last group may run past the domain's last row: rows past it load
   // nothing and store nothing
 #pragma unroll 1
   for (int j = -1; j <= NPT && y0 + j - 1 < a.m; j += 3) {
-    mom_walk_row<MODEL, NPT, PF, 0>(a, w, j, y0, wx, x0, lane, inx, owner, hseed);
-    mom_walk_row<MODEL, NPT, PF, 1>(a, w, j + 1, y0, wx, x0, lane, inx, owner, hseed);
-    mom_walk_row<MODEL, NPT, PF, 2>(a, w, j + 2, y0, wx, x0, lane, inx, owner, hseed);
+    mom_walk_row<MODEL, NPT, PF, LD, 0>(a, w, j, y0, wx, x0, lane, owner, hseed);
+    mom_walk_row<MODEL, NPT, PF, LD, 1>(a, w, j + 1, y0, wx, x0, lane, owner, hseed);
+    mom_walk_row<MODEL, NPT, PF, LD, 2>(a, w, j + 2, y0, wx, x0, lane, owner, hseed);
   }
-  mom_flag(a, w.ok, w.probe);
+  mom_flag(a, w.rmax <= a.fx_rlim && w.jmax <= a.fx_jlim, w.probe);
 }
 
 // Nodes with boundary work (class 3) and their fluid neighbours (class 2),

@@ -14,10 +14,10 @@ __global__ void __launch_bounds__(256) k_resid_mom(const __grid_constant__ StepA
 
 template <int MODEL>
 void fill_mom_model(MomKernels &t) {
-  t.step[MODEL][0] = (const void *)k_step_mom<MODEL, MOM_NPT[0], MOM_MINB[0], MOM_PFL[0]>;
-  t.step[MODEL][1] = (const void *)k_step_mom<MODEL, MOM_NPT[1], MOM_MINB[1], MOM_PFL[1]>;
-  t.step[MODEL][2] = (const void *)k_step_mom<MODEL, MOM_NPT[2], MOM_MINB[2], MOM_PFL[2]>;
-  t.step[MODEL][3] = (const void *)k_step_mom<MODEL, MOM_NPT[3], MOM_MINB[3], MOM_PFL[3]>;
+  t.step[MODEL][0] = (const void *)k_step_mom<MODEL, MOM_NPT[0], MOM_MINB[0], MOM_PFL[0], MOM_LD[0]>;
+  t.step[MODEL][1] = (const void *)k_step_mom<MODEL, MOM_NPT[1], MOM_MINB[1], MOM_PFL[1], MOM_LD[1]>;
+  t.step[MODEL][2] = (const void *)k_step_mom<MODEL, MOM_NPT[2], MOM_MINB[2], MOM_PFL[2], MOM_LD[2]>;
+  t.step[MODEL][3] = (const void *)k_step_mom<MODEL, MOM_NPT[3], MOM_MINB[3], MOM_PFL[3], MOM_LD[3]>;
   static_assert(MOM_NVAR == 4, "moment tile table");
   t.special[MODEL] = (const void *)k_special_mom<MODEL>;
   t.init[MODEL] = (const void *)k_init_mom<MODEL>;

@@ -60,11 +60,16 @@ constexpr TileVariant VARS[NVAR] = {
 // Bulk-step tiles of the moment storage: blocks of 4 warps x 60 columns, these
 // rows per thread.
 constexpr int MOM_NVAR = 4;
-constexpr int MOM_NPT[MOM_NVAR] = {16, 34, 34, 34};  // (NPT + 2) % 3 == 0
-constexpr int MOM_MINB[MOM_NVAR] = {4, 4, 4, 3};     // resident blocks per SM (register cap)
-constexpr bool MOM_PFL[MOM_NVAR] = {true, false, true, true};  // L2 prefetch of the rows ahead
+constexpr int MOM_NPT[MOM_NVAR] = {34, 34, 64, 64};  // (NPT + 2) % 3 == 0
+constexpr int MOM_MINB[MOM_NVAR] = {4, 5, 4, 5};     // resident blocks per SM (register cap)
+constexpr bool MOM_PFL[MOM_NVAR] = {true, true, true, true};  // L2 prefetch of the rows ahead
+constexpr int MOM_LD[MOM_NVAR] = {2, 1, 2, 1};       // source rows loaded this many rows ahead
 constexpr int TMA_MAX_SMEM = 200 * 1024;  // dynamic shared memory budget of one TMA block
 constexpr int TMA_MAX_STAGES = 4;
+
+// Scale of the stored FP16 non-equilibrium moments of the moment storage
+// (a power of two: stored = neq_s x value).
+constexpr float MOM_NEQ_S = 4096.f;
 
 constexpr int NSUM = 10;  // finish-kernel reduction lanes
 enum SumLane : int {
@@ -103,6 +108,11 @@ struct StepArgs {
   float neq_s, neq_is;      // scale of the stored non-equilibrium moments and its inverse
   unsigned gen;             // generation written by this launch (seed of the rounding dither)
   float f_rho0, f_om, f_omA;  // rho0, omega, omegaA in FP32 (moment storage)
+  float f_i4rho0;           // 1 / (4 rho0) in FP32 (moment storage)
+  float fx_enc[2];          // 64 / fx_rho and 32 / fx_j: the scaled codes of the dithered rounding
+  float fx_rlim, fx_jlim;   // largest |rho - rho0| and |j| whose codes stay within the range
+  float enc_c[6];           // storage references from codes: 2 S h_r, -3 S h_j^2, -S h_r,
+                            // 3 S h_j^2, S h_j, -S h_j^2 / rho0 (S = neq_s, h = fixed-point steps)
 };
 
 // Outputs of the read-only finish kernel (any pointer may be null).

@@ -49,8 +49,8 @@ def test_fp16neq_against_fp64(name):
 
 @pytest.mark.parametrize("tile", [1, 2, 3, 4])
 def test_every_tile_against_fp64(tile):
-    """The four bulk tiles (16 or 34 rows per thread, with or without L2
-    prefetch, 4 or 3 blocks per SM) do the same arithmetic per node, but the
+    """The four bulk tiles (34 or 64 rows per thread, source rows loaded one
+    or two rows ahead, 4 or 5 blocks per SM) do the same arithmetic per node, but the
     compiler may fuse multiply-adds differently in each; a
     last-bit difference can move a dithered fixed-point code by one step, so
     the tiles are not bitwise equal: each meets the FP64 tolerances."""

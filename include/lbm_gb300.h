@@ -208,7 +208,16 @@ lbm_status lbm_batch_set_state(lbm_batch *b, int32_t case_index, const double *r
                                const double *u, const double *v);
 /* Fixes the batched step's tile shape (0..3: 128x1, 64x4, 128x2, 128x4 threads x rows). */
 lbm_status lbm_batch_set_tile(lbm_batch *b, int32_t tile_variant);
-/* Times the batched step's tile shapes and keeps the fastest (before stepping). */
+/* Fixes the boundary-node pass's grid of FP32 / FP16-dev batches: 0 = one
+ * thread per list entry, k = k blocks per multiprocessor walking the list
+ * (the results do not depend on it).  No counterpart in the reference (its
+ * loop steps one domain). */
+lbm_status lbm_batch_set_special_blocks(lbm_batch *b, int32_t blocks_per_sm);
+/* Times the batched step's tile shapes and keeps the fastest (before stepping);
+ * for FP32 and FP16-dev batches then also the boundary-node pass's blocks per
+ * multiprocessor (one thread per entry, or a grid of 2, 4 or 8 blocks per SM
+ * that leaves block slots to the bulk pass running alongside).  The report is
+ * JSON: {"variant", "ms", "special_blocks_per_sm", "special_ms"}. */
 lbm_status lbm_batch_autotune(lbm_batch *b, int32_t steps_per_trial, char *report,
                               size_t report_cap);
 /* Steps every unconverged case until all have converged or max_steps have run

@@ -283,25 +283,19 @@ __device__ __noinline__ void batch_special_full(const StepArgs &a, long long nod
   step_special_rec<ST, MODEL>(a, node, a.rec[rec]);
 }
 
-// Boundary-node pass of the per-tile batches (FP32, FP16-dev): one thread per
-// entry of the (case, node, record, flags) list.  The case arguments are
-// assembled in registers from the 128-byte BulkArgs of the case's parity and
-// its SpecExtra, both read once, so the chain of dependent loads per node is
+// One entry (case, node, record, flags) of the boundary-node pass of the
+// per-tile batches (FP32, FP16-dev).  The case arguments are assembled in
+// registers from the 128-byte BulkArgs of the case's parity and its
+// SpecExtra, both read once, so the chain of dependent loads per node is
 // entry -> (parity, arguments, record) -> populations, and no argument is
 // reloaded after the node's stores.  Nodes of an extrapolating outlet take
 // the full path with the arguments in global memory.
 template <class ST, int MODEL>
-__global__ void __launch_bounds__(128) k_batch_special_c(const BulkArgs *__restrict__ args,
-                                                         const SpecExtra *__restrict__ extra,
-                                                         const BatchCase *__restrict__ cases,
-                                                         const int4 *__restrict__ list,
-                                                         const int *__restrict__ nlist_live,
-                                                         const int *__restrict__ active,
-                                                         const int *__restrict__ gpar) {
-  const int nlist = __ldg(nlist_live);
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nlist) return;
-  const int4 e = __ldg(&list[i]);
+__device__ __forceinline__ void batch_special_entry(const BulkArgs *__restrict__ args,
+                                                    const SpecExtra *__restrict__ extra,
+                                                    const BatchCase *__restrict__ cases,
+                                                    const int4 e, const int *__restrict__ active,
+                                                    const int *__restrict__ gpar) {
   if (!__ldg(&active[e.x])) return;
   const int par = __ldg(&gpar[e.x]) & 1;
   const SpecExtra &x = extra[e.x];
@@ -334,6 +328,23 @@ __global__ void __launch_bounds__(128) k_batch_special_c(const BulkArgs *__restr
       out[k] = M[k];
     }
   }
+}
+
+// Boundary-node pass of the per-tile batches over the whole list.
+template <class ST, int MODEL>
+__global__ void __launch_bounds__(128) k_batch_special_c(const BulkArgs *__restrict__ args,
+                                                         const SpecExtra *__restrict__ extra,
+                                                         const BatchCase *__restrict__ cases,
+                                                         const int4 *__restrict__ list,
+                                                         const int *__restrict__ nlist_live,
+                                                         const int *__restrict__ active,
+                                                         const int *__restrict__ gpar) {
+  const int nlist = __ldg(nlist_live);
+  // grid-stride: the host may launch fewer blocks than entries, so that this
+  // latency-bound pass holds a few block slots per SM and the bulk pass,
+  // launched alongside, keeps the rest
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nlist; i += gridDim.x * blockDim.x)
+    batch_special_entry<ST, MODEL>(args, extra, cases, __ldg(&list[i]), active, gpar);
 }
 
 // The planes the boundary-node pass did not write (WRec::exported clear),

@@ -71,6 +71,8 @@ struct lbm_batch {
   int4 *d_live_tiles = nullptr;   // compacted work lists of the cases still stepping
   int *d_live_n = nullptr;        // [0]: live tiles
   int variant = 1;
+  int special_bps = 0;        // boundary-node pass: blocks per SM (0: one thread per entry)
+  int sms = 152;              // multiprocessors of the device
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;  // boundary-node pass, concurrent with the bulk pass
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -78,7 +80,7 @@ struct lbm_batch {
   const lbm::BatchKernels *bk = nullptr;
   int *d_err = nullptr;
   cudaGraphExec_t graph = nullptr;
-  int graph_k = -1, graph_var = -1;
+  int graph_k = -1, graph_var = -1, graph_bps = -1;
   double graph_tol = -1;
   int64_t dev_bytes = 0;
   long long nodes = 0, fluid = 0;
@@ -226,9 +228,12 @@ lbm_status launch_steps(lbm_batch *b, int k) {
       void *sargs[] = {&b->d_cases, &b->d_special, &b->d_nspecial, &b->s.active, &b->s.gpar};
       void *cargs[] = {&b->d_bulk,     &b->d_extra,    &b->d_cases, &b->d_special,
                        &b->d_nspecial, &b->s.active, &b->s.gpar};
-      // k_batch_special_c: one thread per entry; k_batch_special: grid-stride
-      const int sg = b->bk->per_tile ? (b->nspecial + 127) / 128
-                                     : std::min((b->nspecial + 127) / 128, 152 * 16);
+      // both grid-stride; k_batch_special_c one thread per entry unless
+      // special_bps caps its blocks per SM (lbm_batch_autotune's choice)
+      const int need = (b->nspecial + 127) / 128;
+      const int sg = b->bk->per_tile
+                         ? (b->special_bps > 0 ? std::min(need, b->sms * b->special_bps) : need)
+                         : std::min(need, b->sms * 16);
       e = cudaLaunchKernel(b->bk->special[b->model], dim3(sg), dim3(128),
                            b->bk->per_tile ? cargs : sargs, 0, b->side);
       if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch special: ") + cudaGetErrorString(e));
@@ -270,7 +275,8 @@ lbm_status launch_check(lbm_batch *b, int k, double tol) {
 
 // One graph = check_every steps followed by one convergence check.
 lbm_status ensure_graph(lbm_batch *b, int k, double tol) {
-  if (b->graph && b->graph_k == k && b->graph_var == b->variant && b->graph_tol == tol)
+  if (b->graph && b->graph_k == k && b->graph_var == b->variant && b->graph_bps == b->special_bps &&
+      b->graph_tol == tol)
     return LBM_OK;
   if (b->graph) {
     cudaGraphExecDestroy(b->graph);
@@ -288,6 +294,7 @@ lbm_status ensure_graph(lbm_batch *b, int k, double tol) {
   if (e != cudaSuccess) return fail(LBM_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
   b->graph_k = k;
   b->graph_var = b->variant;
+  b->graph_bps = b->special_bps;
   b->graph_tol = tol;
   return LBM_OK;
 }
@@ -326,6 +333,9 @@ lbm_status lbm_batch_create(const lbm_mesh *meshes, const lbm_params *params, in
     default: b->ks = &lbm::kernels_f16(); b->bk = &lbm::batch_kernels_2(); break;
   }
   if (cudaSetDevice(p0.device) != cudaSuccess) return bail(fail(LBM_CUDA, "cudaSetDevice failed"));
+  if (cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, p0.device) != cudaSuccess ||
+      b->sms < 1)
+    b->sms = 152;
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
       !create_side_stream(&b->side) ||
       cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
@@ -589,6 +599,13 @@ lbm_status lbm_batch_set_tile(lbm_batch *b, int32_t tile_variant) {
   return LBM_OK;
 }
 
+lbm_status lbm_batch_set_special_blocks(lbm_batch *b, int32_t blocks_per_sm) {
+  if (!b || blocks_per_sm < 0 || blocks_per_sm > 16)
+    return fail(LBM_INVALID, "blocks per SM must be 0 (one thread per entry) .. 16");
+  b->special_bps = blocks_per_sm;
+  return LBM_OK;
+}
+
 lbm_status lbm_batch_set_rest(lbm_batch *b) {
   if (!b) return fail(LBM_INVALID, "null argument");
   LBM_BCK(cudaSetDevice(b->device));
@@ -642,10 +659,7 @@ lbm_status lbm_batch_autotune(lbm_batch *b, int32_t steps_per_trial, char *repor
   cudaEvent_t e0, e1;
   LBM_BCK(cudaEventCreate(&e0));
   LBM_BCK(cudaEventCreate(&e1));
-  double ms[lbm::BVAR];
-  int best = 0;
-  for (int v = 0; v < lbm::BVAR && s == LBM_OK; v++) {
-    b->variant = v;
+  auto trial = [&](double *out) {
     s = launch_steps(b, 2);
     cudaEventRecord(e0, b->stream);
     if (s == LBM_OK) s = launch_steps(b, steps_per_trial);
@@ -653,19 +667,42 @@ lbm_status lbm_batch_autotune(lbm_batch *b, int32_t steps_per_trial, char *repor
     cudaEventSynchronize(e1);
     float t = 0.f;
     cudaEventElapsedTime(&t, e0, e1);
-    ms[v] = (double)t / steps_per_trial;
+    *out = (double)t / steps_per_trial;
+  };
+  // bulk tiles first (boundary pass one thread per entry), then the
+  // boundary pass's blocks per SM with the chosen tile: fewer blocks leave
+  // block slots to the bulk pass that runs alongside
+  constexpr int kBps[4] = {0, 2, 4, 8};
+  double ms[lbm::BVAR], bms[4] = {0, 0, 0, 0};
+  int best = 0, best_bps = 0;
+  b->special_bps = 0;
+  for (int v = 0; v < lbm::BVAR && s == LBM_OK; v++) {
+    b->variant = v;
+    trial(&ms[v]);
     if (ms[v] < ms[best]) best = v;
+  }
+  b->variant = best;
+  const bool tune_bps = b->bk->per_tile && b->nspecial > 0;
+  for (int i = 0; i < 4 && tune_bps && s == LBM_OK; i++) {
+    b->special_bps = kBps[i];
+    trial(&bms[i]);
+    if (bms[i] < bms[best_bps]) best_bps = i;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   b->have_state = false;
   if (s != LBM_OK) return s;
-  b->variant = best;
+  b->special_bps = kBps[best_bps];
   if (report && report_cap > 0) {
     std::string r = "{\"variant\": " + std::to_string(best) + ", \"ms\": [";
     char buf[32];
     for (int v = 0; v < lbm::BVAR; v++) {
       std::snprintf(buf, sizeof buf, "%s%.5f", v ? ", " : "", ms[v]);
+      r += buf;
+    }
+    r += "], \"special_blocks_per_sm\": " + std::to_string(b->special_bps) + ", \"special_ms\": [";
+    for (int i = 0; i < 4; i++) {
+      std::snprintf(buf, sizeof buf, "%s%.5f", i ? ", " : "", bms[i]);
       r += buf;
     }
     r += "]}";

@@ -55,6 +55,7 @@ def test_batch_tiles_and_autotune(precision):
     ref = None
     rep = G.Batch(cs, precision=precision).autotune(2)
     assert 0 <= rep["variant"] < 4 and len(rep["ms"]) == 4
+    assert rep["special_blocks_per_sm"] in (0, 2, 4, 8) and len(rep["special_ms"]) == 4
     for tile in range(4):
         b = G.Batch(cs, precision=precision)
         b.set_tile(tile)
@@ -126,3 +127,27 @@ def test_batch_outlet_kinds_match_single_contexts(precision):
         assert err <= 1e-5, (c, err)
         assert np.abs(got["rho"] - want["rho"]).max() <= 1e-6
     b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16dev"])
+def test_boundary_pass_grid_does_not_change_results(precision):
+    """The boundary-node pass walks its list grid-stride: one thread per entry
+    or a few blocks per multiprocessor give the same arithmetic per node, so
+    the fields are bitwise equal."""
+    cs = batch_cases(3)
+    ref = None
+    for bps in (0, 1, 2, 8):
+        b = G.Batch(cs, precision=precision)
+        b.set_tile(1)
+        b.set_special_blocks(bps)
+        b.set_rest()
+        r = b.run(60, check_every=30, tol=-1.0)
+        assert (r["steps"] == 60).all()
+        f = [b.fields(c) for c in range(len(cs))]
+        b.close()
+        if ref is None:
+            ref = f
+            continue
+        for c in range(len(cs)):
+            for k in ("rho", "u", "v"):
+                assert np.array_equal(f[c][k], ref[c][k]), (bps, c, k)

@@ -384,6 +384,13 @@ def run_gpu(args):
         rho_o = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
         u_o = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
         v_o = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+        # one untimed pass of the same calls first: the first device access to
+        # freshly pinned host pages and the first launch of each kernel cost
+        # once per process (3-4x the steady set_state time on the GB300 host)
+        solver.set_state(None, rho_h.numpy(), u_h.numpy(), v_h.numpy())
+        solver.step(1, 1)
+        assert solver.L.lbm_get_fields(solver.h, rho_o.ctypes.data, u_o.ctypes.data,
+                                       v_o.ctypes.data, None, None) == 0
         barrier(ws)
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
@@ -403,7 +410,8 @@ def run_gpu(args):
                "h2d_bytes_per_step": int(3 * 8 * N / args.steps),
                "d2h_bytes_per_step": int(32 + 3 * 8 * N / args.steps),
                "what": "lbm_set_state(host rho,u,v) + steps x lbm_step(1, residual line) + "
-                       "lbm_get_fields(host rho,u,v), wall clock",
+                       "lbm_get_fields(host rho,u,v), wall clock, after one untimed pass of "
+                       "the same calls",
                "phases_ms": {"set_state": round((t1 - t0) * 1e3, 2),
                              "steps": round((t2 - t1) * 1e3, 2),
                              "get_fields": round((t3 - t2) * 1e3, 2)}}

@@ -636,15 +636,24 @@ lbm_status lbm_get_fields(lbm_ctx *ctx, double *rho, double *u, double *v, doubl
   double **dev[5] = {&o.rho, &o.u, &o.v, &o.f, &o.metaf};
   size_t cnt[5] = {N, N, N, 9 * N, 9 * N};
   lbm_status s = LBM_OK;
-  for (int i = 0; i < 5 && s == LBM_OK; i++)
-    if (host[i] && cudaMallocAsync((void **)dev[i], cnt[i] * 8, ctx->stream) != cudaSuccess)
+  // rho, u, v go through the set_state field buffers, in place: the finish
+  // kernel reads a solid cell's reported value and writes the same element,
+  // and the fluid cells' entries are not read again before the next
+  // lbm_set_state refills them.  F and METAF need device temporaries.
+  double *fields[3] = {ctx->d_rho0, ctx->d_u0, ctx->d_v0};
+  for (int i = 0; i < 5 && s == LBM_OK; i++) {
+    if (!host[i]) continue;
+    if (i < 3)
+      *dev[i] = fields[i];
+    else if (cudaMallocAsync((void **)dev[i], cnt[i] * 8, ctx->stream) != cudaSuccess)
       s = fail(LBM_NOMEM, "device temporary for field read-back");
+  }
   if (s == LBM_OK) s = launch_finish(ctx, o);
   for (int i = 0; i < 5 && s == LBM_OK; i++)
     if (host[i] && cudaMemcpyAsync(host[i], *dev[i], cnt[i] * 8, cudaMemcpyDeviceToHost,
                                    ctx->stream) != cudaSuccess)
       s = fail(LBM_CUDA, "field read-back failed");
-  for (int i = 0; i < 5; i++)
+  for (int i = 3; i < 5; i++)
     if (*dev[i]) cudaFreeAsync(*dev[i], ctx->stream);
   LBM_CK(cudaStreamSynchronize(ctx->stream));
   return s;

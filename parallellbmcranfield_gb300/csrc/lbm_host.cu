@@ -526,6 +526,14 @@ lbm_status lbm_create(const lbm_mesh *mesh, const lbm_params *params, lbm_ctx **
     a.enc_c[3] = (float)(3.0 * S * hj * hj);
     a.enc_c[4] = (float)(S * hj);
     a.enc_c[5] = (float)(-S * hj * hj / r0);
+    // relaxation rates of the moment collision (collide_mom): MRT 1.4, 1.2,
+    // omega (serial/CellFunctions.c:401-438); TRT omega, omegaA, omega; BGK omega
+    const int model = params->collision_model;
+    const double s12 = model == 3 ? 1.4 : P.omega;
+    const double s46 = model == 3 ? 1.2 : (model == 2 ? P.omegaA : P.omega);
+    const double es[9] = {3.0 * S * s12, -2.0 * S * s12, S * s12, -3.0 * S * s12, S * (1.0 - s12),
+                          -S * s46, S * (1.0 - s46), S * P.omega, S * (1.0 - P.omega)};
+    for (int k = 0; k < 9; k++) a.enc_s[k] = (float)es[k];
     a.f_rho0 = (float)a.rho0;
     a.f_om = (float)a.omega;
     a.f_omA = (float)a.omegaA;

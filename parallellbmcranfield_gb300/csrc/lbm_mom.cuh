@@ -397,37 +397,23 @@ __device__ __forceinline__ void pops_to_mom2(const float2 d[9], float2 &r, float
   m[5] = sub2(p57, p68);
 }
 
-// collide_mom on pairs.
+// Collision (collide_mom on pairs) and encoding of a pair's pulled moments
+// (r, j and the pre-collision non-equilibrium moments m), and the stores of
+// the nodes whose `own` flag is set (both: full words; one: its own
+// elements).  Each stored value is one expression: with the relaxation rate
+// s_i, the equilibrium e_i of the pulled r, j and the storage reference b_i
+// of the stored (rounded) r, j,
+//   n_i = S (m_i - s_i (m_i - e_i) - b_i) = S (1 - s_i) m_i + S s_i e_i - S b_i
+// (S = neq_s; the products S s_i and S (1 - s_i) come from the host).  The
+// largest |rho - rho0| and |j| of the stored nodes go to rmax / jmax (the
+// caller compares them with the fixed-point range once, at the end of its
+// walk), their density deviation and stored n_7 to the NaN probe.
 template <int MODEL>
-__device__ __forceinline__ void collide_mom2(float2 r, float2 jx, float2 jy, float2 m[6],
-                                            const StepArgs &a) {
-  const float2 rho = add2(bc2(a.f_rho0), r);
-  // 1 / rho enters only the equilibria of the non-conserved moments, whose
-  // stored form keeps 11 bits: the approximate reciprocal is ample
-  const float2 inv = make_float2(__fdividef(1.f, rho.x), __fdividef(1.f, rho.y));
-  const float2 jj = fma2(jx, jx, mul2(jy, jy));
-  const float2 q = MODEL == 3 ? jj : mul2(jj, inv);
-  const float2 e1 = fma2(bc2(3.f), q, mul2(bc2(-2.f), r)), e2 = fma2(bc2(-3.f), q, r);
-  const float2 e7 = mul2(mul2(sub2(jx, jy), add2(jx, jy)), inv), e8 = mul2(mul2(jx, jy), inv);
-  const float om = a.f_om;
-  const float s12 = MODEL == 3 ? 1.4f : om;
-  const float s46 = MODEL == 3 ? 1.2f : (MODEL == 2 ? a.f_omA : om);
-  m[0] = fma2(bc2(-s12), sub2(m[0], e1), m[0]);
-  m[1] = fma2(bc2(-s12), sub2(m[1], e2), m[1]);
-  m[2] = fma2(bc2(-s46), add2(m[2], jx), m[2]);
-  m[3] = fma2(bc2(-s46), add2(m[3], jy), m[3]);
-  m[4] = fma2(bc2(-om), sub2(m[4], e7), m[4]);
-  m[5] = fma2(bc2(-om), sub2(m[5], e8), m[5]);
-}
-
-// Encodes the post-collision moments of a pair and stores the nodes whose
-// `own` flag is set (both: full words; one: its own elements).  The largest
-// |rho - rho0| and |j| of the stored nodes go to rmax / jmax: the caller
-// compares them with the fixed-point range once, at the end of its walk.
-__device__ __forceinline__ void mom_encode_store2(const StepArgs &a, char *p16, char *plo,
-                                                  long long z, uint32_t hseed, float2 r, float2 jx,
-                                                  float2 jy, const float2 m[6], bool own0,
-                                                  bool own1, float &rmax, float &jmax) {
+__device__ __forceinline__ void mom_collide_store2(const StepArgs &a, char *p16, char *plo,
+                                                   long long z, uint32_t hseed, float2 r,
+                                                   float2 jx, float2 jy, const float2 m[6],
+                                                   bool own0, bool own1, float &rmax, float &jmax,
+                                                   float &probe) {
   // Dithered codes in integers: R = round(2^D v / step), t = (R + u) >> D
   // with u uniform in 0 .. 2^D - 1, so that E[t] = R / 2^D, within 2^-(D+1)
   // of v / step.  The pair's dithers come from one hash: node 0 in bits
@@ -456,21 +442,41 @@ __device__ __forceinline__ void mom_encode_store2(const StepArgs &a, char *p16, 
     rmax = fmaxf(rmax, fabsf(r.y));
     jmax = fmaxf(jmax, fmaxf(fabsf(jx.y), fabsf(jy.y)));
   }
-  // minus the references b_i (times neq_s) of the stored conserved moments,
-  // from the codes with the fixed-point steps folded into the constants
-  // (enc_c), so that each stored value is one multiply-add
+  // -S b_i of the stored conserved moments, from the codes with the
+  // fixed-point steps folded into the constants (enc_c)
   const float2 qr = qf[0], qx = qf[1], qy = qf[2];
   const float2 qyy = mul2(qy, qy);
-  const float2 jj = fma2(qx, qx, qyy);
-  const float2 xmy = fma2(bc2(-2.f), qyy, jj);
+  const float2 qjj = fma2(qx, qx, qyy);
+  const float2 qxmy = fma2(bc2(-2.f), qyy, qjj);
   const float2 c5 = bc2(a.enc_c[5]), c4 = bc2(a.enc_c[4]);
-  const float2 mref[6] = {fma2(jj, bc2(a.enc_c[1]), mul2(qr, bc2(a.enc_c[0]))),
-                          fma2(jj, bc2(a.enc_c[3]), mul2(qr, bc2(a.enc_c[2]))), mul2(qx, c4),
-                          mul2(qy, c4), mul2(xmy, c5), mul2(mul2(qx, qy), c5)};
+  const float2 mref[6] = {fma2(qjj, bc2(a.enc_c[1]), mul2(qr, bc2(a.enc_c[0]))),
+                          fma2(qjj, bc2(a.enc_c[3]), mul2(qr, bc2(a.enc_c[2]))), mul2(qx, c4),
+                          mul2(qy, c4), mul2(qxmy, c5), mul2(mul2(qx, qy), c5)};
+  // equilibria of the pulled r, j (the reference's MRT: e_1 = -2 r + 3 |j|^2,
+  // e_2 = r - 3 |j|^2, e_4 = -j_x, e_6 = -j_y, e_7 = (j_x^2 - j_y^2) / rho,
+  // e_8 = j_x j_y / rho; BGK and TRT with |j|^2 / rho).  1 / rho enters only
+  // the equilibria of the non-conserved moments, whose stored form keeps 11
+  // bits: the approximate reciprocal is ample
+  const float2 rho = add2(bc2(a.f_rho0), r);
+  const float2 inv = make_float2(__fdividef(1.f, rho.x), __fdividef(1.f, rho.y));
+  const float2 jyy = mul2(jy, jy);
+  const float2 jj = fma2(jx, jx, jyy);
+  const float2 q = MODEL == 3 ? jj : mul2(jj, inv);
+  const float2 e7 = mul2(fma2(bc2(-2.f), jyy, jj), inv), e8 = mul2(mul2(jx, jy), inv);
+  const float *es = a.enc_s;  // S s_12 x (3, -2, 1, -3), S (1 - s_12), -S s_46, S (1 - s_46), S om, S (1 - om)
+  float2 n[6];
+  n[0] = fma2(m[0], bc2(es[4]), fma2(q, bc2(es[0]), fma2(r, bc2(es[1]), mref[0])));
+  n[1] = fma2(m[1], bc2(es[4]), fma2(q, bc2(es[3]), fma2(r, bc2(es[2]), mref[1])));
+  n[2] = fma2(m[2], bc2(es[6]), fma2(jx, bc2(es[5]), mref[2]));
+  n[3] = fma2(m[3], bc2(es[6]), fma2(jy, bc2(es[5]), mref[3]));
+  n[4] = fma2(m[4], bc2(es[8]), fma2(e7, bc2(es[7]), mref[4]));
+  n[5] = fma2(m[5], bc2(es[8]), fma2(e8, bc2(es[7]), mref[5]));
+  if (own0) probe += r.x + n[4].x;
+  if (own1) probe += r.y + n[4].y;
   uint32_t nw[6];
 #pragma unroll
   for (int i = 0; i < 6; i++) {
-    const __half2 hh = __float22half2_rn(fma2(m[i], bc2(MOM_NEQ_S), mref[i]));
+    const __half2 hh = __float22half2_rn(n[i]);
     memcpy(&nw[i], &hh, 4);
   }
   if (own0 && own1) {
@@ -545,19 +551,21 @@ __device__ __forceinline__ void mom_walk_row(const StepArgs &a, MomWalk &w, int 
   const uint32_t cw = j >= 1 && owner && y < a.m
                           ? __ldg((const unsigned short *)(a.cls + (long long)y * a.pitch + x0))
                           : 0u;
-  if (PF && lane < 24) {
+  if (PF) {
     // one 128-byte line per lane: the warp's span of a row is one or two
     // whole chunks (at most 2688 bytes, 22 lines at a 64-byte offset) for
     // lanes 0..21, the span's class bytes (64 bytes, at most two lines) for
-    // lanes 22 and 23; the last address of each is clamped into the span
+    // lanes 22 and 23; the last address of each is clamped into the span.
+    // A predicated instruction, not a branch: lanes 24..31 and rows past
+    // the domain issue nothing (their addresses are formed, not used).
     const int rp = r + MOM_PF;
-    if (rp < a.m && j + MOM_PF <= NPT) {
-      const char *p =
-          lane < 22 ? src + (long long)rp * w.rowb + min(w.pf0 + 128 * lane, w.pf1 - 1)
-                    : (const char *)a.cls + (long long)rp * a.pitch +
-                          (lane == 22 ? max(wx - 2, 0) : min(wx + 61, a.pitch - 1));
-      asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-    }
+    const bool go = lane < 24 && rp < a.m && j + MOM_PF <= NPT;
+    const char *p = lane < 22 ? src + (long long)rp * w.rowb + min(w.pf0 + 128 * lane, w.pf1 - 1)
+                              : (const char *)a.cls + (long long)rp * a.pitch +
+                                    (lane == 22 ? max(wx - 2, 0) : min(wx + 61, a.pitch - 1));
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %1, 0;\n\t@p prefetch.global.L2 [%0];\n\t}" ::"l"(p),
+        "r"((unsigned)go));
   }
   float2 d[9];
   mom_decode2(a, w.raw[PH], d);
@@ -582,12 +590,9 @@ __device__ __forceinline__ void mom_walk_row(const StepArgs &a, MomWalk &w, int 
     // the nodes a lane owns are stored and counted
     float2 rr, jx, jy, m[6];
     pops_to_mom2(w.Fa, rr, jx, jy, m);
-    collide_mom2<MODEL>(rr, jx, jy, m, a);
-    if (own0) w.probe += rr.x + m[4].x;
-    if (own1) w.probe += rr.y + m[4].y;
     char *dst = (char *)a.dst + (long long)y * w.rowb;
-    mom_encode_store2(a, dst + w.o16, dst + w.olo, (long long)y * a.pitch + x0, hseed, rr, jx, jy,
-                      m, own0, own1, w.rmax, w.jmax);
+    mom_collide_store2<MODEL>(a, dst + w.o16, dst + w.olo, (long long)y * a.pitch + x0, hseed, rr,
+                              jx, jy, m, own0, own1, w.rmax, w.jmax, w.probe);
   }
 #pragma unroll
   for (int k = 0; k < 9; k++) {

@@ -113,6 +113,8 @@ struct StepArgs {
   float fx_rlim, fx_jlim;   // largest |rho - rho0| and |j| whose codes stay within the range
   float enc_c[6];           // storage references from codes: 2 S h_r, -3 S h_j^2, -S h_r,
                             // 3 S h_j^2, S h_j, -S h_j^2 / rho0 (S = neq_s, h = fixed-point steps)
+  float enc_s[9];           // collision folded into the encoding: 3 S s12, -2 S s12, S s12,
+                            // -3 S s12, S (1 - s12), -S s46, S (1 - s46), S om, S (1 - om)
 };
 
 // Outputs of the read-only finish kernel (any pointer may be null).

@@ -1241,17 +1241,25 @@ __global__ void __launch_bounds__(128, NPT == 2 ? 8 : 1) k_step_h2(const __grid_
   const int y0 = blockIdx.y * NPT;
   // L2 prefetch for the block a.pf_blocks launch positions ahead (a fraction
   // of a wave later): 9 planes x NPT rows of its 256-node tile, one 512-byte bulk
-  // prefetch each, so that its loads find their sectors in L2.  A hint only:
-  // no completion to wait for; every address lies inside the state array.
-  if (a.pf_blocks > 0 && threadIdx.x < 9 * NPT) {
+  // prefetch each, and its NPT rows of class bytes (256 bytes each: the
+  // first loads of a block, on which all others wait), so that its loads find
+  // their sectors in L2.  A hint only: no completion to wait for; every
+  // address lies inside the state or the class array (16-byte aligned: the
+  // pitch is a multiple of 256).
+  if (a.pf_blocks > 0 && threadIdx.x < 10 * NPT) {
     const long long L = (long long)blockIdx.y * gridDim.x + blockIdx.x + a.pf_blocks;
     if (L < (long long)gridDim.x * gridDim.y) {
       const int px = (int)(L % gridDim.x), py = (int)(L / gridDim.x);
       const int k = threadIdx.x / NPT, y = py * NPT + threadIdx.x % NPT;
-      const int plane = (PH == PH_AA_A) ? OPP[k] : k;
       if (y < a.m && px * 256 + 256 <= a.pitch) {
-        const T *p = (const T *)a.src + (long long)plane * a.plane + (long long)y * a.pitch + px * 256;
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], 512;" ::"l"(p) : "memory");
+        if (k < 9) {
+          const int plane = (PH == PH_AA_A) ? OPP[k] : k;
+          const T *p = (const T *)a.src + (long long)plane * a.plane + (long long)y * a.pitch + px * 256;
+          asm volatile("cp.async.bulk.prefetch.L2.global [%0], 512;" ::"l"(p) : "memory");
+        } else {
+          const uint8_t *p = a.cls + (long long)y * a.pitch + px * 256;
+          asm volatile("cp.async.bulk.prefetch.L2.global [%0], 256;" ::"l"(p) : "memory");
+        }
       }
     }
   }

@@ -208,16 +208,19 @@ lbm_status lbm_batch_set_state(lbm_batch *b, int32_t case_index, const double *r
                                const double *u, const double *v);
 /* Fixes the batched step's tile shape (0..3: 128x1, 64x4, 128x2, 128x4 threads x rows). */
 lbm_status lbm_batch_set_tile(lbm_batch *b, int32_t tile_variant);
-/* Fixes the boundary-node pass's grid of FP32 / FP16-dev batches: 0 = one
- * thread per list entry, k = k blocks per multiprocessor walking the list
- * (the results do not depend on it).  No counterpart in the reference (its
- * loop steps one domain). */
-lbm_status lbm_batch_set_special_blocks(lbm_batch *b, int32_t blocks_per_sm);
+/* Fixes the launch options of FP32 / FP16-dev batches that lbm_batch_autotune
+ * otherwise picks: the boundary-node pass's grid (0 = one thread per list
+ * entry, k = k blocks per multiprocessor walking the list) and the bulk
+ * pass's L2 prefetch of the tile a quarter of a wave of blocks ahead (0 or
+ * 1).  The results do not depend on either.  No counterpart in the
+ * reference (its loop steps one domain). */
+lbm_status lbm_batch_set_launch(lbm_batch *b, int32_t special_blocks_per_sm, int32_t bulk_prefetch);
 /* Times the batched step's tile shapes and keeps the fastest (before stepping);
  * for FP32 and FP16-dev batches then also the boundary-node pass's blocks per
  * multiprocessor (one thread per entry, or a grid of 2, 4 or 8 blocks per SM
- * that leaves block slots to the bulk pass running alongside).  The report is
- * JSON: {"variant", "ms", "special_blocks_per_sm", "special_ms"}. */
+ * that leaves block slots to the bulk pass running alongside), then the bulk
+ * pass's L2 prefetch.  The report is JSON: {"variant", "ms",
+ * "special_blocks_per_sm", "special_ms", "bulk_prefetch", "prefetch_ms"}. */
 lbm_status lbm_batch_autotune(lbm_batch *b, int32_t steps_per_trial, char *report,
                               size_t report_cap);
 /* Steps every unconverged case until all have converged or max_steps have run

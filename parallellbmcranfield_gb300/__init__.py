@@ -60,7 +60,7 @@ EXPORTS = ["lbm_status_string", "lbm_last_error", "lbm_create", "lbm_destroy", "
            "lbm_set_state", "lbm_step", "lbm_get_fields", "lbm_check", "lbm_check_noalloc",
            "lbm_get_info", "lbm_autotune",
            "lbm_inspect_mesh", "lbm_batch_create", "lbm_batch_destroy", "lbm_batch_set_rest", "lbm_batch_set_tile",
-           "lbm_batch_set_special_blocks",
+           "lbm_batch_set_launch",
            "lbm_batch_set_state",
            "lbm_batch_autotune", "lbm_batch_run", "lbm_batch_get_fields", "lbm_batch_dims",
            "lbm_batch_info", "lbm_mesh_read", "lbm_mesh_cavity", "lbm_mesh_channel", "lbm_mesh_write",
@@ -102,7 +102,7 @@ def load():
     L.lbm_batch_destroy.restype = None
     L.lbm_batch_set_rest.argtypes = [vp]
     L.lbm_batch_set_tile.argtypes = [vp, i32]
-    L.lbm_batch_set_special_blocks.argtypes = [vp, i32]
+    L.lbm_batch_set_launch.argtypes = [vp, i32, i32]
     L.lbm_batch_set_state.argtypes = [vp, i32, dp, dp, dp]
     L.lbm_batch_autotune.argtypes = [vp, i32, C.c_char_p, C.c_size_t]
     L.lbm_batch_run.argtypes = [vp, C.c_int64, i32, C.c_double, dp, dp, dp, C.POINTER(C.c_double)]
@@ -337,9 +337,9 @@ class Batch:
     def set_tile(self, variant):
         _check(self.L.lbm_batch_set_tile(self.h, int(variant)), "lbm_batch_set_tile")
 
-    def set_special_blocks(self, blocks_per_sm):
-        _check(self.L.lbm_batch_set_special_blocks(self.h, int(blocks_per_sm)),
-               "lbm_batch_set_special_blocks")
+    def set_launch(self, special_blocks_per_sm=0, bulk_prefetch=False):
+        _check(self.L.lbm_batch_set_launch(self.h, int(special_blocks_per_sm), int(bulk_prefetch)),
+               "lbm_batch_set_launch")
 
     def run(self, max_steps, check_every=100, tol=1e-6, raise_on_nan=True):
         nc = self.n_cases

@@ -152,15 +152,39 @@ __device__ __forceinline__ void bulk_column(const StepArgs &a, int x, int y0) {
 // and no shared-memory copy of the case arguments, so a block's loads go out
 // as soon as it starts and the hardware keeps every SM filled with blocks.
 // Blocks past the live count (the grid is sized for all tiles when the
-// graph is captured) return at once.
+// graph is captured) return at once.  With pf > 0 the first 10 x NPT threads
+// first prefetch into L2 the tile pf positions further down the live list
+// (a fraction of a wave of blocks later): its NPT rows of the nine planes
+// and of the class bytes, one bulk prefetch each (a hint, nothing waits for
+// it; rows inside the case, x + BX <= pitch since the pitch is a multiple of
+// 256, and every address 16-byte aligned).
 template <class ST, int MODEL, int BX, int NPT>
 __global__ void __launch_bounds__(BX) k_batch_bulk(const BulkArgs *__restrict__ args,
                                                    const int4 *__restrict__ tiles,
                                                    const int *__restrict__ ntiles_live,
                                                    const int *__restrict__ active,
-                                                   const int *__restrict__ gpar) {
+                                                   const int *__restrict__ gpar, int pf) {
+  static_assert(10 * NPT <= BX, "prefetch threads");
   const int t = blockIdx.x;
-  if (t >= __ldg(ntiles_live)) return;
+  const int nlive = __ldg(ntiles_live);
+  if (t >= nlive) return;
+  if (pf > 0 && threadIdx.x < 10 * NPT && t + pf < nlive) {
+    const int4 u = __ldg(&tiles[t + pf]);
+    const BulkArgs &q = args[2 * u.x + (__ldg(&gpar[u.x]) & 1)];
+    const int k = threadIdx.x / NPT, y = u.z * NPT + threadIdx.x % NPT;
+    if (y < q.m) {
+      const long long node = (long long)y * q.pitch + (long long)u.y * BX;
+      using T = typename ST::T;
+      if (k < 9) {
+        const T *p = (const T *)q.src + (long long)k * q.plane + node;
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "n"(BX * (int)sizeof(T))
+                     : "memory");
+      } else {
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(q.cls + node), "n"(BX)
+                     : "memory");
+      }
+    }
+  }
   const int4 tl = __ldg(&tiles[t]);
   if (!__ldg(&active[tl.x])) return;
   const BulkArgs &b = args[2 * tl.x + (__ldg(&gpar[tl.x]) & 1)];

@@ -72,6 +72,8 @@ struct lbm_batch {
   int *d_live_n = nullptr;        // [0]: live tiles
   int variant = 1;
   int special_bps = 0;        // boundary-node pass: blocks per SM (0: one thread per entry)
+  bool bulk_pf = false;       // bulk pass: L2 prefetch a quarter of a wave of blocks ahead
+  int bulk_pf_blocks[lbm::BVAR] = {};  // that distance per tile variant (0: not known yet)
   int sms = 152;              // multiprocessors of the device
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;  // boundary-node pass, concurrent with the bulk pass
@@ -80,7 +82,7 @@ struct lbm_batch {
   const lbm::BatchKernels *bk = nullptr;
   int *d_err = nullptr;
   cudaGraphExec_t graph = nullptr;
-  int graph_k = -1, graph_var = -1, graph_bps = -1;
+  int graph_k = -1, graph_var = -1, graph_bps = -1, graph_pf = -1;
   double graph_tol = -1;
   int64_t dev_bytes = 0;
   long long nodes = 0, fluid = 0;
@@ -210,6 +212,19 @@ lbm_status launch_steps(lbm_batch *b, int k) {
   const int grid = b->bk->per_tile ? b->ntiles[b->variant]
                                    : std::min(b->ntiles[b->variant], persistent_blocks(fn, bx, b->device));
   void *step_args0 = b->bk->per_tile ? (void *)b->d_bulk : (void *)b->d_cases;
+  // prefetch distance of the per-tile bulk pass: a quarter of a wave of
+  // resident blocks (the distance that served the single-domain 16-bit step)
+  int pf = 0;
+  if (b->bk->per_tile && b->bulk_pf) {
+    int &d = b->bulk_pf_blocks[b->variant];
+    if (d == 0) {
+      int per_sm = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, bx, 0) != cudaSuccess)
+        per_sm = 0;
+      d = per_sm > 0 ? std::max(1, per_sm * b->sms / 4) : -1;
+    }
+    pf = d > 0 ? d : 0;
+  }
   lbm_status st = launch_compact(b);
   if (st != LBM_OK) return st;
   int *cnt_t = b->d_live_n;
@@ -221,7 +236,8 @@ lbm_status launch_steps(lbm_batch *b, int k) {
       LBM_BCK(cudaEventRecord(b->ev_fork, b->stream));
       LBM_BCK(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
     }
-    void *args[] = {&step_args0, &b->d_live_tiles, &cnt_t, &b->s.active, &b->s.gpar};
+    // (k_batch_bulk's parameters; the persistent FP64 k_batch_step takes the first five)
+    void *args[] = {&step_args0, &b->d_live_tiles, &cnt_t, &b->s.active, &b->s.gpar, &pf};
     cudaError_t e = cudaLaunchKernel(fn, dim3(grid), dim3(bx), args, 0, b->stream);
     if (e != cudaSuccess) return fail(LBM_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
     if (b->nspecial > 0) {
@@ -276,6 +292,7 @@ lbm_status launch_check(lbm_batch *b, int k, double tol) {
 // One graph = check_every steps followed by one convergence check.
 lbm_status ensure_graph(lbm_batch *b, int k, double tol) {
   if (b->graph && b->graph_k == k && b->graph_var == b->variant && b->graph_bps == b->special_bps &&
+      b->graph_pf == (int)b->bulk_pf &&
       b->graph_tol == tol)
     return LBM_OK;
   if (b->graph) {
@@ -295,6 +312,7 @@ lbm_status ensure_graph(lbm_batch *b, int k, double tol) {
   b->graph_k = k;
   b->graph_var = b->variant;
   b->graph_bps = b->special_bps;
+  b->graph_pf = (int)b->bulk_pf;
   b->graph_tol = tol;
   return LBM_OK;
 }
@@ -599,10 +617,13 @@ lbm_status lbm_batch_set_tile(lbm_batch *b, int32_t tile_variant) {
   return LBM_OK;
 }
 
-lbm_status lbm_batch_set_special_blocks(lbm_batch *b, int32_t blocks_per_sm) {
-  if (!b || blocks_per_sm < 0 || blocks_per_sm > 16)
+lbm_status lbm_batch_set_launch(lbm_batch *b, int32_t special_blocks_per_sm,
+                                int32_t bulk_prefetch) {
+  if (!b || special_blocks_per_sm < 0 || special_blocks_per_sm > 16)
     return fail(LBM_INVALID, "blocks per SM must be 0 (one thread per entry) .. 16");
-  b->special_bps = blocks_per_sm;
+  if (bulk_prefetch != 0 && bulk_prefetch != 1) return fail(LBM_INVALID, "bulk_prefetch is 0 or 1");
+  b->special_bps = special_blocks_per_sm;
+  b->bulk_pf = bulk_prefetch != 0;
   return LBM_OK;
 }
 
@@ -673,9 +694,10 @@ lbm_status lbm_batch_autotune(lbm_batch *b, int32_t steps_per_trial, char *repor
   // boundary pass's blocks per SM with the chosen tile: fewer blocks leave
   // block slots to the bulk pass that runs alongside
   constexpr int kBps[4] = {0, 2, 4, 8};
-  double ms[lbm::BVAR], bms[4] = {0, 0, 0, 0};
+  double ms[lbm::BVAR], bms[4] = {0, 0, 0, 0}, pms[2] = {0, 0};
   int best = 0, best_bps = 0;
   b->special_bps = 0;
+  b->bulk_pf = false;
   for (int v = 0; v < lbm::BVAR && s == LBM_OK; v++) {
     b->variant = v;
     trial(&ms[v]);
@@ -688,6 +710,15 @@ lbm_status lbm_batch_autotune(lbm_batch *b, int32_t steps_per_trial, char *repor
     trial(&bms[i]);
     if (bms[i] < bms[best_bps]) best_bps = i;
   }
+  // then the bulk pass's L2 prefetch of the tile a quarter of a wave ahead
+  b->special_bps = kBps[best_bps];
+  bool pf = false;
+  for (int i = 0; i < 2 && b->bk->per_tile && s == LBM_OK; i++) {
+    b->bulk_pf = i == 1;
+    trial(&pms[i]);
+    if (i == 1 && pms[1] < pms[0]) pf = true;
+  }
+  b->bulk_pf = pf;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   b->have_state = false;
@@ -703,6 +734,11 @@ lbm_status lbm_batch_autotune(lbm_batch *b, int32_t steps_per_trial, char *repor
     r += "], \"special_blocks_per_sm\": " + std::to_string(b->special_bps) + ", \"special_ms\": [";
     for (int i = 0; i < 4; i++) {
       std::snprintf(buf, sizeof buf, "%s%.5f", i ? ", " : "", bms[i]);
+      r += buf;
+    }
+    r += "], \"bulk_prefetch\": " + std::to_string((int)b->bulk_pf) + ", \"prefetch_ms\": [";
+    for (int i = 0; i < 2; i++) {
+      std::snprintf(buf, sizeof buf, "%s%.5f", i ? ", " : "", pms[i]);
       r += buf;
     }
     r += "]}";

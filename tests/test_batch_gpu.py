@@ -56,6 +56,7 @@ def test_batch_tiles_and_autotune(precision):
     rep = G.Batch(cs, precision=precision).autotune(2)
     assert 0 <= rep["variant"] < 4 and len(rep["ms"]) == 4
     assert rep["special_blocks_per_sm"] in (0, 2, 4, 8) and len(rep["special_ms"]) == 4
+    assert rep["bulk_prefetch"] in (0, 1) and len(rep["prefetch_ms"]) == 2
     for tile in range(4):
         b = G.Batch(cs, precision=precision)
         b.set_tile(tile)
@@ -130,16 +131,16 @@ def test_batch_outlet_kinds_match_single_contexts(precision):
 
 
 @pytest.mark.parametrize("precision", ["fp32", "fp16dev"])
-def test_boundary_pass_grid_does_not_change_results(precision):
-    """The boundary-node pass walks its list grid-stride: one thread per entry
-    or a few blocks per multiprocessor give the same arithmetic per node, so
-    the fields are bitwise equal."""
+def test_launch_options_do_not_change_results(precision):
+    """The boundary-node pass walks its list grid-stride (one thread per entry
+    or a few blocks per multiprocessor) and the bulk pass's L2 prefetch is a
+    hint: the arithmetic per node is the same, so the fields are bitwise equal."""
     cs = batch_cases(3)
     ref = None
-    for bps in (0, 1, 2, 8):
+    for bps, pf in ((0, False), (1, False), (2, True), (8, True), (0, True)):
         b = G.Batch(cs, precision=precision)
         b.set_tile(1)
-        b.set_special_blocks(bps)
+        b.set_launch(bps, pf)
         b.set_rest()
         r = b.run(60, check_every=30, tol=-1.0)
         assert (r["steps"] == 60).all()
@@ -150,4 +151,4 @@ def test_boundary_pass_grid_does_not_change_results(precision):
             continue
         for c in range(len(cs)):
             for k in ("rho", "u", "v"):
-                assert np.array_equal(f[c][k], ref[c][k]), (bps, c, k)
+                assert np.array_equal(f[c][k], ref[c][k]), (bps, pf, c, k)

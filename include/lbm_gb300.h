@@ -267,8 +267,10 @@ typedef struct lbm_sg_config {
   int32_t coarse_block;    /* divides height and width */
   int32_t products;        /* 0: convolution products on tcgen05 (tensor-memory accumulators)
                               where the shapes allow, 3x3 layers with W a multiple of 128 and C a
-                              multiple of 32 in the TMA-fed halo-tile form; 1: every product on the
-                              mma.sync kernels; 2: tcgen05 with the im2col gather only */
+                              multiple of 32 in the TMA-fed halo-tile form (several row segments
+                              per block where H is a multiple of 4); 1: every product on the
+                              mma.sync kernels; 2: tcgen05 with the im2col gather only; 3: as 0
+                              with one row segment per halo-tile convolution block */
 } lbm_sg_config;
 lbm_status lbm_sg_create(const lbm_sg_config *cfg, lbm_sg **out);
 void lbm_sg_destroy(lbm_sg *s);

@@ -412,7 +412,7 @@ def _load_sg(L):
 
 
 # tensor-core paths of the network's products (lbm_sg_config.products)
-PRODUCTS = {"tcgen05": 0, "mma": 1, "tcgen05-gather": 2}
+PRODUCTS = {"tcgen05": 0, "mma": 1, "tcgen05-gather": 2, "tcgen05-1seg": 3}
 
 
 class Surrogate:
@@ -423,7 +423,9 @@ class Surrogate:
                  weight_decay=0.0, coarse_weight=0.0, coarse_block=8, products="tcgen05"):
         """products: "tcgen05" (the convolution products on the 5th-generation
         tensor cores where the shapes allow, the TMA-fed halo-tile form for
-        3x3 layers with W a multiple of 128 and C a multiple of 32),
+        3x3 layers with W a multiple of 128 and C a multiple of 32, four row
+        segments per convolution block where H is a multiple of 4),
+        "tcgen05-1seg" (the same with one row segment per convolution block),
         "tcgen05-gather" (tcgen05 with the im2col gather only) or "mma" (every
         product on the mma.sync kernels)."""
         L = self.L = _load_sg(load())

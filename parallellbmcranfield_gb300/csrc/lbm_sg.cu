@@ -871,11 +871,58 @@ bool tc_conv3h(lbm_sg *s, const bf16 *X, int P, int H, int W, int C, const bf16 
   return true;
 }
 
+// The same product with several row segments per block (k_tc_conv3m): H a
+// multiple of TC_SEGS as well, out 16-byte aligned.  Returns false (nothing
+// launched) when the tensor maps cannot be encoded.
+template <int EPI, int BN>
+bool tc_conv3m(lbm_sg *s, const bf16 *X, int P, int H, int W, int C, const bf16 *Bt, int N, int Kp,
+               const float *bias, bf16 *out, cudaError_t *err) {
+  using M = sgtc::TcHaloM<BN>;
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc || ((uintptr_t)X & 15) || ((uintptr_t)Bt & 15) || ((uintptr_t)out & 15)) return false;
+  const int imgs = P / (H * W);
+  CUtensorMap ma, mb;
+  const cuuint64_t da[5] = {8, (cuuint64_t)W, (cuuint64_t)(C / 8), (cuuint64_t)H, (cuuint64_t)imgs};
+  const cuuint64_t sa[4] = {(cuuint64_t)C * 2, 16, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+  const cuuint32_t ba[5] = {8, 130, 4, 3, 1}, ea[5] = {1, 1, 1, 1, 1};
+  const cuuint64_t db[4] = {8, (cuuint64_t)N, (cuuint64_t)(C / 8), 9};
+  const cuuint64_t sb[3] = {(cuuint64_t)Kp * 2, 16, (cuuint64_t)C * 2};
+  const cuuint32_t bb[4] = {8, (cuuint32_t)BN, 4, 9}, eb[4] = {1, 1, 1, 1};
+  if (enc(&ma, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, (void *)X, da, sa, ba, ea,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS ||
+      enc(&mb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)Bt, db, sb, bb, eb,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  static bool attr = false;
+  if (!attr) {
+    *err = cudaFuncSetAttribute(sgtc::k_tc_conv3m<EPI, BN>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, M::BYTES);
+    if (*err != cudaSuccess) return true;
+    attr = true;
+  }
+  dim3 grid((unsigned)(W / sgtc::TC_BM * (N / BN)), (unsigned)(H / sgtc::TC_SEGS), (unsigned)imgs);
+  sgtc::k_tc_conv3m<EPI, BN><<<grid, sgtc::TC3M_THREADS, M::BYTES, s->stream>>>(
+      ma, mb, H, W, C, N, bias, out, s->d_err);
+  *err = cudaGetLastError();
+  return true;
+}
+
 template <int EPI>
 cudaError_t tc_conv(lbm_sg *s, const bf16 *X, int P, int H, int W, int C, int taps,
                     const bf16 *Bt, int N, int Kp, const float *bias, bf16 *out) {
   if (taps == 9 && W % sgtc::TC_BM == 0 && C % 32 == 0 && Kp >= 9 * C && Kp % 8 == 0 &&
-      P % (H * W) == 0 && s->cfg.products == 0) {
+      P % (H * W) == 0 && s->cfg.products == 0 && H % sgtc::TC_SEGS == 0) {
+    cudaError_t e = cudaSuccess;
+    bool done = false;
+    if (N % 128 == 0) done = tc_conv3m<EPI, 128>(s, X, P, H, W, C, Bt, N, Kp, bias, out, &e);
+    else if (N % 64 == 0) done = tc_conv3m<EPI, 64>(s, X, P, H, W, C, Bt, N, Kp, bias, out, &e);
+    else if (N % 32 == 0) done = tc_conv3m<EPI, 32>(s, X, P, H, W, C, Bt, N, Kp, bias, out, &e);
+    if (done) return e;
+  }
+  if (taps == 9 && W % sgtc::TC_BM == 0 && C % 32 == 0 && Kp >= 9 * C && Kp % 8 == 0 &&
+      P % (H * W) == 0 && (s->cfg.products == 0 || s->cfg.products == 3)) {
     cudaError_t e = cudaSuccess;
     bool done = false;
     if (N % 128 == 0) done = tc_conv3h<EPI, 128>(s, X, P, H, W, C, Bt, N, Kp, bias, out, &e);
@@ -1054,8 +1101,8 @@ lbm_status conv_bwd(lbm_sg *s, int li, int xi, int yi, int B, bool need_dx) {
   }
   lbm_status st = LBM_OK;
   bool halo_done = false;
-  if (s->cfg.products == 0 && c.taps == 9 && X.w % sgtc::TC_BM == 0 && X.c % 32 == 0 &&
-      c.cout % 8 == 0 && c.Kp >= 9 * X.c && M % (X.h * X.w) == 0) {
+  if ((s->cfg.products == 0 || s->cfg.products == 3) && c.taps == 9 && X.w % sgtc::TC_BM == 0 &&
+      X.c % 32 == 0 && c.cout % 8 == 0 && c.Kp >= 9 * X.c && M % (X.h * X.w) == 0) {
     cudaError_t e = cudaSuccess;
     halo_done = tc_wgrad3h(s, Y.dx, X.x, M, X.h, X.w, X.c, c.cout, s->g + c.woff, c.Kp, &e);
     if (halo_done && e != cudaSuccess)
@@ -1304,9 +1351,10 @@ lbm_status lbm_sg_create(const lbm_sg_config *cfg, lbm_sg **out) {
       (st = salloc(s, &s->msk, P)) || (st = salloc(s, &s->xin, P * ci)) ||
       (st = salloc(s, &s->yout, P * co)) || (st = salloc(s, &s->loss, 3)))
     return bail(st);
-  if (cfg->products < 0 || cfg->products > 2)
+  if (cfg->products < 0 || cfg->products > 3)
     return bail(fail(LBM_INVALID,
-                     "surrogate: products must be 0 (tcgen05), 1 (mma.sync) or 2 (tcgen05, gather only)"));
+                     "surrogate: products must be 0 (tcgen05), 1 (mma.sync), 2 (tcgen05, gather only) or 3 "
+                     "(tcgen05, one row segment per halo-tile block)"));
   if ((st = salloc(s, &s->d_err, 1)) != LBM_OK) return bail(st);
   cudaMemset(s->d_err, 0, sizeof(int));
   if (cfg->coarse_weight > 0.f) {

@@ -644,6 +644,175 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_conv3h(const __grid_constant_
   if (tid < 32) tm_free(tmem, BN < 32 ? 32 : BN);
 }
 
+// The halo-tile convolution over several row segments per block: rows
+// y0 .. y0 + TC_SEGS - 1 at the same x0, output tile and image, so that the
+// loads, MMAs and epilogue of consecutive segments overlap instead of
+// following one another as in k_tc_conv3h.  Warp 4 (one lane) issues the
+// TMA loads (halo and weights per 32-channel chunk, tensor maps as for
+// k_tc_conv3h) into a ring of two stages and the MMAs, each segment into one
+// of two tensor-memory accumulators; warps 0-3 (tensor-memory lanes 0-127:
+// warp w reads lanes 32w..32w+31) drain the other accumulator, each thread
+// storing its pixel's BN outputs as 32-byte row pieces (two 16-byte stores
+// per 16 columns, whole sectors).  mbarriers: full / empty per stage (the
+// loads landed / the MMAs reading it are done), accfull per accumulator (its
+// segment's MMAs are done), accfree per accumulator (128 arrivals: the
+// epilogue has read it), done (every MMA issued is done).  Every wait is
+// bounded; on expiry the block sets *err, stops issuing, lets the loads and
+// MMAs in flight finish (bounded) and frees its tensor memory.
+constexpr int TC_SEGS = 4;
+constexpr int TC3M_THREADS = 160;
+template <int BN>
+struct TcHaloM {
+  static constexpr int STAGES = 2;
+  static constexpr int STAGE = TcHalo<BN>::STAGE;
+  static constexpr int BYTES = STAGES * STAGE + 128 + 1024;  // stages, mbarriers + slot, alignment
+};
+
+__device__ __forceinline__ void mb_arrive(uint64_t *b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(saddr(b)) : "memory");
+}
+
+template <int EPI, int BN>
+__global__ void __launch_bounds__(TC3M_THREADS) k_tc_conv3m(const __grid_constant__ CUtensorMap mapA,
+                                                            const __grid_constant__ CUtensorMap mapB,
+                                                            int H, int W, int C, int N,
+                                                            const float *__restrict__ bias,
+                                                            bf16 *__restrict__ out, int *err) {
+  static_assert(BN >= 32 && BN <= 128 && BN % 16 == 0, "accumulator width");
+  using T = TcHalo<BN>;
+  constexpr int S = TcHaloM<BN>::STAGES;
+  uint8_t *sm = tc_smem_base();
+  uint64_t *bars = (uint64_t *)(sm + S * T::STAGE);
+  uint64_t *full = bars, *empty = bars + 2, *accfull = bars + 4, *accfree = bars + 6, *done = bars + 8;
+  uint32_t *slot = (uint32_t *)(bars + 9);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int segs = W / TC_BM;
+  const int x0 = (blockIdx.x % segs) * TC_BM, n0 = (blockIdx.x / segs) * BN;
+  const int y0 = blockIdx.y * TC_SEGS, img = blockIdx.z;
+  const int nch = C / 32;
+  const int G = TC_SEGS * nch;  // chunks of this block, segment-major
+  if (tid == 0) {
+    for (int i = 0; i < 6; i++) mb_init(&bars[i], 1);
+    mb_init(&accfree[0], TC_BM);
+    mb_init(&accfree[1], TC_BM);
+    mb_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    fence_async_smem();
+  }
+  __syncwarp();
+  if (tid < 32) tm_alloc(slot, 2 * BN);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *slot;
+  bool ok = true;
+  if (warp == 4) {
+    if (lane == 0) {
+      const uint32_t idesc = tc_idesc(BN, 0, 0);
+      int issued = 0, consumed = 0;  // chunks whose loads were issued / have landed
+      auto issue = [&](int g, int st) {
+        const int seg = g / nch, kc = g - seg * nch;
+        const uint32_t a = saddr(sm + st * T::STAGE), b = a + TH_A_SLOT;
+        mb_expect_tx(&full[st], TH_A_BYTES + T::B_BYTES);
+        tma_load_5d(a, &mapA, &full[st], 0, x0 - 1, kc * 4, y0 + seg - 1, img);
+        tma_load_4d(b, &mapB, &full[st], 0, n0, kc * 4, 0);
+        issued = g + 1;
+      };
+      for (int i = 0; i < S && i < G; i++) issue(i, i);
+      for (int g = 0; g < G; g++) {
+        const int seg = g / nch, kc = g - seg * nch, st = g % S, acc = seg & 1;
+        // the accumulator of segment seg - 2 must have been read out
+        if (kc == 0 && seg >= 2 && !mb_wait(&accfree[acc], (uint32_t)((seg - 2) >> 1) & 1u)) {
+          ok = false;
+          break;
+        }
+        if (!mb_wait(&full[st], (uint32_t)(g / S) & 1u)) {
+          ok = false;
+          break;
+        }
+        consumed = g + 1;
+        tc_fence_after();
+        const uint32_t a = saddr(sm + st * T::STAGE), b = a + TH_A_SLOT;
+        const uint32_t d = tmem + (uint32_t)(acc * BN);
+#pragma unroll
+        for (int tap = 0; tap < 9; tap++) {
+          const int dy = tap / 3, dx = tap % 3;  // offsets + 1
+#pragma unroll
+          for (int k2 = 0; k2 < 2; k2++) {
+            const uint32_t ad = a + dy * (4 * 2080) + (2 * k2) * 2080 + dx * 16;
+            const uint32_t bd = b + tap * (4 * BN * 16) + (2 * k2) * (BN * 16);
+            tc_mma(d, tc_desc(ad, 2080, 128), tc_desc(bd, BN * 16, 128), idesc,
+                   (kc | tap | k2) != 0);
+          }
+        }
+        tc_commit(&empty[st]);
+        if (kc == nch - 1) tc_commit(&accfull[acc]);
+        // refill the stage the previous chunk used: its MMAs complete ahead
+        // of the ones just issued
+        if (g >= 1 && g - 1 + S < G) {
+          const int pst = (g - 1) % S;
+          if (!mb_wait(&empty[pst], (uint32_t)((g - 1) / S) & 1u)) {
+            ok = false;
+            break;
+          }
+          issue(g - 1 + S, pst);
+        }
+      }
+      tc_commit(done);  // arrives when every MMA issued above is complete
+      if (!ok) {
+        // loads still in flight land in this block's shared memory: wait for
+        // them (bounded) before the block may exit
+        for (int g = consumed; g < issued; g++) mb_wait(&full[g % S], (uint32_t)(g / S) & 1u);
+      }
+      if (!mb_wait(done, 0)) ok = false;
+    }
+    __syncwarp();
+  } else {
+    // epilogue: this thread's pixel of each segment, from the segment's accumulator
+    for (int seg = 0; seg < TC_SEGS; seg++) {
+      const int acc = seg & 1;
+      const bool landed = __all_sync(0xffffffffu, mb_wait(&accfull[acc], (uint32_t)(seg >> 1) & 1u));
+      tc_fence_after();
+      if (landed && ok) {
+        const long long row = ((long long)img * H + y0 + seg) * W + x0 + warp * 32 + lane;
+        bf16 *o = out + row * N + n0;
+#pragma unroll
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+          float v[16];
+          tm_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(acc * BN + c0), v);
+          uint32_t w[8];
+#pragma unroll
+          for (int j = 0; j < 16; j += 2) {
+            float v0 = v[j], v1 = v[j + 1];
+            if (EPI != TC_PLAIN) {
+              v0 += bias[n0 + c0 + j];
+              v1 += bias[n0 + c0 + j + 1];
+            }
+            if (EPI == TC_BIAS_RELU) {
+              v0 = fmaxf(v0, 0.f);
+              v1 = fmaxf(v1, 0.f);
+            }
+            const __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
+            memcpy(&w[j / 2], &h, 4);
+          }
+          *(uint4 *)(o + c0) = make_uint4(w[0], w[1], w[2], w[3]);
+          *(uint4 *)(o + c0 + 8) = make_uint4(w[4], w[5], w[6], w[7]);
+        }
+      } else {
+        ok = false;
+      }
+      tc_fence_before();
+      mb_arrive(&accfree[acc]);
+    }
+  }
+  ok = __syncthreads_and(ok) != 0;
+  if (!ok && tid == 0) atomicExch(err, 1);
+  tc_fence_before();
+  __syncthreads();
+  __syncwarp();
+  if (tid < 32) tm_free(tmem, 2 * BN);
+}
+
 // Weight gradient of a 3x3 convolution (pad 1, W a multiple of 128, C a
 // multiple of 32) in the halo-tile form: dW[n][tap][c] = sum over pixels p of
 // dZ[p][n] X[p + offset(tap)][c], as nine products D_tap[n][c] (M = 128

@@ -343,7 +343,7 @@ def main(argv=None):
                    help="only time training on random inputs (samples/s)")
     p.add_argument("--reference-start", action="store_true",
                    help="no network: seed the warm starts with the reference fields")
-    p.add_argument("--products", default="tcgen05", choices=["tcgen05", "tcgen05-gather", "mma"],
+    p.add_argument("--products", default="tcgen05", choices=["tcgen05", "tcgen05-gather", "tcgen05-1seg", "mma"],
                    help="tensor-core path of the network's convolution products")
     p.add_argument("--base", type=int, default=32, help="channels of the first level")
     a = p.parse_args(argv)

@@ -279,15 +279,16 @@ def test_gap_flow_of_an_empty_channel_is_the_inlet_parabola():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("tc", ["tcgen05", "tcgen05-gather"])
+@pytest.mark.parametrize("tc", ["tcgen05", "tcgen05-1seg", "tcgen05-gather"])
 @pytest.mark.parametrize("h,B", [(64, 2), (256, 1)])
 def test_tcgen05_and_mma_products_agree(tc, h, B):
     """The tcgen05 product paths against mma.sync at base width 32: at 64 x 64
     every layer takes the im2col gather (tile widths 32, 64, 128, several K
     tiles); at 256 x 256 the 3x3 layers of levels 0 and 1 (W 256 and 128, C a
     multiple of 32, N 32 or 64) take the TMA-fed halo-tile form with
-    "tcgen05", the gather with "tcgen05-gather".  Forward outputs and
-    gradients agree to the BF16 rounding of the activations."""
+    "tcgen05" (four row segments per convolution block) and "tcgen05-1seg"
+    (one), the gather with "tcgen05-gather".  Forward outputs and gradients
+    agree to the BF16 rounding of the activations."""
     import parallellbmcranfield_gb300 as G
 
     x, t, m = sample(seed=9, B=B, h=h, cin=8)

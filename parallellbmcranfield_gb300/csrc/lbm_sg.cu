@@ -880,6 +880,23 @@ bool tc_conv3m(lbm_sg *s, const bf16 *X, int P, int H, int W, int C, const bf16 
   using M = sgtc::TcHaloM<BN>;
   EncodeTiledFn enc = encode_tiled();
   if (!enc || ((uintptr_t)X & 15) || ((uintptr_t)Bt & 15) || ((uintptr_t)out & 15)) return false;
+  // halo ring depth: the most halo loads in flight per SM (stages used, at
+  // most the block's TC_SEGS x nch loads, times resident blocks: shared
+  // memory and 2 BN tensor-memory columns per block; fewer stages on a tie),
+  // at least two stages (a stage is refilled while the next one is read)
+  const int nch = C / 32;
+  constexpr int kSmemSM = 233472, kSmemBlock = 232448;  // per SM, per block (bytes)
+  int S = 0, best = 0;
+  for (int st = 2; st <= sgtc::TC3M_MAX_STAGES; st++) {
+    const int bytes = M::bytes(st, nch);
+    if (bytes > kSmemBlock) break;
+    const int blocks = std::min(kSmemSM / (bytes + 1024), 512 / (2 * BN));
+    if (std::min(st, sgtc::TC_SEGS * nch) * blocks > best) {
+      best = std::min(st, sgtc::TC_SEGS * nch) * blocks;
+      S = st;
+    }
+  }
+  if (S == 0) return false;
   const int imgs = P / (H * W);
   CUtensorMap ma, mb;
   const cuuint64_t da[5] = {8, (cuuint64_t)W, (cuuint64_t)(C / 8), (cuuint64_t)H, (cuuint64_t)imgs};
@@ -898,13 +915,13 @@ bool tc_conv3m(lbm_sg *s, const bf16 *X, int P, int H, int W, int C, const bf16 
   static bool attr = false;
   if (!attr) {
     *err = cudaFuncSetAttribute(sgtc::k_tc_conv3m<EPI, BN>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, M::BYTES);
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBlock);
     if (*err != cudaSuccess) return true;
     attr = true;
   }
   dim3 grid((unsigned)(W / sgtc::TC_BM * (N / BN)), (unsigned)(H / sgtc::TC_SEGS), (unsigned)imgs);
-  sgtc::k_tc_conv3m<EPI, BN><<<grid, sgtc::TC3M_THREADS, M::BYTES, s->stream>>>(
-      ma, mb, H, W, C, N, bias, out, s->d_err);
+  sgtc::k_tc_conv3m<EPI, BN><<<grid, sgtc::TC3M_THREADS, M::bytes(S, nch), s->stream>>>(
+      ma, mb, H, W, C, N, S, bias, out, s->d_err);
   *err = cudaGetLastError();
   return true;
 }

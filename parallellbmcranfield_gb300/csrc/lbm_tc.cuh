@@ -647,25 +647,31 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_conv3h(const __grid_constant_
 // The halo-tile convolution over several row segments per block: rows
 // y0 .. y0 + TC_SEGS - 1 at the same x0, output tile and image, so that the
 // loads, MMAs and epilogue of consecutive segments overlap instead of
-// following one another as in k_tc_conv3h.  Warp 4 (one lane) issues the
-// TMA loads (halo and weights per 32-channel chunk, tensor maps as for
-// k_tc_conv3h) into a ring of two stages and the MMAs, each segment into one
-// of two tensor-memory accumulators; warps 0-3 (tensor-memory lanes 0-127:
-// warp w reads lanes 32w..32w+31) drain the other accumulator, each thread
-// storing its pixel's BN outputs as 32-byte row pieces (two 16-byte stores
-// per 16 columns, whole sectors).  mbarriers: full / empty per stage (the
-// loads landed / the MMAs reading it are done), accfull per accumulator (its
+// following one another as in k_tc_conv3h, and more halo loads are in
+// flight per SM.  The weights of all 32-channel chunks (one TMA load each,
+// tensor map as for k_tc_conv3h) stay in shared memory for the whole block;
+// the halos (one TMA load per segment and chunk) go through a ring of S
+// stages, S from the host.  Warp 4 (one lane) issues the loads and the MMAs,
+// each segment into one of two tensor-memory accumulators; warps 0-3
+// (tensor-memory lanes 0-127: warp w reads lanes 32w..32w+31) drain the
+// other accumulator, each thread storing its pixel's BN outputs as 32-byte
+// row pieces (two 16-byte stores per 16 columns, whole sectors).
+// mbarriers: wfull (the weights landed), full / empty per stage (the halo
+// landed / the MMAs reading it are done), accfull per accumulator (its
 // segment's MMAs are done), accfree per accumulator (128 arrivals: the
 // epilogue has read it), done (every MMA issued is done).  Every wait is
 // bounded; on expiry the block sets *err, stops issuing, lets the loads and
 // MMAs in flight finish (bounded) and frees its tensor memory.
 constexpr int TC_SEGS = 4;
 constexpr int TC3M_THREADS = 160;
+constexpr int TC3M_MAX_STAGES = 8;
 template <int BN>
 struct TcHaloM {
-  static constexpr int STAGES = 2;
-  static constexpr int STAGE = TcHalo<BN>::STAGE;
-  static constexpr int BYTES = STAGES * STAGE + 128 + 1024;  // stages, mbarriers + slot, alignment
+  static constexpr int B_CHUNK = TcHalo<BN>::B_BYTES;  // weights of one 32-channel chunk
+  // halo ring, weights, mbarriers and the tensor-memory slot (256 bytes), alignment slack
+  static constexpr int bytes(int stages, int nch) {
+    return stages * TH_A_SLOT + nch * B_CHUNK + 256 + 1024;
+  }
 };
 
 __device__ __forceinline__ void mb_arrive(uint64_t *b) {
@@ -675,27 +681,32 @@ __device__ __forceinline__ void mb_arrive(uint64_t *b) {
 template <int EPI, int BN>
 __global__ void __launch_bounds__(TC3M_THREADS) k_tc_conv3m(const __grid_constant__ CUtensorMap mapA,
                                                             const __grid_constant__ CUtensorMap mapB,
-                                                            int H, int W, int C, int N,
+                                                            int H, int W, int C, int N, int S,
                                                             const float *__restrict__ bias,
                                                             bf16 *__restrict__ out, int *err) {
   static_assert(BN >= 32 && BN <= 128 && BN % 16 == 0, "accumulator width");
-  using T = TcHalo<BN>;
-  constexpr int S = TcHaloM<BN>::STAGES;
+  using M = TcHaloM<BN>;
   uint8_t *sm = tc_smem_base();
-  uint64_t *bars = (uint64_t *)(sm + S * T::STAGE);
-  uint64_t *full = bars, *empty = bars + 2, *accfull = bars + 4, *accfree = bars + 6, *done = bars + 8;
-  uint32_t *slot = (uint32_t *)(bars + 9);
+  const int nch = C / 32;
+  uint8_t *wts = sm + S * TH_A_SLOT;  // nch chunks of weights
+  uint64_t *bars = (uint64_t *)(wts + nch * M::B_CHUNK);
+  uint64_t *full = bars, *empty = bars + TC3M_MAX_STAGES;
+  uint64_t *accfull = bars + 2 * TC3M_MAX_STAGES, *accfree = accfull + 2, *done = accfull + 4,
+           *wfull = accfull + 5;
+  uint32_t *slot = (uint32_t *)(accfull + 6);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int segs = W / TC_BM;
   const int x0 = (blockIdx.x % segs) * TC_BM, n0 = (blockIdx.x / segs) * BN;
   const int y0 = blockIdx.y * TC_SEGS, img = blockIdx.z;
-  const int nch = C / 32;
-  const int G = TC_SEGS * nch;  // chunks of this block, segment-major
+  const int G = TC_SEGS * nch;  // halo loads of this block, segment-major
   if (tid == 0) {
-    for (int i = 0; i < 6; i++) mb_init(&bars[i], 1);
+    for (int i = 0; i < 2 * TC3M_MAX_STAGES; i++) mb_init(&bars[i], 1);
+    mb_init(&accfull[0], 1);
+    mb_init(&accfull[1], 1);
     mb_init(&accfree[0], TC_BM);
     mb_init(&accfree[1], TC_BM);
     mb_init(done, 1);
+    mb_init(wfull, 1);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     fence_async_smem();
   }
@@ -709,17 +720,22 @@ __global__ void __launch_bounds__(TC3M_THREADS) k_tc_conv3m(const __grid_constan
   if (warp == 4) {
     if (lane == 0) {
       const uint32_t idesc = tc_idesc(BN, 0, 0);
-      int issued = 0, consumed = 0;  // chunks whose loads were issued / have landed
+      int issued = 0, consumed = 0;  // halo loads issued / landed
+      bool wlanded = false;
       auto issue = [&](int g, int st) {
         const int seg = g / nch, kc = g - seg * nch;
-        const uint32_t a = saddr(sm + st * T::STAGE), b = a + TH_A_SLOT;
-        mb_expect_tx(&full[st], TH_A_BYTES + T::B_BYTES);
-        tma_load_5d(a, &mapA, &full[st], 0, x0 - 1, kc * 4, y0 + seg - 1, img);
-        tma_load_4d(b, &mapB, &full[st], 0, n0, kc * 4, 0);
+        mb_expect_tx(&full[st], TH_A_BYTES);
+        tma_load_5d(saddr(sm + st * TH_A_SLOT), &mapA, &full[st], 0, x0 - 1, kc * 4, y0 + seg - 1,
+                    img);
         issued = g + 1;
       };
+      mb_expect_tx(wfull, nch * M::B_CHUNK);
+      for (int kc = 0; kc < nch; kc++)
+        tma_load_4d(saddr(wts + kc * M::B_CHUNK), &mapB, wfull, 0, n0, kc * 4, 0);
       for (int i = 0; i < S && i < G; i++) issue(i, i);
-      for (int g = 0; g < G; g++) {
+      ok = mb_wait(wfull, 0);
+      wlanded = ok;
+      for (int g = 0; g < G && ok; g++) {
         const int seg = g / nch, kc = g - seg * nch, st = g % S, acc = seg & 1;
         // the accumulator of segment seg - 2 must have been read out
         if (kc == 0 && seg >= 2 && !mb_wait(&accfree[acc], (uint32_t)((seg - 2) >> 1) & 1u)) {
@@ -732,7 +748,7 @@ __global__ void __launch_bounds__(TC3M_THREADS) k_tc_conv3m(const __grid_constan
         }
         consumed = g + 1;
         tc_fence_after();
-        const uint32_t a = saddr(sm + st * T::STAGE), b = a + TH_A_SLOT;
+        const uint32_t a = saddr(sm + st * TH_A_SLOT), b = saddr(wts + kc * M::B_CHUNK);
         const uint32_t d = tmem + (uint32_t)(acc * BN);
 #pragma unroll
         for (int tap = 0; tap < 9; tap++) {
@@ -747,7 +763,7 @@ __global__ void __launch_bounds__(TC3M_THREADS) k_tc_conv3m(const __grid_constan
         }
         tc_commit(&empty[st]);
         if (kc == nch - 1) tc_commit(&accfull[acc]);
-        // refill the stage the previous chunk used: its MMAs complete ahead
+        // refill the stage the previous halo used: its MMAs complete ahead
         // of the ones just issued
         if (g >= 1 && g - 1 + S < G) {
           const int pst = (g - 1) % S;
@@ -762,6 +778,7 @@ __global__ void __launch_bounds__(TC3M_THREADS) k_tc_conv3m(const __grid_constan
       if (!ok) {
         // loads still in flight land in this block's shared memory: wait for
         // them (bounded) before the block may exit
+        if (!wlanded) mb_wait(wfull, 0);
         for (int g = consumed; g < issued; g++) mb_wait(&full[g % S], (uint32_t)(g / S) & 1u);
       }
       if (!mb_wait(done, 0)) ok = false;

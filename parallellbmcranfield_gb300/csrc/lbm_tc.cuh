@@ -596,16 +596,17 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_conv3h(const __grid_constant_
         consumed = kc + 1;
         tc_fence_after();
         const uint32_t a = saddr(sm + st * T::STAGE), b = a + TH_A_SLOT;
+        // the taps are start-address offsets, added to the descriptors'
+        // address field (16-byte units, no carry: shared addresses < 2^18)
+        const uint64_t da = tc_desc(a, 2080, 128), db = tc_desc(b, BN * 16, 128);
   #pragma unroll
         for (int tap = 0; tap < 9; tap++) {
           const int dy = tap / 3, dx = tap % 3;  // offsets + 1
   #pragma unroll
-          for (int k2 = 0; k2 < 2; k2++) {
-            const uint32_t ad = a + dy * (4 * 2080) + (2 * k2) * 2080 + dx * 16;
-            const uint32_t bd = b + tap * (4 * BN * 16) + (2 * k2) * (BN * 16);
-            tc_mma(tmem, tc_desc(ad, 2080, 128), tc_desc(bd, BN * 16, 128), idesc,
+          for (int k2 = 0; k2 < 2; k2++)
+            tc_mma(tmem, da + (uint64_t)((dy * (4 * 2080) + (2 * k2) * 2080 + dx * 16) >> 4),
+                   db + (uint64_t)((tap * (4 * BN * 16) + (2 * k2) * (BN * 16)) >> 4), idesc,
                    (kc | tap | k2) != 0);
-          }
         }
         tc_commit(&empty[st]);
         // refill the stage the previous chunk used: its MMAs complete ahead of
@@ -750,16 +751,17 @@ __global__ void __launch_bounds__(TC3M_THREADS) k_tc_conv3m(const __grid_constan
         tc_fence_after();
         const uint32_t a = saddr(sm + st * TH_A_SLOT), b = saddr(wts + kc * M::B_CHUNK);
         const uint32_t d = tmem + (uint32_t)(acc * BN);
+        // the taps are start-address offsets, added to the descriptors'
+        // address field (16-byte units, no carry: shared addresses < 2^18)
+        const uint64_t da = tc_desc(a, 2080, 128), db = tc_desc(b, BN * 16, 128);
 #pragma unroll
         for (int tap = 0; tap < 9; tap++) {
           const int dy = tap / 3, dx = tap % 3;  // offsets + 1
 #pragma unroll
-          for (int k2 = 0; k2 < 2; k2++) {
-            const uint32_t ad = a + dy * (4 * 2080) + (2 * k2) * 2080 + dx * 16;
-            const uint32_t bd = b + tap * (4 * BN * 16) + (2 * k2) * (BN * 16);
-            tc_mma(d, tc_desc(ad, 2080, 128), tc_desc(bd, BN * 16, 128), idesc,
+          for (int k2 = 0; k2 < 2; k2++)
+            tc_mma(d, da + (uint64_t)((dy * (4 * 2080) + (2 * k2) * 2080 + dx * 16) >> 4),
+                   db + (uint64_t)((tap * (4 * BN * 16) + (2 * k2) * (BN * 16)) >> 4), idesc,
                    (kc | tap | k2) != 0);
-          }
         }
         tc_commit(&empty[st]);
         if (kc == nch - 1) tc_commit(&accfull[acc]);
@@ -909,16 +911,20 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_wgrad3h(const __grid_constant
         consumed = i + 1;
         tc_fence_after();
         const uint32_t xa = saddr(sm + st * T::STAGE), za = xa + TH_A_SLOT;
-  #pragma unroll 1
+        // one descriptor per operand and stage; every tap and K step is a
+        // start-address offset, added to the descriptor's address field
+        // (16-byte units; shared addresses stay below 2^18, so no carry
+        // leaves the field), and the 72 MMAs are unrolled: the issuing
+        // thread spends a few instructions per MMA
+        const uint64_t da = tc_desc(za, 128, 2048), db = tc_desc(xa, 128, 2080);
+  #pragma unroll
         for (int tap = 0; tap < 9; tap++) {
           const int dy = tap / 3, dx = tap % 3;  // offsets + 1
   #pragma unroll
-          for (int kk = 0; kk < 8; kk++) {
-            const uint32_t ad = za + kk * 256;
-            const uint32_t bd = xa + dy * (4 * 2080) + (16 * kk + dx) * 16;
-            tc_mma(tmem + tap * 32, tc_desc(ad, 128, 2048), tc_desc(bd, 128, 2080), idesc,
+          for (int kk = 0; kk < 8; kk++)
+            tc_mma(tmem + tap * 32, da + (uint64_t)((kk * 256) >> 4),
+                   db + (uint64_t)((dy * (4 * 2080) + (16 * kk + dx) * 16) >> 4), idesc,
                    (i | kk) != 0);
-          }
         }
         tc_commit(&empty[st]);
         // refill the stage the previous segment used (see k_tc_conv3h)

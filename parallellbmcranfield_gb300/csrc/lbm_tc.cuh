@@ -872,8 +872,13 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_wgrad3h(const __grid_constant
   const int groups = min(16, (N - n0) / 8);
   const uint32_t tx_bytes = TH_A_BYTES + 8 * 128 * groups * 2;
   const int segs_per_row = W / TC_BM;
+  // two threads issue the MMAs, lane 0 of warp 0 (taps 0-4, and the loads)
+  // and lane 0 of warp 1 (taps 5-8): one thread alone could not issue the
+  // 72 MMAs of a segment as fast as the tensor pipe runs them.  empty[] and
+  // done take one tcgen05.commit from each.
   if (tid == 0) {
-    for (int i = 0; i < 2 * S + 1; i++) mb_init(&bars[i], 1);
+    for (int i = 0; i < S; i++) mb_init(&bars[i], 1);
+    for (int i = S; i < 2 * S + 1; i++) mb_init(&bars[i], 2);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     fence_async_smem();
   }
@@ -884,10 +889,11 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_wgrad3h(const __grid_constant
   tc_fence_after();
   const uint32_t tmem = *slot;
   bool ok = true;
-  // warp 0 issues, lane 0 alone; its other lanes wait at __syncwarp
-  // instead of polling the mbarrier beside it
-  if (tid < 32) {
-    if (tid == 0) {
+  // the other lanes of warps 0 and 1 wait at __syncwarp instead of polling
+  // the mbarriers beside the issuing lanes
+  if (warp < 2) {
+    if (lane == 0) {
+      const int role = warp;  // 0: taps 0-4 and the loads; 1: taps 5-8
       const uint32_t idesc = tc_idesc(32, 1, 1);
       int issued = 0, consumed = 0;
       auto issue = [&](int i, int st) {
@@ -900,7 +906,8 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_wgrad3h(const __grid_constant
         tma_load_5d(d, &mapDZ, &full[st], 0, x0, n0 / 8, y, img);
         issued = i + 1;
       };
-      for (int i = 0; i < S && i < ns; i++) issue(i, i);
+      if (role == 0)
+        for (int i = 0; i < S && i < ns; i++) issue(i, i);
       for (int i = 0; i < ns && ok; i++) {
         const int st = i % S;
         const uint32_t ph = (uint32_t)(i / S) & 1u;
@@ -920,6 +927,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_wgrad3h(const __grid_constant
   #pragma unroll
         for (int tap = 0; tap < 9; tap++) {
           const int dy = tap / 3, dx = tap % 3;  // offsets + 1
+          if ((tap < 5) != (role == 0)) continue;
   #pragma unroll
           for (int kk = 0; kk < 8; kk++)
             tc_mma(tmem + tap * 32, da + (uint64_t)((kk * 256) >> 4),
@@ -928,7 +936,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_wgrad3h(const __grid_constant
         }
         tc_commit(&empty[st]);
         // refill the stage the previous segment used (see k_tc_conv3h)
-        if (i >= 1 && i - 1 + S < ns) {
+        if (role == 0 && i >= 1 && i - 1 + S < ns) {
           const int pst = (i - 1) % S;
           if (!mb_wait(&empty[pst], (uint32_t)((i - 1) / S) & 1u)) {
             ok = false;
@@ -938,7 +946,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_wgrad3h(const __grid_constant
         }
       }
       tc_commit(done);
-      if (!ok)
+      if (!ok && role == 0)
         for (int i = consumed; i < issued; i++) mb_wait(&full[i % S], (uint32_t)(i / S) & 1u);
     }
     __syncwarp();

@@ -408,6 +408,23 @@ __global__ void k_relu_back(bf16 *dY, const bf16 *Y, size_t n) {
 
 // db[c] += sum over pixels of dZ[p][c] for C <= 8 channels (the output
 // layer): per-thread sums over a pixel stride, then a warp reduction.
+// Sum of v over the block's threads (blocks of up to 32 warps), in thread 0;
+// a block-level sum first, so that a kernel adds one value per block into
+// global memory instead of one per warp (the adds to one address serialise).
+template <class T>
+__device__ __forceinline__ T block_sum(T v) {
+  __shared__ T part[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();  // part[] may still be read by a previous call
+  if ((threadIdx.x & 31) == 0) part[w] = v;
+  __syncthreads();
+  T s = 0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < nw; i++) s += part[i];
+  return s;
+}
+
 __global__ void k_bias_grad(const bf16 *dZ, float *db, size_t P, int C) {
   float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < P; p += (size_t)gridDim.x * blockDim.x)
@@ -416,9 +433,9 @@ __global__ void k_bias_grad(const bf16 *dZ, float *db, size_t P, int C) {
       if (c < C) acc[c] += bf(dZ[p * C + c]);
 #pragma unroll
   for (int c = 0; c < 8; c++) {
-    float v = acc[c];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0 && c < C) atomicAdd(db + c, v);
+    if (c >= C) break;  // C is uniform
+    const float v = block_sum(acc[c]);
+    if (threadIdx.x == 0) atomicAdd(db + c, v);
   }
 }
 
@@ -608,24 +625,28 @@ __global__ void k_mask_sum(const float *mask, size_t P, double *out) {
   double s = 0.0;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < P; i += (size_t)gridDim.x * blockDim.x)
     s += mask[i];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+  s = block_sum(s);
+  if (threadIdx.x == 0) atomicAdd(out, s);
 }
 
 // Masked mean-squared error: loss = sum m (y - t)^2 / (sum m * C); dY in BF16.
 // msum = sum of the mask (k_mask_sum).
+// (P * C < 2^31: the host checks; 32-bit indices, the division by C per
+// element being the costly part in 64 bits)
 __global__ void k_mse(const bf16 *Y, const float *T, const float *mask, bf16 *dY, size_t P, int C,
                       const double *msum, double *loss) {
   const double inv_count = *msum > 0 ? 1.0 / (*msum * C) : 0.0;
+  const float g2 = (float)(2.0 * inv_count);
+  const unsigned n = (unsigned)(P * C), uc = (unsigned)C;
   double s = 0.0;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < P * C; i += (size_t)gridDim.x * blockDim.x) {
-    const float m = mask[i / C];
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float m = mask[i / uc];
     const float d = bf(Y[i]) - T[i];
     s += (double)m * d * d;
-    dY[i] = __float2bfloat16_rn((float)(2.0 * inv_count) * m * d);
+    dY[i] = __float2bfloat16_rn(g2 * m * d);
   }
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(loss, s * inv_count);
+  s = block_sum(s);
+  if (threadIdx.x == 0) atomicAdd(loss, s * inv_count);
 }
 
 // Block-mean term of the loss: the masked means of output and target over
@@ -696,8 +717,17 @@ __global__ void k_adam(float *w, const float *g, float *m, float *v, size_t n, f
 // BF16 copies of one layer's FP32 master weights W[co][Kp] (k = r*Cin + ci,
 // zero beyond taps*Cin): Wt = W for the forward product, and the flipped,
 // transposed Wd[ci][k'] (k' = r*Cout + co, r -> taps-1-r) for the input gradient.
-__global__ void k_weights(const float *W, bf16 *Wt, bf16 *Wd, int Cout, int Cin, int taps, int Kp,
-                          int Kpd) {
+// The BF16 weights of every layer in one launch: blockIdx.y is the layer.
+struct WeightJob {
+  const float *W;
+  bf16 *Wt, *Wd;
+  int Cout, Cin, taps, Kp, Kpd;
+};
+__global__ void k_weights(const WeightJob *__restrict__ jobs) {
+  const WeightJob j = jobs[blockIdx.y];
+  const float *W = j.W;
+  bf16 *Wt = j.Wt, *Wd = j.Wd;
+  const int Cout = j.Cout, Cin = j.Cin, taps = j.taps, Kp = j.Kp, Kpd = j.Kpd;
   const int n = Cout * Kp;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     Wt[i] = __float2bfloat16_rn(W[i]);
@@ -758,6 +788,7 @@ struct lbm_sg {
   float *ds_x = nullptr, *ds_y = nullptr, *ds_m = nullptr;
   int ds_count = 0;
   int *d_err = nullptr;  // set by a tcgen05 kernel whose bounded wait gave up
+  void *d_wjobs = nullptr;  // k_weights' per-layer jobs (one launch refreshes every layer)
 };
 
 namespace {
@@ -1075,8 +1106,8 @@ lbm_status gemm(lbm_sg *s, int epi, const bf16 *A, const bf16 *Bt, int M, int N,
 }
 
 void refresh_weights(lbm_sg *s) {
-  for (const Conv &c : s->conv)
-    k_weights<<<64, 256, 0, s->stream>>>(s->w + c.woff, c.Wt, c.Wd, c.cout, c.cin, c.taps, c.Kp, c.Kpd);
+  k_weights<<<dim3(64, (unsigned)s->conv.size()), 256, 0, s->stream>>>(
+      (const WeightJob *)s->d_wjobs);
 }
 
 // The implicit im2col needs every 16-byte chunk inside one tap.
@@ -1239,6 +1270,8 @@ lbm_status loss_grads(lbm_sg *s, int B, double *loss_out) {
   if (st != LBM_OK) return st;
   cudaMemsetAsync(s->g, 0, s->nparam * sizeof(float), s->stream);
   cudaMemsetAsync(s->loss, 0, 3 * sizeof(double), s->stream);  // loss, mask sum, block count
+  if (P * c.out_channels >= (1ull << 31))
+    return fail(LBM_INVALID, "surrogate: batch x height x width x outputs must stay below 2^31");
   k_mask_sum<<<grid_for(P), 256, 0, s->stream>>>(s->msk, P, s->loss + 1);
   k_mse<<<grid_for(P * c.out_channels), 256, 0, s->stream>>>(s->act[A_OUT].x, s->tgt, s->msk, s->act[A_OUT].dx, P,
                                                            c.out_channels, s->loss + 1, s->loss);
@@ -1374,6 +1407,17 @@ lbm_status lbm_sg_create(const lbm_sg_config *cfg, lbm_sg **out) {
                      "(tcgen05, one row segment per halo-tile block)"));
   if ((st = salloc(s, &s->d_err, 1)) != LBM_OK) return bail(st);
   cudaMemset(s->d_err, 0, sizeof(int));
+  {
+    std::vector<WeightJob> jobs;
+    for (const Conv &c : s->conv)
+      jobs.push_back(WeightJob{s->w + c.woff, c.Wt, c.Wd, c.cout, c.cin, c.taps, c.Kp, c.Kpd});
+    WeightJob *d = nullptr;
+    if ((st = salloc(s, &d, jobs.size())) != LBM_OK) return bail(st);
+    if (cudaMemcpy(d, jobs.data(), jobs.size() * sizeof(WeightJob), cudaMemcpyHostToDevice) !=
+        cudaSuccess)
+      return bail(fail(LBM_CUDA, "surrogate: upload of the weight jobs failed"));
+    s->d_wjobs = d;
+  }
   if (cfg->coarse_weight > 0.f) {
     const size_t nb = (size_t)B * (H / cfg->coarse_block) * (W / cfg->coarse_block);
     if ((st = salloc(s, &s->coarse_d, nb * co)) || (st = salloc(s, &s->coarse_w, nb))) return bail(st);

@@ -751,6 +751,9 @@ namespace {
 
 int rup(int x, int a) { return (x + a - 1) / a * a; }
 int grid_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 32); }
+// Reductions into one address: two blocks per SM, so that the per-block adds
+// (which serialise on that address) stay few.
+int grid_sum(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 2); }
 
 struct Conv {
   int cin, cout, taps, Kp, Kpd;
@@ -1145,7 +1148,7 @@ lbm_status conv_bwd(lbm_sg *s, int li, int xi, int yi, int B, bool need_dx) {
   } else {
     if (c.cout > 8) return fail(LBM_INVALID, "surrogate: output channels must be <= 8 or a multiple of 8");
     if (c.relu) k_relu_back<<<grid_for(ny), 256, 0, s->stream>>>(Y.dx, Y.x, ny);
-    k_bias_grad<<<grid_for((size_t)M), 256, 0, s->stream>>>(Y.dx, s->g + c.boff, (size_t)M, c.cout);
+    k_bias_grad<<<grid_sum((size_t)M), 256, 0, s->stream>>>(Y.dx, s->g + c.boff, (size_t)M, c.cout);
   }
   lbm_status st = LBM_OK;
   bool halo_done = false;
@@ -1272,8 +1275,8 @@ lbm_status loss_grads(lbm_sg *s, int B, double *loss_out) {
   cudaMemsetAsync(s->loss, 0, 3 * sizeof(double), s->stream);  // loss, mask sum, block count
   if (P * c.out_channels >= (1ull << 31))
     return fail(LBM_INVALID, "surrogate: batch x height x width x outputs must stay below 2^31");
-  k_mask_sum<<<grid_for(P), 256, 0, s->stream>>>(s->msk, P, s->loss + 1);
-  k_mse<<<grid_for(P * c.out_channels), 256, 0, s->stream>>>(s->act[A_OUT].x, s->tgt, s->msk, s->act[A_OUT].dx, P,
+  k_mask_sum<<<grid_sum(P), 256, 0, s->stream>>>(s->msk, P, s->loss + 1);
+  k_mse<<<grid_sum(P * c.out_channels), 256, 0, s->stream>>>(s->act[A_OUT].x, s->tgt, s->msk, s->act[A_OUT].dx, P,
                                                            c.out_channels, s->loss + 1, s->loss);
   if (c.coarse_weight > 0.f) {
     const int sb = c.coarse_block, nbc = B * (c.height / sb) * (c.width / sb) * c.out_channels;

@@ -335,6 +335,9 @@ def timed_steps(torch, dev, stream, solver, steps, check_every, local=0, clocks=
     return ev0.elapsed_time(ev1), (clk.summary() if clk else None)
 
 
+E2E_PASSES = 3  # timed end-to-end passes; the median is reported
+
+
 def run_gpu(args):
     import torch
 
@@ -391,30 +394,35 @@ def run_gpu(args):
         solver.step(1, 1)
         assert solver.L.lbm_get_fields(solver.h, rho_o.ctypes.data, u_o.ctypes.data,
                                        v_o.ctypes.data, None, None) == 0
-        barrier(ws)
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        solver.set_state(None, rho_h.numpy(), u_h.numpy(), v_h.numpy())
-        t1 = time.perf_counter()
-        for i in range(args.steps):
-            res_h[i] = solver.step(1, 1)[0]
-        t2 = time.perf_counter()
-        out = solver.L.lbm_get_fields(solver.h, rho_o.ctypes.data, u_o.ctypes.data,
-                                      v_o.ctypes.data, None, None)
-        torch.cuda.synchronize(dev)
-        t3 = time.perf_counter()
-        el = t3 - t0
-        assert out == 0
-        el = max_over_ranks(ws, el, dev)
+        # three timed passes, the median reported: the host link of a shared
+        # box is occasionally slower for one pass (set_state 33 ms in most
+        # passes, up to 128 ms in a few)
+        passes = []
+        for _ in range(E2E_PASSES):
+            barrier(ws)
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            solver.set_state(None, rho_h.numpy(), u_h.numpy(), v_h.numpy())
+            t1 = time.perf_counter()
+            for i in range(args.steps):
+                res_h[i] = solver.step(1, 1)[0]
+            t2 = time.perf_counter()
+            out = solver.L.lbm_get_fields(solver.h, rho_o.ctypes.data, u_o.ctypes.data,
+                                          v_o.ctypes.data, None, None)
+            torch.cuda.synchronize(dev)
+            t3 = time.perf_counter()
+            assert out == 0
+            passes.append((max_over_ranks(ws, t3 - t0, dev), t1 - t0, t2 - t1, t3 - t2))
+        el, p1, p2, p3 = sorted(passes)[len(passes) // 2]
         e2e = {"value": round(ws * N * args.steps / el / 1e6, 1), "unit": "MLUPS",
                "h2d_bytes_per_step": int(3 * 8 * N / args.steps),
                "d2h_bytes_per_step": int(32 + 3 * 8 * N / args.steps),
                "what": "lbm_set_state(host rho,u,v) + steps x lbm_step(1, residual line) + "
-                       "lbm_get_fields(host rho,u,v), wall clock, after one untimed pass of "
-                       "the same calls",
-               "phases_ms": {"set_state": round((t1 - t0) * 1e3, 2),
-                             "steps": round((t2 - t1) * 1e3, 2),
-                             "get_fields": round((t3 - t2) * 1e3, 2)}}
+                       "lbm_get_fields(host rho,u,v), wall clock, median of "
+                       f"{E2E_PASSES} passes after one untimed pass of the same calls",
+               "phases_ms": {"set_state": round(p1 * 1e3, 2), "steps": round(p2 * 1e3, 2),
+                             "get_fields": round(p3 * 1e3, 2)},
+               "passes_ms": [round(q[0] * 1e3, 1) for q in passes]}
     solver.close()
 
     variants = {}

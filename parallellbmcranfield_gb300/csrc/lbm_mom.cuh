@@ -512,11 +512,13 @@ __device__ __forceinline__ void mom_collide_store2(const StepArgs &a, char *p16,
 // destination row r+1, c_y = 0 to row r and c_y = -1 to row r-1, which is
 // then complete: it collides and stores (class-1 nodes only; class 2 and 3
 // belong to k_special_mom, solid nodes are never written).  The raw words of
-// source rows are loaded two rows ahead into a ring of three, and lanes 0..21
-// prefetch the warp's span of row r + MOM_PF into L2 (a hint: nothing waits
-// for it, every prefetched address lies inside the row).  Rows are addressed
-// by one pointer per thread and row (the chunked layout), each value at an
-// immediate offset from it.
+// source rows are loaded one or two rows ahead (LD) into a ring of three,
+// from addresses clamped into the domain, and lanes 0..23 prefetch the
+// warp's span of row r + MOM_PF and its class bytes into L2 (a hint: nothing
+// waits for it, every prefetched address lies inside the row).  Rows are
+// addressed by one pointer per thread and row (the chunked layout), each
+// value at an immediate offset from it.  Every lane runs the collision and
+// the encoding; only the nodes a lane owns are stored.
 // The row walk is a loop over groups of three rows, the period of the ring
 // and of the three population rows, so that the code stays small.
 constexpr int MOM_PF = 6;

@@ -9,6 +9,9 @@
 * The folded-constant operator of the two-node 16-bit kernel
   (collide_mrt_pair_raw: raw stored values in and out) equals the
   deviation-form one.
+* The moment storage's bulk step (lbm_mom.cuh): its decode with folded
+  constants is the reference transform's inverse, and its collision folded
+  into the encoding is the reference's MRT relaxation.
 Each is restated here in float64 from its source."""
 import numpy as np
 
@@ -172,3 +175,93 @@ def test_folded_raw_operator_equals_deviation_operator():
                 s = d / (C36W[:, None] * u0)
                 got = mrt_raw(s, rho0, om, u0) * (C36W[:, None] * u0)
                 assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+# ---- moment storage (LBM_FP16NEQ): parallellbmcranfield_gb300/csrc/lbm_mom.cuh
+# A node's stored set is r = rho - rho0, j = (x, y) and six non-equilibrium
+# moments n_i (stored units: n_i = S (m_i - b_i), S = 4096) of the rows 1, 2,
+# 4, 6, 7, 8 of the reference's transform applied to d_k = f_k - w_k rho0;
+# b_1 = -2 r + 3 |j|^2, b_2 = r - 3 |j|^2, b_4 = -x, b_6 = -y,
+# b_7 = (x^2 - y^2) / rho0, b_8 = x y / rho0.
+MOM_S = 4096.0
+
+
+def mom_refs(r, x, y, rho0):
+    jj = x * x + y * y
+    return np.array([-2 * r + 3 * jj, r - 3 * jj, -x, -y, (x * x - y * y) / rho0, x * y / rho0])
+
+
+def mom_decode_folded(r, x, y, n, rho0):
+    """mom_decode2: populations of a stored set with the 1/36 of the inverse
+    transform and the storage scale folded into the constants."""
+    s = 1 / MOM_S
+    yy = y * y
+    jj = x * x + yy
+    xmy = jj - 2 * yy
+    i4 = 0.25 / rho0
+    dg = n[1] * (s / 36) + (n[0] * (2 * s / 36) + (jj / 12 + r / 36))
+    Q = n[5] * (s / 4) + x * y * i4
+    Xd, Yd = n[2] * (s / 12) + x / 12, n[3] * (s / 12) + y / 12
+    gp, gm, sp, sm = dg + Q, dg - Q, Xd + Yd, Xd - Yd
+    d5, d6, d7, d8 = gp + sp, gm - sm, gp - sp, gm + sm
+    ax = n[1] * (-2 * s / 36) + (n[0] * (-s / 36) + (jj * 3 / 36 + r * 4 / 36))
+    P = n[4] * (s / 4) + xmy * i4
+    s13, s24 = ax + P, ax - P
+    e57, e86 = d5 - d7, d8 - d6
+    dx, dy = x - (e57 + e86), y - (e57 - e86)
+    d1, d3, d2, d4 = 0.5 * dx + s13, -0.5 * dx + s13, 0.5 * dy + s24, -0.5 * dy + s24
+    d0 = r - (((d1 + d3) + (d2 + d4)) + ((d5 + d7) + (d6 + d8)))
+    return np.array([d0, d1, d2, d3, d4, d5, d6, d7, d8])
+
+
+def test_moment_decode_is_the_inverse_transform():
+    """The folded decode returns Minv m for m = (r, b_1 + n_1/S, b_2 + n_2/S, x,
+    b_4 + n_4/S, y, b_6 + n_6/S, b_7 + n_7/S, b_8 + n_8/S)."""
+    rng = np.random.default_rng(21)
+    Minv = np.linalg.inv(TM)
+    for rho0 in (1.0, 5.0):
+        r = rho0 * rng.normal(0, 0.02, 300)
+        x, y = rho0 * rng.normal(0, 0.05, (2, 300))
+        n = MOM_S * rho0 * rng.normal(0, 1e-3, (6, 300))
+        b = mom_refs(r, x, y, rho0)
+        m = b + n / MOM_S
+        mv = np.array([r, m[0], m[1], x, m[2], y, m[3], m[4], m[5]])
+        ref = Minv @ mv
+        got = mom_decode_folded(r, x, y, n, rho0)
+        assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+        # and the transform of the decoded populations gives the set back
+        back = TM @ got
+        assert np.abs(back[[0, 3, 5]] - np.array([r, x, y])).max() <= 1e-13 * rho0
+
+
+def test_moment_collision_folded_into_the_encoding():
+    """mom_collide_store2: n_i = S (1 - s_i) m_i + S s_i e_i - S b_i equals
+    S (m_i - s_i (m_i - e_i) - b_i), the reference's MRT relaxation of the pulled
+    moments (serial/CellFunctions.c:401-438: rates 1.4, 1.4, 1.2, 1.2, omega,
+    omega; e_1 = -2 r + 3 |j|^2, e_2 = r - 3 |j|^2, e_4 = -x, e_6 = -y,
+    e_7 = (x^2 - y^2) / rho, e_8 = x y / rho) stored against the references of
+    the (rounded) stored r, j; checked against the moment-space operator of
+    mrt_reference on f = d + w rho0."""
+    rng = np.random.default_rng(22)
+    w = C36W / 36
+    for rho0 in (1.0, 2.5):
+        for om in (1.9, 1.3):
+            d = w[:, None] * rho0 * rng.normal(0, 0.3, (9, 400))
+            mom = TM @ d  # pulled moments of the deviations
+            r, x, y = mom[0], mom[3], mom[5]
+            m = mom[[1, 2, 4, 6, 7, 8]]
+            rho = rho0 + r
+            jj = x * x + y * y
+            e = np.array([-2 * r + 3 * jj, r - 3 * jj, -x, -y, (x * x - y * y) / rho, x * y / rho])
+            s = np.array([1.4, 1.4, 1.2, 1.2, om, om])[:, None]
+            # the stored r, j after rounding to the 24-bit grid
+            rq = np.round(r * 2 ** 24) / 2 ** 24
+            xq, yq = np.round(x * 2 ** 25) / 2 ** 25, np.round(y * 2 ** 25) / 2 ** 25
+            b = mom_refs(rq, xq, yq, rho0)
+            folded = MOM_S * (1 - s) * m + MOM_S * s * e - MOM_S * b
+            direct = MOM_S * (m - s * (m - e) - b)
+            assert np.abs(folded - direct).max() <= 1e-10 * np.abs(direct).max()
+            # the post-collision moments are the reference operator's
+            f = d + w[:, None] * rho0
+            post = TM @ (mrt_reference(f, om) - w[:, None] * rho0)
+            assert np.abs(post[[1, 2, 4, 6, 7, 8]] - (m - s * (m - e))).max() <= 1e-12 * rho0

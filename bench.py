@@ -117,6 +117,12 @@ def job_mlups(ws, nodes, steps, ms_max):
     return ws * nodes * steps / (ms_max / 1e3) / 1e6
 
 
+def median_pass(passes):
+    """The median of the timed end-to-end passes, each (job time over ranks,
+    set_state, steps, get_fields) in seconds: the middle one by job time."""
+    return sorted(passes)[len(passes) // 2]
+
+
 def max_over_ranks(ws, x, device):
     if ws == 1:
         return x
@@ -413,7 +419,7 @@ def run_gpu(args):
             t3 = time.perf_counter()
             assert out == 0
             passes.append((max_over_ranks(ws, t3 - t0, dev), t1 - t0, t2 - t1, t3 - t2))
-        el, p1, p2, p3 = sorted(passes)[len(passes) // 2]
+        el, p1, p2, p3 = median_pass(passes)
         e2e = {"value": round(ws * N * args.steps / el / 1e6, 1), "unit": "MLUPS",
                "h2d_bytes_per_step": int(3 * 8 * N / args.steps),
                "d2h_bytes_per_step": int(32 + 3 * 8 * N / args.steps),

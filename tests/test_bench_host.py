@@ -60,3 +60,12 @@ def test_reference_arm_loads_no_gpu_library():
 def test_host_info():
     h = bench.host_info()
     assert h["nproc"] == os.cpu_count() and isinstance(h["cpu_model"], str)
+
+
+def test_e2e_median_pass():
+    """The end-to-end figure is the middle one of the timed passes by job time,
+    with that pass's phases (one slow pass on a shared host link does not set it)."""
+    passes = [(0.132, 0.033, 0.059, 0.040), (0.228, 0.128, 0.060, 0.040), (0.131, 0.033, 0.058, 0.040)]
+    assert bench.median_pass(passes) == passes[0]
+    assert bench.median_pass(passes[:1]) == passes[0]
+    assert bench.E2E_PASSES >= 3 and bench.E2E_PASSES % 2 == 1
